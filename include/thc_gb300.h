@@ -1,0 +1,132 @@
+/*
+ * thc_gb300.h -- C ABI of the GB300 ISDF library (libthc_gb300.so).
+ *
+ * Plain pointers and sizes only.  Every array argument may be a host pointer or a
+ * device pointer of the context's device; the library detects which with
+ * cudaPointerGetAttributes, copies host inputs to the device and writes outputs back
+ * to wherever the output pointer lives.  Nothing here frees caller memory.  All entry
+ * points return a status (THC_OK = 0) and never exit the process.
+ *
+ * The entry points replace the arithmetic behind thcpp's C++ solver classes:
+ *
+ *   thc_kmeans_initial_indices  KMeansSolver::guess_initial_centroids
+ *                               (src/kmeans.cpp:159-175)
+ *   thc_kmeans                  KMeansSolver::kernel (src/kmeans.cpp:187-264) with
+ *                               classify_grid_points (:88-106), update_centroids
+ *                               (:108-144), normed_difference
+ *                               (src/matrix_operations.h:42-57) and map_to_grid (:146-157)
+ *   thc_isdf                    IVecs::IVecs + IVecs::kernel
+ *                               (src/interpolating_vectors.cpp:17-57, :406-455):
+ *                               setup_pseudo_dm/setup_CZt (:59-141), setup_CCt (:163-190),
+ *                               least_squares (:416), fft_vectors (:331-404),
+ *                               construct_muv (:247-281), dump_thc_data's Cholesky (:283-315)
+ *
+ * Threading: calls on distinct contexts may run concurrently from different host
+ * threads; one context must not be used by two threads at once.
+ */
+#ifndef THC_GB300_H
+#define THC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define THC_OK                0
+#define THC_ERR_ARG           1  /* invalid argument (sizes, null pointers, max_it < 1) */
+#define THC_ERR_CUDA          2  /* CUDA runtime error (message in thc_ctx_last_error)  */
+#define THC_ERR_EMPTY_CLUSTER 3  /* a k-means centroid weight fell below 1e-8
+                                    (the reference exits: src/kmeans.cpp:131-143)        */
+#define THC_ERR_NOT_PD        4  /* Cholesky of M failed; the info field holds the
+                                    1-based leading minor (the reference prints it and
+                                    still writes Luv: src/interpolating_vectors.cpp:296-304) */
+#define THC_ERR_SHAPE         5  /* mesh product != N_g, or sizes above the limits     */
+#define THC_ERR_IO            6  /* file I/O (host tools only)                          */
+#define THC_ERR_TIMEOUT       7  /* a bounded device wait gave up                       */
+#define THC_ERR_NOMEM         8  /* device allocation failed                            */
+#define THC_ERR_CUFFT         9  /* cuFFT plan or execution failed                      */
+
+/* Arithmetic of a context. */
+#define THC_PREC_FP64  0  /* all-FP64: the drop-in path                                  */
+#define THC_PREC_MIXED 1  /* FP32 k-means assign + FP64 recheck, sliced-BF16 tensor-core
+                             GEMMs, FP32 FFT, FP64 Cholesky of C and of M               */
+
+typedef struct thc_ctx thc_ctx;
+
+typedef struct thc_kmeans_stats {
+  int iterations;          /* completed k-means iterations                               */
+  int converged;           /* 1 if the normed difference fell below the threshold        */
+  int zero_filled;         /* 1 if the last difference neither fell below nor rose above
+                              the threshold (the reference then leaves the indices 0)    */
+  int duplicates;          /* repeated indices after sorting (the reference warns)       */
+  double final_diff;       /* last normed difference                                     */
+  double pct_changed;      /* % of grid points whose label changed in the last iteration */
+  long long rechecked;     /* points resolved by the FP64 recheck (mixed precision)      */
+  double device_ms;        /* device time of the call                                    */
+} thc_kmeans_stats;
+
+typedef struct thc_isdf_stats {
+  int chol_c_info;         /* 0, or 1-based pivot at which Cholesky of C broke down with no
+                              shift (before the shift retry)                             */
+  int chol_m_info;         /* 0, or 1-based leading minor of M that is not positive      */
+  int rank_deficient;      /* 1 if C needed the diagonal shift                           */
+  int n_anti;              /* half-spectrum points where v(G) != v(-G)                   */
+  double shift_used;       /* absolute diagonal shift added to C                         */
+  double c_min_pivot;      /* min / max squared Cholesky pivot of C (cond estimate^-1)   */
+  double device_ms;        /* device time of the call                                    */
+} thc_isdf_stats;
+
+/* Context lifetime.  `precision` is THC_PREC_FP64 or THC_PREC_MIXED. */
+int thc_ctx_create(int device, int precision, thc_ctx** out_ctx);
+int thc_ctx_destroy(thc_ctx* ctx);
+/* Run on a caller stream (a cudaStream_t); NULL restores the context's own stream. */
+int thc_ctx_set_stream(thc_ctx* ctx, void* cuda_stream);
+/* Named numeric options: "slices_p", "slices_z" (sliced-GEMM depths, mixed path). */
+int thc_ctx_set_option(thc_ctx* ctx, const char* key, double value);
+const char* thc_ctx_last_error(const thc_ctx* ctx);
+const char* thc_status_string(int status);
+/* Number of kernels this context has launched so far (its own kernels only). */
+long long thc_ctx_kernel_launches(const thc_ctx* ctx);
+
+/*
+ * Initial interpolating-point indices (host only): iota(0..ng-1) shuffled by
+ * std::shuffle with std::mt19937(seed), the first nmu kept and sorted ascending.
+ */
+int thc_kmeans_initial_indices(long long ng, int nmu, unsigned int seed, int* out_idx);
+
+/*
+ * Density-weighted k-means at the semantics of one MPI rank of the reference.
+ *   grid      ng x 3 doubles, C order (the `real_space_grid` dataset)
+ *   rho       ng doubles (the `density` / `density_occ` dataset)
+ *   init_idx  nmu initial grid indices (from thc_kmeans_initial_indices)
+ *   out_idx   nmu sorted interpolating-point indices (bit-identical to the reference)
+ *   stats     optional
+ * Returns THC_ERR_EMPTY_CLUSTER where the reference exits.
+ */
+int thc_kmeans(thc_ctx* ctx, const double* grid, const double* rho, long long ng, int nmu,
+               const int* init_idx, int max_it, double threshold, int* out_idx,
+               thc_kmeans_stats* stats);
+
+/*
+ * ISDF interpolating vectors + FFT Coulomb matrix + its Cholesky factor.
+ *   phi           ng x norb doubles, C order: the real part of `aoR` (real orbitals)
+ *   idx           nmu grid indices (the k-means output)
+ *   mesh          3 ints, n0*n1*n2 == ng (the `fft_grid` dataset)
+ *   coulG         ng doubles (the `fft_coulomb` dataset)
+ *   shift_rel     < 0: automatic (no shift unless Cholesky of C breaks down, then
+ *                 1e-10 * tr(C)/nmu); >= 0: shift = shift_rel * tr(C)/nmu always
+ *   out_orbitals  norb x nmu x 2 doubles: `/Hamiltonian/THC/Orbitals` (may be NULL)
+ *   out_M         nmu x nmu x 2 doubles: the full Hermitian Coulomb matrix M (may be NULL)
+ *   out_L         nmu x nmu x 2 doubles: `/Hamiltonian/THC/Luv`, lower triangle of
+ *                 chol(M), upper triangle zero, C order (may be NULL)
+ * Returns THC_ERR_NOT_PD (after writing all outputs) when Cholesky of M fails, as the
+ * reference prints a warning and still writes Luv.
+ */
+int thc_isdf(thc_ctx* ctx, const double* phi, long long ng, int norb, const int* idx, int nmu,
+             const int* mesh, const double* coulG, double shift_rel, double* out_orbitals,
+             double* out_M, double* out_L, thc_isdf_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* THC_GB300_H */

@@ -1,0 +1,51 @@
+"""Hand-made k-means inputs with constructed ties (shared by CPU and GPU tests)."""
+import math
+
+import numpy as np
+
+
+def sqrt_tie_vectors(s=1.3):
+    """Two offsets v1, v2 with d2(v2) < d2(v1) but sqrt(d2(v1)) == sqrt(d2(v2)).
+
+    d2 is evaluated as the reference does: ((dx*dx + dy*dy) + dz*dz) in IEEE double.
+    A first-index argmin over sqrt values must keep v1 (index 0); an argmin over the
+    squared distances would wrongly pick v2.
+    """
+    def d2(v):
+        return (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]
+
+    v1 = (s, 0.0, 0.0)
+    a1 = d2(v1)
+    r1 = math.sqrt(a1)
+    want = math.nextafter(a1, 0.0)           # the double just below d2(v1)
+    for k in range(1, 4000):
+        a = s * (1.0 - k * 2.0 ** -30)
+        target = want - a * a
+        if target <= 0:
+            continue
+        b = math.sqrt(target)
+        v2 = (a, b, 0.0)
+        a2 = d2(v2)
+        if a2 < a1 and math.sqrt(a2) == r1:
+            return v1, v2
+    raise RuntimeError("no sqrt tie found")
+
+
+def sqrt_tie_grid():
+    """Grid [C0, C1, P0] with P0 at the origin tied (after sqrt) between C0 and C1.
+
+    With initial centroids at grid points 0 and 1, one iteration moves the centroid that
+    captures P0 (weight 10) onto P0; map_to_grid then returns {0 or 1, 2}.
+    """
+    v1, v2 = sqrt_tie_vectors()
+    grid = np.array([v1, v2, (0.0, 0.0, 0.0)], dtype=np.float64)
+    rho = np.array([1.0, 1.0, 10.0])
+    return grid, rho
+
+
+def exact_tie_grid(n=6):
+    """Integer lattice with centroids placed so that many points are exactly equidistant."""
+    ax = np.arange(n, dtype=np.float64)
+    g = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+    rho = 1.0 + 0.01 * np.arange(g.shape[0]) % 7
+    return g, rho

@@ -1,0 +1,110 @@
+"""GPU ISDF through the C ABI against the oracle (FP64 and mixed precision)."""
+import numpy as np
+import pytest
+
+import oracle
+from thcpp_gb300 import capi
+from tests.conftest import system
+
+pytestmark = pytest.mark.gpu
+
+_KM = {}
+
+
+def kmeans_idx(name):
+    if name not in _KM:
+        _KM[name] = oracle.kmeans_system(system(name)).idx
+    return _KM[name]
+
+
+def _cplx(a):
+    return a[..., 0] + 1j * a[..., 1]
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _run(ctx, name, shift=-1.0):
+    s = system(name)
+    idx = kmeans_idx(name)
+    r = ctx.isdf(s.phi, idx, s.mesh, s.coulG, shift)
+    return s, idx, r
+
+
+# (config, FP64 tolerance, mixed tolerance) on ||dM||/||M|| against the oracle
+CASES = [("tiny", 1e-8, 1e-6), ("c2", 1e-9, 1e-6)]
+
+
+@pytest.mark.parametrize("name,tol64,tolmx", CASES)
+def test_isdf_fp64_matches_oracle(gpu_ctx_fp64, name, tol64, tolmx):
+    s, idx, r = _run(gpu_ctx_fp64, name)
+    assert r["status"] == 0
+    ref = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG)
+    M = _cplx(r["M"])
+    assert _rel(M, ref["M"]) < tol64
+    L = _cplx(r["L"])
+    assert np.allclose(np.triu(L, 1), 0)
+    assert _rel(L @ L.conj().T, M) < 1e-12
+    orb = _cplx(r["orbitals"])
+    assert np.array_equal(orb.real, s.phi[idx].T) and not orb.imag.any()
+    assert r["stats"].rank_deficient == 0 and r["stats"].n_anti == 0
+
+
+@pytest.mark.parametrize("name,tol64,tolmx", CASES)
+def test_isdf_mixed_matches_oracle(gpu_ctx_mixed, name, tol64, tolmx):
+    s, idx, r = _run(gpu_ctx_mixed, name)
+    assert r["status"] == 0
+    ref = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG)
+    M = _cplx(r["M"])
+    err = _rel(M, ref["M"])
+    print(f"{name}: mixed ||dM||/||M|| = {err:.3e}")
+    assert err < tolmx
+    L = _cplx(r["L"])
+    assert _rel(L @ L.conj().T, M) < 1e-12
+
+
+def test_isdf_fp64_vs_reference_qr_c2(gpu_ctx_fp64):
+    """Against the literal complex restatement (zgels QR, C2C FFT, herk, zpotrf)."""
+    s, idx, r = _run(gpu_ctx_fp64, "c2")
+    ref = oracle.isdf_reference(s.phi, idx, s.mesh, s.coulG)
+    assert _rel(_cplx(r["M"]), ref["M"]) < 1e-9
+    assert _rel(_cplx(r["L"]), ref["L"]) < 1e-8
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_isdf_rank_deficient_c1(request, prec):
+    ctx = request.getfixturevalue("gpu_ctx_fp64" if prec == "fp64" else "gpu_ctx_mixed")
+    s, idx, r = _run(ctx, "c1")
+    st = r["stats"]
+    assert st.rank_deficient == 1 and st.chol_c_info > 0 and st.n_anti > 0
+    pm = s.phi[idx]
+    tr = np.trace((pm @ pm.T) ** 2) / s.nmu
+    assert abs(st.shift_used - 1e-10 * tr) < 1e-12 * tr
+    ref = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG, shift=1e-10 * tr)
+    M = _cplx(r["M"])
+    err = _rel(M, ref["M"])
+    print(f"c1 {prec}: ||dM||/||M|| = {err:.3e}")
+    assert err < 1e-6
+    pairs = [(i, j) for i in range(s.norb) for j in range(i, s.norb)]
+    ex = oracle.pair_coulomb_exact(s.phi, s.mesh, s.coulG, pairs)
+    th = oracle.thc_pair_coulomb(s.phi, idx, M, pairs)
+    assert _rel(th, ex) < 1e-5
+
+
+def test_isdf_mesh_mismatch(gpu_ctx_fp64):
+    s = system("tiny")
+    r = gpu_ctx_fp64.isdf(s.phi, kmeans_idx("tiny"), (16, 16, 15), s.coulG, raise_on_error=False)
+    assert r["status"] == capi.THC_ERR_SHAPE
+
+
+def test_isdf_device_pointers(gpu_ctx_mixed):
+    import torch
+    s = system("tiny")
+    idx = kmeans_idx("tiny")
+    host = gpu_ctx_mixed.isdf(s.phi, idx, s.mesh, s.coulG)
+    dev_M = torch.zeros((s.nmu, s.nmu, 2), dtype=torch.float64, device="cuda")
+    gpu_ctx_mixed.isdf(torch.from_numpy(s.phi).cuda(), torch.from_numpy(idx).cuda(), s.mesh,
+                       torch.from_numpy(s.coulG).cuda(), out_M=dev_M, want=("M",))
+    torch.cuda.synchronize()
+    assert np.array_equal(dev_M.cpu().numpy(), host["M"])

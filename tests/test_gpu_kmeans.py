@@ -1,0 +1,90 @@
+"""GPU k-means through the C ABI: bit-identical to the oracle (one rank of the reference)."""
+import numpy as np
+import pytest
+
+import oracle
+from thcpp_gb300 import capi
+from tests import kmeans_cases
+from tests.conftest import system
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(request, prec):
+    return request.getfixturevalue("gpu_ctx_fp64" if prec == "fp64" else "gpu_ctx_mixed")
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["tiny", "c1", "c2"])
+def test_kmeans_bit_exact(request, name, prec):
+    s = system(name)
+    ref = oracle.kmeans_system(s)
+    ctx = _ctx(request, prec)
+    init = capi.initial_indices(s.ng, s.nmu, s.rng_seed)
+    idx, st, status = ctx.kmeans(s.grid, s.density, s.nmu, init, s.max_it, s.threshold)
+    assert status == 0
+    assert np.array_equal(idx, ref.idx)
+    assert st.iterations == ref.iters
+    assert st.final_diff == ref.diff          # bit-identical normed difference
+    assert st.converged == (ref.diff < s.threshold)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_kmeans_sqrt_tie(request, prec):
+    grid, rho = kmeans_cases.sqrt_tie_grid()
+    init = np.array([0, 1], np.int32)
+    ref = oracle.kmeans(grid, rho, 2, init, 1, 0.0)
+    idx, st, status = _ctx(request, prec).kmeans(grid, rho, 2, init, 1, 0.0)
+    assert status == 0 and ref.status == 0
+    assert np.array_equal(idx, ref.idx)
+    assert list(idx) == [1, 2]                # P0 joined centroid 0 (first index)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_kmeans_exact_ties(request, prec):
+    g, rho = kmeans_cases.exact_tie_grid(8)
+    init = oracle.initial_indices(g.shape[0], 12, 5)
+    ref = oracle.kmeans(g, rho, 12, init, 50, 1e-12)
+    idx, st, status = _ctx(request, prec).kmeans(g, rho, 12, init, 50, 1e-12)
+    assert status == 0 and np.array_equal(idx, ref.idx) and st.iterations == ref.iters
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_kmeans_empty_cluster(request, prec):
+    grid = np.array([[0.0, 0, 0], [1.0, 0, 0], [5.0, 0, 0]])
+    rho = np.array([1.0, 1.0, 0.0])
+    _, _, status = _ctx(request, prec).kmeans(grid, rho, 3, np.array([0, 1, 2], np.int32), 5,
+                                               1e-9, raise_on_error=False)
+    assert status == capi.THC_ERR_EMPTY_CLUSTER
+
+
+def test_kmeans_zero_filled_when_diff_equals_threshold(gpu_ctx_fp64):
+    s = system("tiny")
+    init = capi.initial_indices(s.ng, s.nmu, s.rng_seed)
+    _, st, _ = gpu_ctx_fp64.kmeans(s.grid, s.density, s.nmu, init, 5, 0.0)
+    d = st.final_diff
+    ref = oracle.kmeans(s.grid, s.density, s.nmu, init, 5, d)
+    idx, st2, status = gpu_ctx_fp64.kmeans(s.grid, s.density, s.nmu, init, 5, d)
+    assert status == 0 and st2.zero_filled == 1
+    assert np.array_equal(idx, ref.idx) and not idx.any()
+
+
+def test_kmeans_device_pointers(gpu_ctx_mixed):
+    import torch
+    s = system("tiny")
+    ref = oracle.kmeans_system(s)
+    init = capi.initial_indices(s.ng, s.nmu, s.rng_seed)
+    g = torch.from_numpy(s.grid).cuda()
+    r = torch.from_numpy(s.density).cuda()
+    i0 = torch.from_numpy(init).cuda()
+    out = torch.zeros(s.nmu, dtype=torch.int32, device="cuda")
+    gpu_ctx_mixed.kmeans(g, r, s.nmu, i0, s.max_it, s.threshold, out_idx=out)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), ref.idx)
+
+
+def test_kmeans_argument_errors(gpu_ctx_fp64):
+    s = system("tiny")
+    init = capi.initial_indices(s.ng, s.nmu, s.rng_seed)
+    _, _, st = gpu_ctx_fp64.kmeans(s.grid, s.density, s.nmu, init, 0, 1e-6, raise_on_error=False)
+    assert st == capi.THC_ERR_ARG

@@ -1,0 +1,192 @@
+"""CPU tests of the oracle: pure-Python restatements and known-answer tests."""
+import math
+
+import numpy as np
+import pytest
+import scipy.fft as sfft
+
+import oracle
+from thcpp_gb300 import synth
+from tests import kmeans_cases
+
+
+def py_classify(pts, cen):
+    """Loop restatement of classify_grid_points (src/kmeans.cpp:88-106)."""
+    out = []
+    for p in pts:
+        best, arg = None, 0
+        for j, c in enumerate(cen):
+            dx, dy, dz = c[0] - p[0], c[1] - p[1], c[2] - p[2]
+            d = math.sqrt((dx * dx + dy * dy) + dz * dz)
+            if best is None or d < best:
+                best, arg = d, j
+        out.append(arg)
+    return np.array(out)
+
+
+def py_normed_difference(a, b):
+    scale = max(abs(max(a)), abs(min(a))) + max(abs(max(b)), abs(min(b)))
+    diff = 0.0
+    for x, y in zip(a, b):
+        q = (x - y) / scale
+        diff += q * q
+    return scale * math.sqrt(diff)
+
+
+def py_kmeans(grid, rho, init, max_it, thr):
+    """Single-rank loop restatement of KMeansSolver::kernel (src/kmeans.cpp:187-264)."""
+    nmu = len(init)
+    cur = [tuple(grid[i]) for i in init]
+    lab = py_classify(grid, cur)
+    diff = 0.0
+    nxt = None
+    conv = False
+    for it in range(max_it):
+        lab = py_classify(grid, cur)
+        w = [0.0] * nmu
+        s = [[0.0, 0.0, 0.0] for _ in range(nmu)]
+        for i in range(len(grid)):
+            k = lab[i]
+            w[k] += rho[i]
+            for d in range(3):
+                s[k][d] += rho[i] * grid[i][d]
+        if min(w) < 1e-8:
+            return None
+        nxt = [tuple(s[k][d] / w[k] for d in range(3)) for k in range(nmu)]
+        diff = py_normed_difference([x for c in nxt for x in c], [x for c in cur for x in c])
+        if diff < thr:
+            conv = True
+            break
+        cur, nxt = nxt, cur
+    fin = nxt if conv else cur
+    idx = sorted(py_classify(np.array(fin), [tuple(g) for g in grid]))
+    return np.array(idx), it + 1, diff
+
+
+def test_sqrt_tie_keeps_first_index():
+    v1, v2 = kmeans_cases.sqrt_tie_vectors()
+    d1 = (v1[0] * v1[0] + v1[1] * v1[1]) + v1[2] * v1[2]
+    d2 = (v2[0] * v2[0] + v2[1] * v2[1]) + v2[2] * v2[2]
+    assert d2 < d1 and math.sqrt(d1) == math.sqrt(d2)
+    lab = oracle.classify(np.zeros((1, 3)), np.array([v1, v2]))
+    assert lab[0] == 0
+    assert py_classify(np.zeros((1, 3)), [v1, v2])[0] == 0
+
+
+def test_exact_ties_lowest_index():
+    g, _ = kmeans_cases.exact_tie_grid()
+    cen = np.array([[1.0, 1.0, 1.0], [3.0, 1.0, 1.0], [1.0, 3.0, 1.0], [3.0, 3.0, 3.0]])
+    a = oracle.classify(g, cen)
+    b = py_classify(g, cen)
+    assert np.array_equal(a, b)
+    # point (2,1,1) is exactly between centroids 0 and 1
+    i = int(np.nonzero((g == [2.0, 1.0, 1.0]).all(1))[0][0])
+    assert a[i] == 0
+
+
+def test_initial_indices_sorted_unique():
+    idx = oracle.initial_indices(13824, 64, 18)
+    assert np.all(np.diff(idx) > 0) and idx.min() >= 0 and idx.max() < 13824
+
+
+@pytest.mark.parametrize("seed", [0, 3, 11])
+def test_kmeans_oracle_matches_python_loops(seed):
+    rng = np.random.default_rng(seed)
+    grid = rng.uniform(0, 4, size=(60, 3))
+    rho = rng.uniform(0.1, 1.0, size=60)
+    init = oracle.initial_indices(60, 5, seed)
+    r = oracle.kmeans(grid, rho, 5, init, 30, 1e-9, nthreads=1)
+    idx, it, diff = py_kmeans(grid, rho, init, 30, 1e-9)
+    assert r.status == 0
+    assert np.array_equal(r.idx, idx) and r.iters == it and r.diff == diff
+
+
+def test_kmeans_oracle_threads_identical():
+    s = synth.config("tiny")
+    a = oracle.kmeans_system(s, nthreads=1)
+    b = oracle.kmeans_system(s, nthreads=4)
+    assert np.array_equal(a.idx, b.idx) and a.iters == b.iters and a.diff == b.diff
+
+
+def test_kmeans_oracle_empty_cluster():
+    grid = np.array([[0.0, 0, 0], [1.0, 0, 0], [5.0, 0, 0]])
+    rho = np.array([1.0, 1.0, 0.0])          # cluster of point 2 gets zero weight
+    r = oracle.kmeans(grid, rho, 3, np.array([0, 1, 2], np.int32), 5, 1e-9)
+    assert r.status == 2
+
+
+def test_normed_difference_known_answer():
+    a = [1.0, 2.0, 3.0]
+    b = [1.0, 2.0, 5.0]
+    # scale = 3 + 5 = 8; diff = sqrt((2/8)^2) * 8 = 2
+    assert py_normed_difference(a, b) == 2.0
+
+
+def test_fft_delta_and_plane_wave():
+    mesh = (6, 5, 8)
+    f = np.zeros(mesh)
+    f[0, 0, 0] = 1.0
+    assert np.allclose(sfft.fftn(f), 1.0)
+    k = (1, 2, 3)
+    idx = np.indices(mesh)
+    pw = np.exp(2j * np.pi * sum(k[d] * idx[d] / mesh[d] for d in range(3)))
+    F = sfft.fftn(pw)                         # FFTW_FORWARD: exp(-i ...) kernel
+    assert abs(F[k] - np.prod(mesh)) < 1e-9
+    F[k] = 0
+    assert np.abs(F).max() < 1e-9
+
+
+def test_coulomb_plane_wave_energy():
+    """sum_G v(G) |rho_hat|^2 = Omega * 4 pi / (2 |G0|^2) for rho = cos(G0 . r)."""
+    s = synth.config("tiny")
+    lat = s.lattice
+    g0 = 2 * np.pi * np.linalg.inv(lat).T[0]       # b_0
+    rho = np.cos(s.grid @ g0)
+    rh = sfft.fftn(rho.reshape(s.mesh)).reshape(-1)
+    e = np.sum(s.coulG * np.abs(rh) ** 2)
+    expect = s.volume * 4 * np.pi / (2 * g0 @ g0)
+    assert abs(e - expect) < 1e-10 * expect
+
+
+def test_half_spectrum_matches_full_c2c_nonorthogonal():
+    """The real-form M (R2C, v_sym / v_anti) equals the complex C2C sum for any v."""
+    rng = np.random.default_rng(1)
+    mesh = (6, 4, 6)
+    lat = np.array([[0.0, 1.0, 1.0], [1.0, 0.0, 1.0], [1.0, 1.0, 0.0]]) * 2.0
+    v = synth.coulomb_g(lat, mesh)
+    dsym, danti = oracle.half_spectrum_weights(v, mesh)
+    assert np.count_nonzero(danti) > 0
+    z = rng.standard_normal((3, int(np.prod(mesh))))
+    zh_full = sfft.fftn(z.reshape(3, *mesh), axes=(1, 2, 3)).reshape(3, -1)
+    Mfull = (zh_full.conj() * v) @ zh_full.T
+    zh = sfft.rfftn(z.reshape(3, *mesh), axes=(1, 2, 3)).reshape(3, -1)
+    re, im = zh.real, zh.imag
+    Mre = (re * dsym) @ re.T + (im * dsym) @ im.T
+    Mim = (re * danti) @ im.T - (im * danti) @ re.T
+    assert np.allclose(Mre + 1j * Mim, Mfull, rtol=1e-12, atol=1e-12 * np.abs(Mfull).max())
+
+
+def test_isdf_forms_agree_full_rank():
+    s = synth.config("tiny")
+    km = oracle.kmeans_system(s)
+    a = oracle.isdf_real(s.phi, km.idx, s.mesh, s.coulG)
+    b = oracle.isdf_reference(s.phi, km.idx, s.mesh, s.coulG)
+    rel = np.linalg.norm(a["M"] - b["M"]) / np.linalg.norm(b["M"])
+    # QR and Cholesky solutions differ by ~cond(C) * 1e-16; this C has cond ~1.5e9.
+    assert rel < 1e-7
+    L = a["L"]
+    assert np.linalg.norm(L @ L.conj().T - a["M"]) < 1e-12 * np.linalg.norm(a["M"])
+
+
+def test_thc_reconstructs_pair_coulomb_rank_deficient():
+    """C1 has N_mu = 64 > 36 pair products: C is singular, M is not unique, but the THC
+    reconstruction of the orbital-pair Coulomb integrals is."""
+    s = synth.config("c1")
+    km = oracle.kmeans_system(s)
+    pm = s.phi[km.idx]
+    tr = np.trace((pm @ pm.T) ** 2) / s.nmu
+    r = oracle.isdf_real(s.phi, km.idx, s.mesh, s.coulG, shift=1e-10 * tr)
+    pairs = [(i, j) for i in range(s.norb) for j in range(i, s.norb)]
+    ex = oracle.pair_coulomb_exact(s.phi, s.mesh, s.coulG, pairs)
+    th = oracle.thc_pair_coulomb(s.phi, km.idx, r["M"], pairs)
+    assert np.linalg.norm(th - ex) / np.linalg.norm(ex) < 1e-5

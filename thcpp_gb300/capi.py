@@ -1,0 +1,195 @@
+"""ctypes binding of libthc_gb300.so (the C ABI declared in include/thc_gb300.h).
+
+Arrays may be numpy arrays (host memory: the library copies them to the device) or
+CUDA tensors / any object with ``data_ptr()`` (device memory: used in place).  Loading
+fails loudly when the shared library is missing -- there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+THC_OK = 0
+THC_ERR_ARG = 1
+THC_ERR_CUDA = 2
+THC_ERR_EMPTY_CLUSTER = 3
+THC_ERR_NOT_PD = 4
+THC_ERR_SHAPE = 5
+THC_ERR_IO = 6
+THC_ERR_TIMEOUT = 7
+THC_ERR_NOMEM = 8
+THC_ERR_CUFFT = 9
+
+THC_PREC_FP64 = 0
+THC_PREC_MIXED = 1
+
+# Every symbol include/thc_gb300.h declares.
+EXPORTS = [
+    "thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
+    "thc_ctx_last_error", "thc_status_string", "thc_ctx_kernel_launches",
+    "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf",
+]
+
+
+class KMeansStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int),
+                ("zero_filled", ctypes.c_int), ("duplicates", ctypes.c_int),
+                ("final_diff", ctypes.c_double), ("pct_changed", ctypes.c_double),
+                ("rechecked", ctypes.c_longlong), ("device_ms", ctypes.c_double)]
+
+
+class IsdfStats(ctypes.Structure):
+    _fields_ = [("chol_c_info", ctypes.c_int), ("chol_m_info", ctypes.c_int),
+                ("rank_deficient", ctypes.c_int), ("n_anti", ctypes.c_int),
+                ("shift_used", ctypes.c_double), ("c_min_pivot", ctypes.c_double),
+                ("device_ms", ctypes.c_double)]
+
+
+class ThcError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load libthc_gb300.so; raise if it is absent (unless asked to build it)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing: run `python -c 'import __graft_entry__ as g; "
+                               f"g.build()'` (no CPU fallback exists)")
+        _build.build()
+    lib = ctypes.CDLL(path)
+    vp, ci, cll, cd, cu = (ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double,
+                           ctypes.c_uint)
+    lib.thc_ctx_create.argtypes = [ci, ci, ctypes.POINTER(vp)]
+    lib.thc_ctx_destroy.argtypes = [vp]
+    lib.thc_ctx_set_stream.argtypes = [vp, vp]
+    lib.thc_ctx_set_option.argtypes = [vp, ctypes.c_char_p, cd]
+    lib.thc_ctx_last_error.argtypes = [vp]
+    lib.thc_ctx_last_error.restype = ctypes.c_char_p
+    lib.thc_status_string.argtypes = [ci]
+    lib.thc_status_string.restype = ctypes.c_char_p
+    lib.thc_ctx_kernel_launches.argtypes = [vp]
+    lib.thc_ctx_kernel_launches.restype = cll
+    lib.thc_kmeans_initial_indices.argtypes = [cll, ci, cu, vp]
+    lib.thc_kmeans.argtypes = [vp, vp, vp, cll, ci, vp, ci, cd, vp, ctypes.POINTER(KMeansStats)]
+    lib.thc_isdf.argtypes = [vp, vp, cll, ci, vp, ci, vp, vp, cd, vp, vp, vp,
+                             ctypes.POINTER(IsdfStats)]
+    for f in ("thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
+              "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf"):
+        getattr(lib, f).restype = ci
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("arrays must be C-contiguous")
+        return a.ctypes.data_as(ctypes.c_void_p)
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def initial_indices(ng: int, nmu: int, seed: int) -> np.ndarray:
+    out = np.zeros(nmu, np.int32)
+    st = load().thc_kmeans_initial_indices(ng, nmu, seed, _ptr(out))
+    if st:
+        raise ThcError(st, "thc_kmeans_initial_indices failed")
+    return out
+
+
+class Context:
+    """One GPU context (device, precision, stream, workspace)."""
+
+    def __init__(self, device: int = 0, precision: int = THC_PREC_FP64):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        st = self.lib.thc_ctx_create(device, precision, ctypes.byref(h))
+        if st:
+            raise ThcError(st, "thc_ctx_create failed: "
+                           + self.lib.thc_status_string(st).decode())
+        self.h = h
+        self.precision = precision
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.thc_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, what):
+        if st:
+            raise ThcError(st, f"{what}: {self.lib.thc_ctx_last_error(self.h).decode()}")
+
+    def set_option(self, key: str, value: float):
+        self._check(self.lib.thc_ctx_set_option(self.h, key.encode(), float(value)), key)
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self.lib.thc_ctx_set_stream(self.h, ctypes.c_void_p(stream_ptr or 0)),
+                    "set_stream")
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.lib.thc_ctx_kernel_launches(self.h))
+
+    def kmeans(self, grid, rho, nmu, init_idx, max_it, threshold, out_idx=None,
+               raise_on_error=True):
+        ng = int(grid.shape[0])
+        if out_idx is None:
+            out_idx = np.zeros(nmu, np.int32)
+        stats = KMeansStats()
+        st = self.lib.thc_kmeans(self.h, _ptr(grid), _ptr(rho), ng, nmu, _ptr(init_idx), max_it,
+                                 threshold, _ptr(out_idx), ctypes.byref(stats))
+        if raise_on_error:
+            self._check(st, "thc_kmeans")
+        return out_idx, stats, st
+
+    def isdf(self, phi, idx, mesh, coulG, shift_rel=-1.0, out_orbitals=None, out_M=None,
+             out_L=None, raise_on_error=True, want=("M", "L", "orbitals")):
+        ng, no = int(phi.shape[0]), int(phi.shape[1])
+        nmu = int(idx.shape[0])
+        mesh_a = np.ascontiguousarray(np.asarray(mesh, dtype=np.int32).reshape(3))
+        if out_M is None and "M" in want:
+            out_M = np.zeros((nmu, nmu, 2))
+        if out_L is None and "L" in want:
+            out_L = np.zeros((nmu, nmu, 2))
+        if out_orbitals is None and "orbitals" in want:
+            out_orbitals = np.zeros((no, nmu, 2))
+        stats = IsdfStats()
+        st = self.lib.thc_isdf(self.h, _ptr(phi), ng, no, _ptr(idx), nmu, _ptr(mesh_a),
+                               _ptr(coulG), float(shift_rel), _ptr(out_orbitals), _ptr(out_M),
+                               _ptr(out_L), ctypes.byref(stats))
+        if raise_on_error and st not in (THC_OK, THC_ERR_NOT_PD):
+            self._check(st, "thc_isdf")
+        return dict(M=out_M, L=out_L, orbitals=out_orbitals, stats=stats, status=st)

@@ -1,0 +1,226 @@
+// The C ABI (include/thc_gb300.h): contexts, workspace, residency and dispatch.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <random>
+#include <vector>
+
+#include "common.cuh"
+#include "isdf.cuh"
+
+struct thc_ctx {
+  thc::Ctx c;
+};
+
+namespace thc {
+
+void* ws_get(Ctx* c, Slot s, size_t bytes)
+{
+  if (bytes == 0) bytes = 16;
+  if (c->ws_bytes[s] >= bytes) return c->ws[s];
+  if (c->ws[s]) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->ws[s]);
+    c->ws[s] = nullptr;
+    c->ws_bytes[s] = 0;
+  }
+  size_t want = bytes + bytes / 8;  // headroom so that slightly larger calls reuse it
+  void* p = nullptr;
+  if (cudaMalloc(&p, want) != cudaSuccess) {
+    cudaGetLastError();
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    want = bytes;
+  }
+  c->ws[s] = p;
+  c->ws_bytes[s] = want;
+  return p;
+}
+
+int set_error(Ctx* c, int status, const char* fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->last_error = buf;
+  return status;
+}
+
+int check_launch(Ctx* c, const char* what)
+{
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return set_error(c, THC_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+  return THC_OK;
+}
+
+bool is_device_ptr(const void* p)
+{
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+const void* to_device(Ctx* c, const void* p, size_t bytes, Slot staging, int* status)
+{
+  *status = THC_OK;
+  if (is_device_ptr(p)) return p;
+  void* d = ws_get(c, staging, bytes);
+  if (!d) {
+    *status = set_error(c, THC_ERR_NOMEM, "staging allocation of %zu bytes failed", bytes);
+    return nullptr;
+  }
+  cudaError_t e = cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) {
+    *status = set_error(c, THC_ERR_CUDA, "host-to-device copy failed: %s", cudaGetErrorString(e));
+    return nullptr;
+  }
+  return d;
+}
+
+}  // namespace thc
+
+extern "C" {
+
+const char* thc_status_string(int status)
+{
+  switch (status) {
+    case THC_OK: return "ok";
+    case THC_ERR_ARG: return "invalid argument";
+    case THC_ERR_CUDA: return "CUDA error";
+    case THC_ERR_EMPTY_CLUSTER: return "empty k-means cluster";
+    case THC_ERR_NOT_PD: return "matrix not positive definite";
+    case THC_ERR_SHAPE: return "shape mismatch";
+    case THC_ERR_IO: return "I/O error";
+    case THC_ERR_TIMEOUT: return "device wait timed out";
+    case THC_ERR_NOMEM: return "device allocation failed";
+    case THC_ERR_CUFFT: return "cuFFT error";
+    default: return "unknown status";
+  }
+}
+
+int thc_ctx_create(int device, int precision, thc_ctx** out)
+{
+  if (!out || (precision != THC_PREC_FP64 && precision != THC_PREC_MIXED)) return THC_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return THC_ERR_CUDA;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return THC_ERR_CUDA;
+  thc_ctx* h = new (std::nothrow) thc_ctx;
+  if (!h) return THC_ERR_NOMEM;
+  thc::Ctx* c = &h->c;
+  c->device = device;
+  c->precision = precision;
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaMallocHost(&c->pinned, 4096) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    return THC_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  *out = h;
+  return THC_OK;
+}
+
+int thc_ctx_destroy(thc_ctx* h)
+{
+  if (!h) return THC_ERR_ARG;
+  thc::Ctx* c = &h->c;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->plans) cufftDestroy(kv.second);
+  for (int s = 0; s < thc::WS_NSLOTS; s++)
+    if (c->ws[s]) cudaFree(c->ws[s]);
+  if (c->pinned) cudaFreeHost(c->pinned);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete h;
+  return THC_OK;
+}
+
+int thc_ctx_set_stream(thc_ctx* h, void* stream)
+{
+  if (!h) return THC_ERR_ARG;
+  h->c.stream = stream ? (cudaStream_t)stream : h->c.own_stream;
+  for (auto& kv : h->c.plans) cufftSetStream(kv.second, h->c.stream);
+  return THC_OK;
+}
+
+int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
+{
+  if (!h || !key) return THC_ERR_ARG;
+  if (!strcmp(key, "slices_p")) {
+    if (value < 2 || value > 8) return THC_ERR_ARG;
+    h->c.slices_p = (int)value;
+    return THC_OK;
+  }
+  if (!strcmp(key, "slices_z")) {
+    if (value < 2 || value > 8) return THC_ERR_ARG;
+    h->c.slices_z = (int)value;
+    return THC_OK;
+  }
+  return THC_ERR_ARG;
+}
+
+const char* thc_ctx_last_error(const thc_ctx* h)
+{
+  return h ? h->c.last_error.c_str() : "null context";
+}
+
+long long thc_ctx_kernel_launches(const thc_ctx* h) { return h ? h->c.launches : 0; }
+
+int thc_kmeans_initial_indices(long long ng, int nmu, unsigned int seed, int* out_idx)
+{
+  // KMeansSolver::guess_initial_centroids (src/kmeans.cpp:159-168): the same standard
+  // library calls on the same types, so the sequence matches the reference's libstdc++.
+  if (ng <= 0 || nmu <= 0 || nmu > ng || !out_idx || ng > 0x7fffffffLL) return THC_ERR_ARG;
+  std::vector<int> tmp((size_t)ng);
+  for (long long i = 0; i < ng; i++) tmp[i] = (int)i;
+  std::mt19937 mt(seed);
+  std::shuffle(tmp.begin(), tmp.end(), mt);
+  std::vector<int> ind(tmp.begin(), tmp.begin() + nmu);
+  std::sort(ind.begin(), ind.end());
+  std::copy(ind.begin(), ind.end(), out_idx);
+  return THC_OK;
+}
+
+int thc_kmeans(thc_ctx* h, const double* grid, const double* rho, long long ng, int nmu,
+               const int* init_idx, int max_it, double threshold, int* out_idx,
+               thc_kmeans_stats* stats)
+{
+  if (!h) return THC_ERR_ARG;
+  if (cudaSetDevice(h->c.device) != cudaSuccess) return THC_ERR_CUDA;
+  if (stats) memset(stats, 0, sizeof(*stats));
+  return thc::kmeans_run(&h->c, grid, rho, ng, nmu, init_idx, max_it, threshold, out_idx, stats);
+}
+
+int thc_isdf(thc_ctx* h, const double* phi, long long ng, int norb, const int* idx, int nmu,
+             const int* mesh, const double* coulG, double shift_rel, double* out_orbitals,
+             double* out_M, double* out_L, thc_isdf_stats* stats)
+{
+  if (!h) return THC_ERR_ARG;
+  if (cudaSetDevice(h->c.device) != cudaSuccess) return THC_ERR_CUDA;
+  if (stats) memset(stats, 0, sizeof(*stats));
+  return thc::isdf_run(&h->c, phi, ng, norb, idx, nmu, mesh, coulG, shift_rel, out_orbitals,
+                       out_M, out_L, stats);
+}
+
+}  // extern "C"

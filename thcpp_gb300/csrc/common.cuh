@@ -1,0 +1,108 @@
+// Shared internals of libthc_gb300: the context, its workspace arena and error helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/thc_gb300.h"
+
+namespace thc {
+
+// Workspace slots: each grows on demand and is reused across calls.
+enum Slot : int {
+  // k-means
+  WS_KM_GRID = 0,   // 3 x ng doubles (SoA)
+  WS_KM_GRID32,     // 3 x ng floats (SoA)
+  WS_KM_RHO,
+  WS_KM_CENT,       // 2 buffers x 3 x nmu doubles
+  WS_KM_CENT32,     // 2 buffers x 3 x nmu floats
+  WS_KM_LABELS,     // 2 x ng ints
+  WS_KM_HIST,       // nmu x nblocks ints
+  WS_KM_TOTAL,      // nmu ints (counts) + nmu ints (starts)
+  WS_KM_MEMBER,     // ng ints
+  WS_KM_TERMS,      // 3 x nmu doubles
+  WS_KM_RECHECK,    // ng ints
+  WS_KM_STATE,
+  WS_KM_PART,       // map_to_grid partials
+  WS_KM_LOG,        // per-iteration diff / pct
+  WS_KM_IO,         // staging of caller arrays
+  WS_KM_IDX,
+  // ISDF
+  WS_PHI,           // ng x norb doubles
+  WS_PHIMU,         // nmu x norb doubles
+  WS_IDX,
+  WS_COUL,          // ng doubles
+  WS_C,             // nmu x nmu doubles
+  WS_CINV,          // nmu x nmu doubles
+  WS_ZT,            // nmu x ng doubles (Z^T)
+  WS_ZETA,          // nmu x ng doubles (zeta^T)
+  WS_ZHAT,          // nmu x nc x 2 doubles
+  WS_DSYM,          // nc doubles
+  WS_DANTI,         // nc doubles + index list
+  WS_M,             // nmu x nmu x 2 doubles
+  WS_L,             // nmu x nmu x 2 doubles
+  WS_SCRATCH,       // small reductions / status
+  WS_SLICE_A,       // sliced-GEMM operands
+  WS_SLICE_B,
+  WS_SLICE_E,
+  WS_OUT,           // staging of caller outputs
+  WS_NSLOTS
+};
+
+struct Ctx {
+  int device = 0;
+  int precision = THC_PREC_FP64;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  void* ws[WS_NSLOTS] = {};
+  size_t ws_bytes[WS_NSLOTS] = {};
+  std::map<std::tuple<int, int, int, int, int>, cufftHandle> plans;  // (n0,n1,n2,batch,type)
+  void* pinned = nullptr;          // 4 KB pinned host scratch
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  long long launches = 0;
+  int slices_p = 5;
+  int slices_z = 6;
+  std::string last_error;
+};
+
+// Grow-only workspace slot; returns nullptr on allocation failure.
+void* ws_get(Ctx* c, Slot s, size_t bytes);
+
+int set_error(Ctx* c, int status, const char* fmt, ...);
+
+// Record a CUDA error after launches (cudaGetLastError).
+int check_launch(Ctx* c, const char* what);
+
+inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Residency of a caller pointer.
+bool is_device_ptr(const void* p);
+
+// Bring a caller array onto the device: returns the device pointer (the caller's own if
+// already resident, else the staging slot after an async copy).
+const void* to_device(Ctx* c, const void* p, size_t bytes, Slot staging, int* status);
+
+}  // namespace thc
+
+#define THC_CUDA(c, call)                                                          \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return thc::set_error((c), THC_ERR_CUDA, "%s: %s (%s:%d)", #call,            \
+                            cudaGetErrorString(e_), __FILE__, __LINE__);           \
+  } while (0)
+
+#define THC_LAUNCHED(c, what)                                                      \
+  do {                                                                             \
+    (c)->launches++;                                                               \
+    int s_ = thc::check_launch((c), (what));                                       \
+    if (s_) return s_;                                                             \
+  } while (0)

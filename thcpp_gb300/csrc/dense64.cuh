@@ -1,0 +1,46 @@
+// FP64 dense kernels shared by the ISDF driver.
+#pragma once
+
+#include "common.cuh"
+
+namespace thc {
+
+enum GemmMode : int { GEMM_STORE = 0, GEMM_SQUARE = 1 };
+
+// C[m, n] = mode(alpha * sum_k A(m, k) dk[k >> dk_shift] B(k, n)) + beta C[m, n]
+// with A(m, k) = A[m*sam + k*sak], B(k, n) = B[n*sbn + k*sbk] and row-major C.
+// GEMM_SQUARE stores the squared product.  lower_only restricts C to n <= m.
+struct GemmArgs {
+  long long M = 0, N = 0;
+  int K = 0;
+  const double* A = nullptr;
+  long long sam = 0, sak = 1;
+  const double* B = nullptr;
+  long long sbn = 0, sbk = 1;
+  double* C = nullptr;
+  long long ldc = 0;
+  const double* dk = nullptr;
+  int dk_shift = 0;
+  double alpha = 1.0, beta = 0.0;
+  int mode = GEMM_STORE;
+  int lower_only = 0;
+  const int* skip_flag = nullptr;   // if non-null and set, the kernel does nothing
+};
+
+struct CholStatus {
+  int flag;        // set on breakdown; later kernels of the same solve become no-ops
+  int info;        // 1-based index of the failing pivot
+  double min_piv;  // smallest / largest accepted pivot (before sqrt)
+  double max_piv;
+};
+
+int dgemm(Ctx* c, const GemmArgs& g);
+int potrf(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs);
+int potrs(Ctx* c, const double* L, long long ld, int n, double* B, long long ldb,
+          long long nrhs, const CholStatus* cs);
+int set_identity(Ctx* c, double* A, long long ld, int n);
+int add_diag_shift(Ctx* c, double* A, long long ld, int n, double rel, double* shift_out);
+int diag_mean(Ctx* c, const double* A, long long ld, int n, double* out);
+int zpotrf_small(Ctx* c, double* A, int n, const double* thr, CholStatus* cs);
+
+}  // namespace thc

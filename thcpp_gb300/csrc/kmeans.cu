@@ -1,0 +1,734 @@
+// k-means interpolating points on the GPU, bit-identical to one rank of the reference.
+//
+// Reference semantics (src/kmeans.cpp):
+//   classify_grid_points (:88-106)  label[i] = first argmin_k sqrt(dx*dx + dy*dy + dz*dz),
+//                                   dx = c_k - g_i, evaluated left to right without FMA.
+//   update_centroids (:108-144)     w_k = sum rho_i, s_k = sum rho_i * g_i over the members
+//                                   of cluster k in ascending i; c_k = s_k / w_k; any
+//                                   w_k < 1e-8 is fatal.
+//   normed_difference               scale * sqrt(sum_i ((a_i - b_i)/scale)^2) summed in
+//   (src/matrix_operations.h:42-57) index order, scale = max|a| + max|b|.
+//   kernel (:187-264)               iterate until diff < threshold or max_it, then
+//                                   map_to_grid (:146-157): for each centroid the first
+//                                   nearest grid point, sorted ascending.
+//
+// GPU layout (HBM): grid as SoA x[], y[], z[] in FP64 and FP32; two centroid buffers
+// (current / new) in FP64 and FP32 SoA; two label buffers (this / previous iteration).
+//
+// Exactness:
+//   * every FP64 operation on the reference's path uses the _rn intrinsics, so no FMA
+//     contraction changes a rounding;
+//   * the argmin compares squared distances first (sqrt is monotone, so d2 >= best_d2
+//     can never win) and takes the correctly rounded sqrt only for candidates that can;
+//     a candidate replaces the best only if its sqrt is strictly smaller, which keeps the
+//     first index among equal sqrt values exactly as std::min_element does;
+//   * per-cluster sums run in ascending grid order through a stable counting sort of
+//     the labels (block histograms -> per-cluster scans -> stable warp scatter), then
+//     one thread per cluster accumulates its members sequentially;
+//   * the normed difference is summed by one thread in index order.
+// Mixed precision: an FP32 pass keeps the best and second-best squared distance and
+// accepts its argmin only when the gap exceeds a proven bound on the FP32 error;
+// every other point is queued and resolved by a warp-parallel FP64 scan with the exact
+// semantics above.  The labels, and hence every later result, equal the FP64 path's.
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace thc {
+
+namespace {
+
+constexpr int kAssignThreads = 256;
+constexpr int kTile = 1024;       // centroids staged per shared-memory tile
+constexpr int kBP = 1024;         // points per histogram / scatter block
+constexpr int kMapChunk = 1024;   // grid points per map_to_grid block
+
+struct KmState {
+  int iter;
+  int done;
+  int converged;
+  int empty;
+  int zero_fill;
+  int final_buf;
+  int recheck_n;
+  int max_it;
+  unsigned long long changed;
+  long long rechecked_total;
+  double diff;
+  double pct;
+  double threshold;
+  double abound;        // |a| bound of the FP32 error estimate
+  unsigned long long absmax[3];
+  int bad_label;
+  int pad2;
+};
+
+struct KmBufs {
+  const double* gx; const double* gy; const double* gz;
+  const float* fx; const float* fy; const float* fz;
+  const double* rho;
+  double* cen;     // [2][3][nmu]
+  float* cen32;    // [2][3][nmu]
+  int* labels;     // [2][ng]
+  int* hist;       // [nmu][nb]
+  int* total;      // [nmu]
+  int* start;      // [nmu]
+  int* member;     // [ng]
+  double* terms;   // [3 nmu]
+  int* recheck;    // [ng]
+  double* log;     // [2][max_it]
+  KmState* st;
+  long long ng;
+  int nmu;
+  int nb;
+};
+
+__device__ __forceinline__ double d2_exact(double cx, double cy, double cz, double gx,
+                                           double gy, double gz)
+{
+  double dx = __dsub_rn(cx, gx);
+  double dy = __dsub_rn(cy, gy);
+  double dz = __dsub_rn(cz, gz);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// Running first-argmin over sqrt distances fed in ascending index order.
+struct ArgMin {
+  double s, m;
+  int k;
+  // Index 0 until something compares smaller, as std::min_element does.
+  __device__ void init() { s = CUDART_INF; m = CUDART_INF; k = 0; }
+  __device__ __forceinline__ void push(double d2, int idx)
+  {
+    if (d2 < m) {
+      double r = __dsqrt_rn(d2);
+      if (r < s) { s = r; m = d2; k = idx; }
+    }
+  }
+  // Combine with a partial result over a disjoint index set.
+  __device__ __forceinline__ void merge(double s2, double m2, int k2)
+  {
+    if (s2 < s || (s2 == s && k2 < k)) { s = s2; m = m2; k = k2; }
+  }
+};
+
+__global__ void km_prep(const double* __restrict__ grid, const double* __restrict__ rho_in,
+                        const int* __restrict__ init_idx, KmBufs b)
+{
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double* gx = const_cast<double*>(b.gx);
+  double* gy = const_cast<double*>(b.gy);
+  double* gz = const_cast<double*>(b.gz);
+  float* fx = const_cast<float*>(b.fx);
+  float* fy = const_cast<float*>(b.fy);
+  float* fz = const_cast<float*>(b.fz);
+  double* rho = const_cast<double*>(b.rho);
+  double ax = 0.0, ay = 0.0, az = 0.0;
+  if (i < b.ng) {
+    double x = grid[3 * i], y = grid[3 * i + 1], z = grid[3 * i + 2];
+    gx[i] = x; gy[i] = y; gz[i] = z;
+    fx[i] = (float)x; fy[i] = (float)y; fz[i] = (float)z;
+    rho[i] = rho_in[i];
+    ax = fabs(x); ay = fabs(y); az = fabs(z);
+  }
+  for (int off = 16; off; off >>= 1) {
+    ax = fmax(ax, __shfl_xor_sync(0xffffffffu, ax, off));
+    ay = fmax(ay, __shfl_xor_sync(0xffffffffu, ay, off));
+    az = fmax(az, __shfl_xor_sync(0xffffffffu, az, off));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    // Non-negative doubles order like their bit patterns.
+    atomicMax(&b.st->absmax[0], (unsigned long long)__double_as_longlong(ax));
+    atomicMax(&b.st->absmax[1], (unsigned long long)__double_as_longlong(ay));
+    atomicMax(&b.st->absmax[2], (unsigned long long)__double_as_longlong(az));
+  }
+  if (i < b.nmu) {
+    long long g = init_idx[i];
+    for (int d = 0; d < 3; d++) {
+      double v = grid[3 * g + d];
+      b.cen[d * b.nmu + i] = v;
+      b.cen32[d * b.nmu + i] = (float)v;
+    }
+  }
+}
+
+__global__ void km_finish_prep(KmState* st)
+{
+  // |a| <= |c| + |g| per component; centroids stay inside the grid's bounding box.
+  double a2 = 0.0;
+  for (int d = 0; d < 3; d++) {
+    double m = __longlong_as_double((long long)st->absmax[d]);
+    a2 += 4.0 * m * m;
+  }
+  st->abound = sqrt(a2);
+}
+
+// FP64 assign: one thread per grid point, centroids staged through shared memory.
+__global__ void __launch_bounds__(kAssignThreads) km_assign64(KmBufs b)
+{
+  const KmState* st = b.st;
+  if (st->done) return;
+  int it = st->iter;
+  const double* cx = b.cen + (size_t)(it & 1) * 3 * b.nmu;
+  const double* cy = cx + b.nmu;
+  const double* cz = cy + b.nmu;
+  __shared__ double sx[kTile], sy[kTile], sz[kTile];
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  bool valid = i < b.ng;
+  double gx = 0, gy = 0, gz = 0;
+  if (valid) { gx = b.gx[i]; gy = b.gy[i]; gz = b.gz[i]; }
+  ArgMin am;
+  am.init();
+  for (int t = 0; t < b.nmu; t += kTile) {
+    int n = min(kTile, b.nmu - t);
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      sx[j] = cx[t + j]; sy[j] = cy[t + j]; sz[j] = cz[t + j];
+    }
+    __syncthreads();
+    if (valid) {
+#pragma unroll 4
+      for (int j = 0; j < n; j++) am.push(d2_exact(sx[j], sy[j], sz[j], gx, gy, gz), t + j);
+    }
+  }
+  if (valid) b.labels[(size_t)(it & 1) * b.ng + i] = am.k;
+}
+
+// FP32 filter.  With u = 2^-24, inputs rounded to FP32 and the FP32 evaluation
+//   |d2_32 - d2_64| <= u (2 |d| |a| + 5 d2) + O(u^2),   a_i = |c_i| + |g_i|,
+// so a gap m2 - m1 > E(m1) + E(m2) with E(m) = 2u (2 sqrt(m) |a| + 5 m) (a factor-2
+// margin for the O(u^2) terms and the evaluation of E itself) proves that every other
+// centroid is strictly farther in FP64 than the FP32 winner, hence also after sqrt.
+__global__ void __launch_bounds__(kAssignThreads) km_assign32(KmBufs b)
+{
+  KmState* st = b.st;
+  if (st->done) return;
+  int it = st->iter;
+  const float* cx = b.cen32 + (size_t)(it & 1) * 3 * b.nmu;
+  const float* cy = cx + b.nmu;
+  const float* cz = cy + b.nmu;
+  __shared__ float sx[kTile], sy[kTile], sz[kTile];
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  bool valid = i < b.ng;
+  float gx = 0, gy = 0, gz = 0;
+  if (valid) { gx = b.fx[i]; gy = b.fy[i]; gz = b.fz[i]; }
+  float m1 = INFINITY, m2 = INFINITY;
+  int k1 = 0;
+  for (int t = 0; t < b.nmu; t += kTile) {
+    int n = min(kTile, b.nmu - t);
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      sx[j] = cx[t + j]; sy[j] = cy[t + j]; sz[j] = cz[t + j];
+    }
+    __syncthreads();
+    if (valid) {
+#pragma unroll 8
+      for (int j = 0; j < n; j++) {
+        float dx = sx[j] - gx, dy = sy[j] - gy, dz = sz[j] - gz;
+        float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+        if (d2 < m1) { m2 = m1; m1 = d2; k1 = t + j; }
+        else if (d2 < m2) { m2 = d2; }
+      }
+    }
+  }
+  if (!valid) return;
+  const double u = 5.9604644775390625e-08;  // 2^-24
+  double a = st->abound;
+  double e1 = 2.0 * u * (2.0 * sqrt((double)m1) * a + 5.0 * (double)m1);
+  double e2 = 2.0 * u * (2.0 * sqrt((double)m2) * a + 5.0 * (double)m2);
+  if ((double)m2 - (double)m1 > e1 + e2 + 1e-300) {
+    b.labels[(size_t)(it & 1) * b.ng + i] = k1;
+  } else {
+    int slot = atomicAdd(&st->recheck_n, 1);
+    b.recheck[slot] = (int)i;
+  }
+}
+
+// FP64 recheck of queued points: one warp per point, lanes split the centroids.
+__global__ void km_recheck(KmBufs b)
+{
+  const KmState* st = b.st;
+  if (st->done) return;
+  int it = st->iter;
+  int n = st->recheck_n;
+  const double* cx = b.cen + (size_t)(it & 1) * 3 * b.nmu;
+  const double* cy = cx + b.nmu;
+  const double* cz = cy + b.nmu;
+  int lane = threadIdx.x & 31;
+  long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long w = warp; w < n; w += nwarps) {
+    long long i = b.recheck[w];
+    double gx = b.gx[i], gy = b.gy[i], gz = b.gz[i];
+    ArgMin am;
+    am.init();
+    for (int j = lane; j < b.nmu; j += 32) am.push(d2_exact(cx[j], cy[j], cz[j], gx, gy, gz), j);
+    for (int off = 16; off; off >>= 1) {
+      double s2 = __shfl_xor_sync(0xffffffffu, am.s, off);
+      double m2 = __shfl_xor_sync(0xffffffffu, am.m, off);
+      int k2 = __shfl_xor_sync(0xffffffffu, am.k, off);
+      am.merge(s2, m2, k2);
+    }
+    if (lane == 0) b.labels[(size_t)(it & 1) * b.ng + i] = am.k;
+  }
+}
+
+// Per-block label histogram (sparse write into the zeroed hist[k][block]) and the
+// count of labels that changed since the previous iteration.
+__global__ void km_hist(KmBufs b)
+{
+  KmState* st = b.st;
+  if (st->done) return;
+  int it = st->iter;
+  extern __shared__ int sh[];
+  for (int k = threadIdx.x; k < b.nmu; k += blockDim.x) sh[k] = 0;
+  __syncthreads();
+  const int* lab = b.labels + (size_t)(it & 1) * b.ng;
+  const int* old = b.labels + (size_t)((it + 1) & 1) * b.ng;
+  long long base = (long long)blockIdx.x * kBP;
+  unsigned changed = 0;
+  for (int t = threadIdx.x; t < kBP; t += blockDim.x) {
+    long long i = base + t;
+    if (i < b.ng) {
+      int l = lab[i];
+      if ((unsigned)l >= (unsigned)b.nmu) {   // never produced by the assign kernels
+        atomicExch(&st->bad_label, 1);
+        continue;
+      }
+      atomicAdd(&sh[l], 1);
+      if (it > 0 && old[i] != l) changed++;
+    }
+  }
+  for (int off = 16; off; off >>= 1) changed += __shfl_xor_sync(0xffffffffu, changed, off);
+  if ((threadIdx.x & 31) == 0 && changed) atomicAdd(&st->changed, (unsigned long long)changed);
+  __syncthreads();
+  for (int k = threadIdx.x; k < b.nmu; k += blockDim.x)
+    if (sh[k]) b.hist[(size_t)k * b.nb + blockIdx.x] = sh[k];
+}
+
+// One warp per cluster: exclusive scan of its block counts (in place) and its total.
+__global__ void km_colscan(KmBufs b)
+{
+  if (b.st->done) return;
+  int lane = threadIdx.x & 31;
+  long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (k >= b.nmu) return;
+  int* h = b.hist + (size_t)k * b.nb;
+  int carry = 0;
+  for (int c = 0; c < b.nb; c += 32) {
+    int j = c + lane;
+    int v = j < b.nb ? h[j] : 0;
+    int x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) x += y;
+    }
+    if (j < b.nb) h[j] = carry + x - v;
+    carry += __shfl_sync(0xffffffffu, x, 31);
+  }
+  if (lane == 0) b.total[k] = carry;
+}
+
+// Single block: exclusive scan of the cluster totals into cluster start offsets.
+__global__ void km_kscan(KmBufs b)
+{
+  if (b.st->done) return;
+  __shared__ int warp_sums[32];
+  int n = b.nmu;
+  int per = (n + blockDim.x - 1) / blockDim.x;
+  int lo = threadIdx.x * per, hi = min(n, lo + per);
+  int s = 0;
+  for (int k = lo; k < hi; k++) s += b.total[k];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = s;
+  for (int off = 1; off < 32; off <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+    int xw = w;
+    for (int off = 1; off < 32; off <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, xw, off);
+      if (lane >= off) xw += y;
+    }
+    warp_sums[lane] = xw - w;
+  }
+  __syncthreads();
+  int run = warp_sums[wid] + x - s;
+  for (int k = lo; k < hi; k++) {
+    b.start[k] = run;
+    run += b.total[k];
+  }
+}
+
+// Stable scatter of point indices into per-cluster member lists.  Warp 0 walks the
+// block's points in ascending order, 32 at a time; lanes with equal labels take ranks
+// from __match_any_sync so each cluster keeps ascending grid order.
+__global__ void km_scatter(KmBufs b)
+{
+  if (b.st->done) return;
+  int it = b.st->iter;
+  extern __shared__ int base[];
+  for (int k = threadIdx.x; k < b.nmu; k += blockDim.x) base[k] = -1;
+  __syncthreads();
+  if (threadIdx.x >= 32) return;
+  int lane = threadIdx.x;
+  const int* lab = b.labels + (size_t)(it & 1) * b.ng;
+  long long blk = (long long)blockIdx.x * kBP;
+  unsigned lt = (1u << lane) - 1u;
+  for (int c = 0; c < kBP; c += 32) {
+    long long i = blk + c + lane;
+    bool valid = i < b.ng;
+    unsigned active = __ballot_sync(0xffffffffu, valid);
+    if (!active) break;
+    if (valid) {
+      int l = lab[i];
+      if ((unsigned)l >= (unsigned)b.nmu) l = 0;  // flagged by km_hist; keeps indexing in range
+      unsigned peers = __match_any_sync(active, l);
+      int leader = __ffs(peers) - 1;
+      if (lane == leader && base[l] < 0)
+        base[l] = b.start[l] + b.hist[(size_t)l * b.nb + blockIdx.x];
+      __syncwarp(active);
+      int pos = base[l] + __popc(peers & lt);
+      b.member[pos] = (int)i;
+      __syncwarp(active);
+      if (lane == leader) base[l] += __popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+// One thread per cluster: sequential sums over members in ascending grid order.
+__global__ void km_sums(KmBufs b)
+{
+  KmState* st = b.st;
+  if (st->done) return;
+  int it = st->iter;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= b.nmu) return;
+  int s = b.start[k], n = b.total[k];
+  double w = 0.0, x = 0.0, y = 0.0, z = 0.0;
+  for (int m = s; m < s + n; m++) {
+    int i = b.member[m];
+    double r = b.rho[i];
+    w = __dadd_rn(w, r);
+    x = __dadd_rn(x, __dmul_rn(r, b.gx[i]));
+    y = __dadd_rn(y, __dmul_rn(r, b.gy[i]));
+    z = __dadd_rn(z, __dmul_rn(r, b.gz[i]));
+  }
+  if (w < 1e-8) atomicExch(&st->empty, 1);
+  double* nc = b.cen + (size_t)((it + 1) & 1) * 3 * b.nmu;
+  float* nc32 = b.cen32 + (size_t)((it + 1) & 1) * 3 * b.nmu;
+  double cx = __ddiv_rn(x, w), cy = __ddiv_rn(y, w), cz = __ddiv_rn(z, w);
+  nc[k] = cx; nc[b.nmu + k] = cy; nc[2 * b.nmu + k] = cz;
+  nc32[k] = (float)cx; nc32[b.nmu + k] = (float)cy; nc32[2 * b.nmu + k] = (float)cz;
+}
+
+__device__ __forceinline__ double block_max(double v, double* red)
+{
+  for (int off = 16; off; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+    for (int off = 16; off; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if (lane == 0) red[0] = v;
+  }
+  __syncthreads();
+  return red[0];
+}
+
+// Single block: normed difference (new vs current), convergence and state update.
+__global__ void km_normdiff(KmBufs b)
+{
+  KmState* st = b.st;
+  if (st->done) return;
+  __shared__ double red[32];
+  int it = st->iter;
+  int n3 = 3 * b.nmu;
+  if (st->empty || st->bad_label) {
+    if (threadIdx.x == 0) { st->done = 1; st->iter = it + 1; }
+    return;
+  }
+  const double* a = b.cen + (size_t)((it + 1) & 1) * 3 * b.nmu;   // new
+  const double* c = b.cen + (size_t)(it & 1) * 3 * b.nmu;         // current
+  double ma = 0.0, mc = 0.0;
+  for (int i = threadIdx.x; i < n3; i += blockDim.x) {
+    int k = i / 3, d = i - 3 * k;
+    ma = fmax(ma, fabs(a[d * b.nmu + k]));
+    mc = fmax(mc, fabs(c[d * b.nmu + k]));
+  }
+  ma = block_max(ma, red);
+  mc = block_max(mc, red);
+  double scale = __dadd_rn(ma, mc);
+  for (int i = threadIdx.x; i < n3; i += blockDim.x) {
+    int k = i / 3, d = i - 3 * k;
+    double q = __ddiv_rn(__dsub_rn(a[d * b.nmu + k], c[d * b.nmu + k]), scale);
+    b.terms[i] = __dmul_rn(q, q);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < n3; i++) s = __dadd_rn(s, b.terms[i]);
+    double diff = __dmul_rn(scale, __dsqrt_rn(s));
+    st->diff = diff;
+    st->pct = 100.0 * (double)st->changed / (double)b.ng;
+    b.log[it] = diff;
+    b.log[st->max_it + it] = st->pct;
+    st->changed = 0;
+    st->rechecked_total += st->recheck_n;
+    st->recheck_n = 0;
+    st->final_buf = (it + 1) & 1;
+    if (diff < st->threshold) {
+      st->converged = 1;
+      st->done = 1;
+    } else if (it + 1 >= st->max_it) {
+      st->done = 1;
+      st->zero_fill = !(diff > st->threshold);
+    }
+    st->iter = it + 1;
+  }
+}
+
+// map_to_grid, part 1: each thread owns one centroid and scans one chunk of grid points.
+__global__ void km_map_part(KmBufs b, double* part_s, int* part_i, int nch)
+{
+  const double* cen = b.cen + (size_t)b.st->final_buf * 3 * b.nmu;
+  __shared__ double sx[kMapChunk], sy[kMapChunk], sz[kMapChunk];
+  long long p0 = (long long)blockIdx.x * kMapChunk;
+  int n = (int)min((long long)kMapChunk, b.ng - p0);
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    sx[j] = b.gx[p0 + j]; sy[j] = b.gy[p0 + j]; sz[j] = b.gz[p0 + j];
+  }
+  __syncthreads();
+  int k = blockIdx.y * blockDim.x + threadIdx.x;
+  if (k >= b.nmu) return;
+  double cx = cen[k], cy = cen[b.nmu + k], cz = cen[2 * b.nmu + k];
+  ArgMin am;
+  am.init();
+  // map_to_grid calls classify with the roles swapped: dx = g_j - c_k.
+#pragma unroll 4
+  for (int j = 0; j < n; j++) am.push(d2_exact(sx[j], sy[j], sz[j], cx, cy, cz), (int)(p0 + j));
+  part_s[(size_t)k * nch + blockIdx.x] = am.s;
+  part_i[(size_t)k * nch + blockIdx.x] = am.k;
+}
+
+__global__ void km_map_reduce(int nmu, int nch, const double* part_s, const int* part_i,
+                              int* idx)
+{
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nmu) return;
+  double s = CUDART_INF;
+  int best = 0;
+  for (int c = 0; c < nch; c++) {
+    double v = part_s[(size_t)k * nch + c];
+    int i = part_i[(size_t)k * nch + c];
+    if (v < s || (v == s && i < best)) { s = v; best = i; }
+  }
+  idx[k] = best;
+}
+
+// Single-block bitonic sort of the nmu indices (padded to a power of two) and the
+// count of adjacent duplicates.
+__global__ void km_sort(int* idx, int n, int npow2, int* dups)
+{
+  extern __shared__ int a[];
+  for (int i = threadIdx.x; i < npow2; i += blockDim.x) a[i] = i < n ? idx[i] : 0x7fffffff;
+  __syncthreads();
+  for (int size = 2; size <= npow2; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < npow2; i += blockDim.x) {
+        int j = i ^ stride;
+        if (j > i) {
+          bool up = (i & size) == 0;
+          int x = a[i], y = a[j];
+          if ((x > y) == up) { a[i] = y; a[j] = x; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  int d = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    idx[i] = a[i];
+    if (i + 1 < n && a[i] == a[i + 1]) d++;
+  }
+  if (d) atomicAdd(dups, d);
+}
+
+}  // namespace
+
+int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng, int nmu,
+               const int* init_in, int max_it, double threshold, int* out_idx,
+               thc_kmeans_stats* stats)
+{
+  if (!grid_in || !rho_in || !init_in || !out_idx || ng <= 0 || nmu <= 0 || nmu > ng ||
+      max_it < 1 || ng > 0x7fffffffLL)
+    return set_error(c, THC_ERR_ARG, "thc_kmeans: invalid arguments");
+  if (nmu > 16384) return set_error(c, THC_ERR_SHAPE, "thc_kmeans: nmu > 16384 unsupported");
+  cudaStream_t s = c->stream;
+  int st_status = 0;
+  const double* grid = (const double*)to_device(c, grid_in, sizeof(double) * 3 * ng,
+                                                WS_KM_IO, &st_status);
+  if (st_status) return st_status;
+  // rho and the initial indices share a second staging area after the grid copy.
+  const double* rho = nullptr;
+  const int* init = nullptr;
+  {
+    size_t rb = sizeof(double) * ng, ib = sizeof(int) * nmu;
+    bool rd = is_device_ptr(rho_in), id = is_device_ptr(init_in);
+    char* stage = nullptr;
+    if (!rd || !id) {
+      stage = (char*)ws_get(c, WS_KM_IDX, rb + ib + 256);
+      if (!stage) return set_error(c, THC_ERR_NOMEM, "thc_kmeans: staging");
+    }
+    if (rd) rho = rho_in;
+    else {
+      THC_CUDA(c, cudaMemcpyAsync(stage, rho_in, rb, cudaMemcpyHostToDevice, s));
+      rho = (const double*)stage;
+    }
+    if (id) init = init_in;
+    else {
+      char* p = stage + ((rb + 255) / 256) * 256;
+      THC_CUDA(c, cudaMemcpyAsync(p, init_in, ib, cudaMemcpyHostToDevice, s));
+      init = (const int*)p;
+    }
+  }
+  KmBufs b{};
+  b.ng = ng;
+  b.nmu = nmu;
+  b.nb = (int)cdiv(ng, kBP);
+  double* g64 = (double*)ws_get(c, WS_KM_GRID, sizeof(double) * 4 * ng);
+  float* g32 = (float*)ws_get(c, WS_KM_GRID32, sizeof(float) * 3 * ng);
+  double* cen = (double*)ws_get(c, WS_KM_CENT, sizeof(double) * 6 * nmu);
+  float* cen32 = (float*)ws_get(c, WS_KM_CENT32, sizeof(float) * 6 * nmu);
+  int* labels = (int*)ws_get(c, WS_KM_LABELS, sizeof(int) * 2 * ng);
+  int* hist = (int*)ws_get(c, WS_KM_HIST, sizeof(int) * (size_t)nmu * b.nb);
+  int* tot = (int*)ws_get(c, WS_KM_TOTAL, sizeof(int) * 2 * nmu);
+  int* member = (int*)ws_get(c, WS_KM_MEMBER, sizeof(int) * ng);
+  double* terms = (double*)ws_get(c, WS_KM_TERMS, sizeof(double) * 3 * nmu);
+  int* recheck = (int*)ws_get(c, WS_KM_RECHECK, sizeof(int) * ng);
+  KmState* st = (KmState*)ws_get(c, WS_KM_STATE, sizeof(KmState) + 64);
+  double* logb = (double*)ws_get(c, WS_KM_LOG, sizeof(double) * 2 * max_it);
+  int nch = (int)cdiv(ng, kMapChunk);
+  double* part_s = (double*)ws_get(c, WS_KM_PART, (sizeof(double) + sizeof(int)) * (size_t)nmu * nch + 64);
+  if (!g64 || !g32 || !cen || !cen32 || !labels || !hist || !tot || !member || !terms ||
+      !recheck || !st || !logb || !part_s)
+    return set_error(c, THC_ERR_NOMEM, "thc_kmeans: workspace allocation failed");
+  int* part_i = (int*)(part_s + (size_t)nmu * nch);
+  b.gx = g64; b.gy = g64 + ng; b.gz = g64 + 2 * ng; b.rho = g64 + 3 * ng;
+  b.fx = g32; b.fy = g32 + ng; b.fz = g32 + 2 * ng;
+  b.cen = cen; b.cen32 = cen32; b.labels = labels; b.hist = hist; b.total = tot;
+  b.start = tot + nmu; b.member = member; b.terms = terms; b.recheck = recheck;
+  b.log = logb; b.st = st;
+
+  KmState h{};
+  h.max_it = max_it;
+  h.threshold = threshold;
+  THC_CUDA(c, cudaMemcpyAsync(st, &h, sizeof(KmState), cudaMemcpyHostToDevice, s));
+  THC_CUDA(c, cudaEventRecord(c->ev0, s));
+  int nprep = (int)cdiv(std::max<long long>(ng, nmu), 256);
+  km_prep<<<nprep, 256, 0, s>>>(grid, rho, init, b);
+  THC_LAUNCHED(c, "km_prep");
+  km_finish_prep<<<1, 1, 0, s>>>(st);
+  THC_LAUNCHED(c, "km_finish_prep");
+
+  const bool mixed = c->precision == THC_PREC_MIXED;
+  int nassign = (int)cdiv(ng, kAssignThreads);
+  size_t hist_smem = sizeof(int) * nmu;
+  if (hist_smem > 48 * 1024) {
+    THC_CUDA(c, cudaFuncSetAttribute(km_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
+    THC_CUDA(c, cudaFuncSetAttribute(km_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
+  }
+  int* hflag = (int*)c->pinned;
+  const int kCheckEvery = 8;
+  for (int it = 0; it < max_it; it++) {
+    if (mixed) {
+      km_assign32<<<nassign, kAssignThreads, 0, s>>>(b);
+      THC_LAUNCHED(c, "km_assign32");
+      km_recheck<<<152 * 4, 256, 0, s>>>(b);
+      THC_LAUNCHED(c, "km_recheck");
+    } else {
+      km_assign64<<<nassign, kAssignThreads, 0, s>>>(b);
+      THC_LAUNCHED(c, "km_assign64");
+    }
+    THC_CUDA(c, cudaMemsetAsync(hist, 0, sizeof(int) * (size_t)nmu * b.nb, s));
+    km_hist<<<b.nb, 256, hist_smem, s>>>(b);
+    THC_LAUNCHED(c, "km_hist");
+    km_colscan<<<(int)cdiv((long long)nmu * 32, 256), 256, 0, s>>>(b);
+    THC_LAUNCHED(c, "km_colscan");
+    km_kscan<<<1, 1024, 0, s>>>(b);
+    THC_LAUNCHED(c, "km_kscan");
+    km_scatter<<<b.nb, 128, hist_smem, s>>>(b);
+    THC_LAUNCHED(c, "km_scatter");
+    km_sums<<<(int)cdiv(nmu, 128), 128, 0, s>>>(b);
+    THC_LAUNCHED(c, "km_sums");
+    km_normdiff<<<1, 1024, 0, s>>>(b);
+    THC_LAUNCHED(c, "km_normdiff");
+    if ((it + 1) % kCheckEvery == 0 && it + 1 < max_it) {
+      THC_CUDA(c, cudaMemcpyAsync(hflag, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+      THC_CUDA(c, cudaStreamSynchronize(s));
+      if (*hflag) break;
+    }
+  }
+  // Map the final centroids to the grid, sort, count duplicates.
+  int* didx = is_device_ptr(out_idx) ? out_idx : (int*)((char*)hist);  // hist is free now
+  int* dups = (int*)(part_i + (size_t)nmu * nch);
+  THC_CUDA(c, cudaMemsetAsync(dups, 0, sizeof(int), s));
+  dim3 mg((unsigned)nch, (unsigned)cdiv(nmu, 256));
+  km_map_part<<<mg, 256, 0, s>>>(b, part_s, part_i, nch);
+  THC_LAUNCHED(c, "km_map_part");
+  km_map_reduce<<<(int)cdiv(nmu, 256), 256, 0, s>>>(nmu, nch, part_s, part_i, didx);
+  THC_LAUNCHED(c, "km_map_reduce");
+  int np2 = 1;
+  while (np2 < nmu) np2 <<= 1;
+  size_t sort_smem = sizeof(int) * np2;
+  if (sort_smem > 48 * 1024)
+    THC_CUDA(c, cudaFuncSetAttribute(km_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem));
+  km_sort<<<1, 1024, sort_smem, s>>>(didx, nmu, np2, dups);
+  THC_LAUNCHED(c, "km_sort");
+  THC_CUDA(c, cudaEventRecord(c->ev1, s));
+  KmState hs{};
+  THC_CUDA(c, cudaMemcpyAsync(&hs, st, sizeof(KmState), cudaMemcpyDeviceToHost, s));
+  int hd = 0;
+  THC_CUDA(c, cudaMemcpyAsync(&hd, dups, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (didx != out_idx)
+    THC_CUDA(c, cudaMemcpyAsync(out_idx, didx, sizeof(int) * nmu, cudaMemcpyDeviceToHost, s));
+  THC_CUDA(c, cudaStreamSynchronize(s));
+  if (hs.bad_label) return set_error(c, THC_ERR_CUDA, "thc_kmeans: internal label out of range");
+  if (hs.empty) {
+    if (stats) stats->iterations = hs.iter;
+    return set_error(c, THC_ERR_EMPTY_CLUSTER, "CRITICAL ERROR: Found centroid with weight ~ 0");
+  }
+  if (hs.zero_fill) {
+    // The reference leaves interp_indxs zero-filled when the last diff equals the threshold.
+    THC_CUDA(c, cudaMemsetAsync(didx, 0, sizeof(int) * nmu, s));
+    if (didx != out_idx) std::fill(out_idx, out_idx + nmu, 0);
+    THC_CUDA(c, cudaStreamSynchronize(s));
+  }
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    stats->iterations = hs.iter;
+    stats->converged = hs.converged;
+    stats->zero_filled = hs.zero_fill;
+    stats->duplicates = hd;
+    stats->final_diff = hs.diff;
+    stats->pct_changed = hs.pct;
+    stats->rechecked = hs.rechecked_total;
+    stats->device_ms = ms;
+  }
+  return THC_OK;
+}
+
+}  // namespace thc

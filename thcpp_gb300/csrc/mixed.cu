@@ -1,0 +1,348 @@
+// Mixed-precision ISDF: the same quantities as isdf.cu with the three large products on
+// the BF16 tensor cores through error-free slicing (ozgemm):
+//   Z^T    = (Phi_mu Phi^T)^2      sliced GEMM, FP64 result, squared in the epilogue
+//   zeta^T = C^{-1} Z^T            sliced GEMM, FP32 result (input of the FP32 FFT)
+//   Re M   = A A^T, A = zeta_hat * sqrt(w v_sym)  sliced GEMM over the half spectrum
+// C, its Cholesky factor and C^{-1} stay FP64 (C is ill-conditioned: cond ~1e6-1e9), and
+// so does the Cholesky factorisation of M.  The slice depths fix the accuracy: each
+// product is exact to ~(L+2) 2^{-7(L+1)} of sum |A||B| (ozgemm.cuh).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+#include "dense64.cuh"
+#include "isdf.cuh"
+#include "ozgemm.cuh"
+
+namespace thc {
+
+namespace {
+
+__global__ void gather_rows_m(const double* __restrict__ phi, long long ng, int no,
+                              const int* __restrict__ idx, int nmu, double* phimu,
+                              double* orbitals, int* bad)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)nmu * no) return;
+  int mu = (int)(e / no), i = (int)(e % no);
+  long long g = idx[mu];
+  if (g < 0 || g >= ng) {
+    atomicExch(bad, 1);
+    return;
+  }
+  double v = phi[g * no + i];
+  phimu[e] = v;
+  if (orbitals) {
+    orbitals[2 * ((long long)i * nmu + mu)] = v;
+    orbitals[2 * ((long long)i * nmu + mu) + 1] = 0.0;
+  }
+}
+
+__global__ void coulomb_weights_m(const double* __restrict__ v, int n0, int n1, int n2,
+                                  double* dsym, double* danti, float* sq, int* n_anti)
+{
+  int nc = n2 / 2 + 1;
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long tot = (long long)n0 * n1 * nc;
+  if (e >= tot) return;
+  int k2 = (int)(e % nc);
+  long long r = e / nc;
+  int k1 = (int)(r % n1), k0 = (int)(r / n1);
+  int j0 = (n0 - k0) % n0, j1 = (n1 - k1) % n1, j2 = (n2 - k2) % n2;
+  double vp = v[((long long)k0 * n1 + k1) * n2 + k2];
+  double vn = v[((long long)j0 * n1 + j1) * n2 + j2];
+  double w = (k2 == 0 || (n2 % 2 == 0 && k2 == n2 / 2)) ? 1.0 : 2.0;
+  double ds = w * 0.5 * (vp + vn);
+  dsym[e] = ds;
+  sq[e] = (float)sqrt(fmax(ds, 0.0));
+  double a = w * 0.5 * (vp - vn);
+  danti[e] = a;
+  if (a != 0.0) atomicAdd(n_anti, 1);
+}
+
+// X[mu, nu] = sum_c danti[c] Re zh[mu, c] Im zh[nu, c] over the points with danti != 0.
+__global__ void imag_part_c64(const float2* __restrict__ zh, long long nc, int nmu,
+                              const double* __restrict__ danti, double* X)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)nmu * nmu) return;
+  int mu = (int)(e / nmu), nu = (int)(e % nmu);
+  double s = 0.0;
+  for (long long c = 0; c < nc; c++) {
+    double d = danti[c];
+    if (d != 0.0) s += d * (double)zh[mu * nc + c].x * (double)zh[nu * nc + c].y;
+  }
+  X[e] = s;
+}
+
+__global__ void assemble_m_m(const double* __restrict__ mre, const double* __restrict__ x,
+                             int n, double* M)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)n * n) return;
+  int r = (int)(e / n), c = (int)(e % n);
+  double re = r >= c ? mre[(long long)r * n + c] : mre[(long long)c * n + r];
+  double im = x ? x[(long long)r * n + c] - x[(long long)c * n + r] : 0.0;
+  M[2 * e] = re;
+  M[2 * e + 1] = im;
+}
+
+__global__ void copy_lower_to_full_m(const double* __restrict__ src, int n, double* dst)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)n * n) return;
+  int r = (int)(e / n), c = (int)(e % n);
+  dst[e] = r >= c ? src[e] : src[(long long)c * n + r];
+}
+
+__global__ void export_l_real_m(const double* __restrict__ L, int n, double* out)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)n * n) return;
+  int r = (int)(e / n), c = (int)(e % n);
+  out[2 * e] = c <= r ? L[e] : 0.0;
+  out[2 * e + 1] = 0.0;
+}
+
+__global__ void zero_upper_complex_m(double* A, int n)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)n * n) return;
+  int r = (int)(e / n), c = (int)(e % n);
+  if (c > r) { A[2 * e] = 0.0; A[2 * e + 1] = 0.0; }
+}
+
+__global__ void mixed_scalars(double* dmean, double* thr, double* shift, double* zero)
+{
+  *thr = 1e-13 * *dmean;
+  *shift = 0.0;
+  *zero = 0.0;
+}
+
+__global__ void init_cs(CholStatus* cs)
+{
+  cs->flag = 0;
+  cs->info = 0;
+  cs->min_piv = 1.0 / 0.0;
+  cs->max_piv = 0.0;
+}
+
+}  // namespace
+
+int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_in,
+                   int nmu, const int* mesh, const double* coul_in, double shift_rel,
+                   double* out_orb, double* out_M, double* out_L, thc_isdf_stats* stats)
+{
+  cudaStream_t s = c->stream;
+  int st = 0;
+  const double* phi = (const double*)to_device(c, phi_in, sizeof(double) * ng * no, WS_PHI, &st);
+  if (st) return st;
+  const int* idx = (const int*)to_device(c, idx_in, sizeof(int) * nmu, WS_IDX, &st);
+  if (st) return st;
+  const double* coul = (const double*)to_device(c, coul_in, sizeof(double) * ng, WS_COUL, &st);
+  if (st) return st;
+  const int n0 = mesh[0], n1 = mesh[1], n2 = mesh[2];
+  const long long nc = (long long)n0 * n1 * (n2 / 2 + 1);
+  const long long nn = (long long)nmu * nmu;
+  const int sp = c->slices_p, sz = c->slices_z, sm = 4;
+  const long long mu_pad = oz_pad_mn(nmu), mu_kpad = oz_pad_k(nmu);
+  const long long ng_pad = oz_pad_mn(ng), no_kpad = oz_pad_k(no);
+  const long long k2_pad = oz_pad_k(2 * nc);
+
+  double* phimu = (double*)ws_get(c, WS_PHIMU, sizeof(double) * nmu * no);
+  double* C = (double*)ws_get(c, WS_C, sizeof(double) * 2 * nn);
+  double* Cinv = (double*)ws_get(c, WS_CINV, sizeof(double) * nn);
+  double* zt = (double*)ws_get(c, WS_ZT, sizeof(double) * nmu * ng);
+  float* zeta = (float*)ws_get(c, WS_ZETA, sizeof(float) * nmu * ng);
+  float2* zhat = (float2*)ws_get(c, WS_ZHAT, sizeof(float2) * nmu * nc);
+  double* dsym = (double*)ws_get(c, WS_DSYM, (sizeof(double) + sizeof(float)) * nc + 64);
+  double* danti = (double*)ws_get(c, WS_DANTI, sizeof(double) * nc);
+  double* Mw = (double*)ws_get(c, WS_M, sizeof(double) * 4 * nn);
+  double* Lw = (double*)ws_get(c, WS_L, sizeof(double) * 2 * nn);
+  char* scr = (char*)ws_get(c, WS_SCRATCH, 4096);
+  size_t a_elems = std::max({(size_t)sp * mu_pad * no_kpad, (size_t)sz * mu_pad * mu_kpad,
+                             (size_t)sm * mu_pad * k2_pad});
+  size_t b_elems = std::max((size_t)sp * ng_pad * no_kpad, (size_t)sz * mu_kpad * ng_pad);
+  __nv_bfloat16* sa = (__nv_bfloat16*)ws_get(c, WS_SLICE_A, sizeof(__nv_bfloat16) * a_elems);
+  __nv_bfloat16* sb = (__nv_bfloat16*)ws_get(c, WS_SLICE_B, sizeof(__nv_bfloat16) * b_elems);
+  int* ex = (int*)ws_get(c, WS_SLICE_E, sizeof(int) * (mu_pad + ng_pad + 64));
+  if (!phimu || !C || !Cinv || !zt || !zeta || !zhat || !dsym || !danti || !Mw || !Lw || !scr ||
+      !sa || !sb || !ex)
+    return set_error(c, THC_ERR_NOMEM, "thc_isdf (mixed): workspace allocation failed");
+  float* sq = (float*)(dsym + nc);
+  int* ea = ex;
+  int* eb = ex + mu_pad;
+  CholStatus* cs = (CholStatus*)scr;
+  CholStatus* csm = cs + 1;
+  double* dmean = (double*)(scr + 256);
+  double* thr = dmean + 1;
+  double* shift_dev = dmean + 2;
+  double* zero = dmean + 3;
+  int* bad = (int*)(scr + 512);
+  int* n_anti = bad + 1;
+  double* orb_dev = nullptr;
+  if (out_orb) orb_dev = is_device_ptr(out_orb) ? out_orb : Lw;
+  THC_CUDA(c, cudaMemsetAsync(scr + 512, 0, 64, s));
+  THC_CUDA(c, cudaEventRecord(c->ev0, s));
+
+  gather_rows_m<<<(int)cdiv((long long)nmu * no, 256), 256, 0, s>>>(phi, ng, no, idx, nmu, phimu,
+                                                                    orb_dev, bad);
+  THC_LAUNCHED(c, "gather_rows");
+  if (out_orb && orb_dev != out_orb)
+    THC_CUDA(c, cudaMemcpyAsync(out_orb, orb_dev, sizeof(double) * 2 * nmu * no,
+                                cudaMemcpyDeviceToHost, s));
+  // C = (Phi_mu Phi_mu^T)^2 in FP64 and its factorisation.
+  {
+    GemmArgs g;
+    g.M = nmu; g.N = nmu; g.K = no;
+    g.A = phimu; g.sam = no; g.sak = 1;
+    g.B = phimu; g.sbn = no; g.sbk = 1;
+    g.C = C; g.ldc = nmu; g.mode = GEMM_SQUARE;
+    if ((st = dgemm(c, g))) return st;
+  }
+  double* Lc = C + nn;
+  if ((st = diag_mean(c, C, nmu, nmu, dmean))) return st;
+  mixed_scalars<<<1, 1, 0, s>>>(dmean, thr, shift_dev, zero);
+  THC_LAUNCHED(c, "mixed_scalars");
+  auto factor = [&](double rel) -> int {
+    THC_CUDA(c, cudaMemcpyAsync(Lc, C, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
+    if (rel > 0.0) {
+      int r = add_diag_shift(c, Lc, nmu, nmu, rel, shift_dev);
+      if (r) return r;
+    }
+    init_cs<<<1, 1, 0, s>>>(cs);
+    THC_LAUNCHED(c, "init_cs");
+    return potrf(c, Lc, nmu, nmu, thr, cs);
+  };
+  // Z^T via the sliced GEMM, overlapping nothing yet: it does not depend on C.
+  if ((st = oz_slice_rows_f64(c, phimu, nmu, no, no, 1, nullptr, 0, sp, sa, no_kpad,
+                              mu_pad * no_kpad, ea, mu_pad)))
+    return st;
+  if ((st = oz_slice_rows_f64(c, phi, ng, no, no, 1, nullptr, 0, sp, sb, no_kpad,
+                              ng_pad * no_kpad, eb, ng_pad)))
+    return st;
+  {
+    OzArgs g;
+    g.M = nmu; g.N = ng; g.K = no;
+    g.a.s = sa; g.a.e = ea; g.a.ld = no_kpad; g.a.slice_stride = mu_pad * no_kpad;
+    g.b.s = sb; g.b.e = eb; g.b.ld = no_kpad; g.b.slice_stride = ng_pad * no_kpad;
+    g.b.k_contig = true;
+    g.levels = sp; g.epilogue = OZ_SQUARE_F64; g.C = zt; g.ldc = ng;
+    if ((st = ozgemm(c, g))) return st;
+  }
+  CholStatus hcs{};
+  int chol_c_info = 0;
+  bool shifted = shift_rel > 0.0;
+  if ((st = factor(shift_rel > 0.0 ? shift_rel : 0.0))) return st;
+  THC_CUDA(c, cudaMemcpyAsync(&hcs, cs, sizeof(CholStatus), cudaMemcpyDeviceToHost, s));
+  THC_CUDA(c, cudaStreamSynchronize(s));
+  if (hcs.flag) {
+    chol_c_info = hcs.info;
+    if (shift_rel < 0.0 && !shifted) {
+      if ((st = factor(1e-10))) return st;
+      shifted = true;
+      THC_CUDA(c, cudaMemcpyAsync(&hcs, cs, sizeof(CholStatus), cudaMemcpyDeviceToHost, s));
+      THC_CUDA(c, cudaStreamSynchronize(s));
+    }
+    if (hcs.flag)
+      return set_error(c, THC_ERR_NOT_PD, "thc_isdf: Cholesky of C failed at pivot %d", hcs.info);
+  }
+  if ((st = set_identity(c, Cinv, nmu, nmu))) return st;
+  if ((st = potrs(c, Lc, nmu, nmu, Cinv, nmu, nmu, cs))) return st;
+  // zeta^T = C^{-1} Z^T: A = C^{-1} sliced by rows, B = Z^T sliced by columns (grid points).
+  if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, sz, sa, mu_kpad,
+                              mu_pad * mu_kpad, ea, mu_pad)))
+    return st;
+  if ((st = oz_slice_cols_f64(c, zt, nmu, ng, ng, sz, sb, ng_pad, mu_kpad * ng_pad, eb, mu_kpad,
+                              ng_pad)))
+    return st;
+  {
+    OzArgs g;
+    g.M = nmu; g.N = ng; g.K = nmu;
+    g.a.s = sa; g.a.e = ea; g.a.ld = mu_kpad; g.a.slice_stride = mu_pad * mu_kpad;
+    g.b.s = sb; g.b.e = eb; g.b.ld = ng_pad; g.b.slice_stride = mu_kpad * ng_pad;
+    g.b.k_contig = false;
+    g.levels = sz; g.epilogue = OZ_STORE_F32; g.C = zeta; g.ldc = ng;
+    if ((st = ozgemm(c, g))) return st;
+  }
+  // FP32 R2C FFT of every interpolating vector.
+  cufftHandle plan;
+  if ((st = get_plan(c, n0, n1, n2, nmu, CUFFT_R2C, &plan))) return st;
+  if (cufftExecR2C(plan, zeta, (cufftComplex*)zhat) != CUFFT_SUCCESS)
+    return set_error(c, THC_ERR_CUFFT, "cufftExecR2C failed");
+  c->launches++;
+  coulomb_weights_m<<<(int)cdiv(nc, 256), 256, 0, s>>>(coul, n0, n1, n2, dsym, danti, sq, n_anti);
+  THC_LAUNCHED(c, "coulomb_weights");
+  int h_anti = 0;
+  THC_CUDA(c, cudaMemcpyAsync(&h_anti, n_anti, sizeof(int), cudaMemcpyDeviceToHost, s));
+  // Re M (lower) = A A^T with A = zeta_hat (interleaved re, im) scaled by sqrt(w v_sym).
+  if ((st = oz_slice_rows_f32(c, (const float*)zhat, nmu, 2 * nc, 2 * nc, sq, 1, sm, sa, k2_pad,
+                              mu_pad * k2_pad, ea, mu_pad)))
+    return st;
+  double* mre = Mw;
+  double* xim = Mw + nn;
+  double* mcx = Mw + 2 * nn;
+  {
+    OzArgs g;
+    g.M = nmu; g.N = nmu; g.K = 2 * nc;
+    g.a.s = sa; g.a.e = ea; g.a.ld = k2_pad; g.a.slice_stride = mu_pad * k2_pad;
+    g.b = g.a;
+    g.b.k_contig = true;
+    g.levels = sm; g.epilogue = OZ_STORE_F64; g.C = mre; g.ldc = nmu; g.lower_only = 1;
+    if ((st = ozgemm(c, g))) return st;
+  }
+  THC_CUDA(c, cudaStreamSynchronize(s));
+  int nb2 = (int)cdiv(nn, 256);
+  if (h_anti > 0) {
+    imag_part_c64<<<nb2, 256, 0, s>>>(zhat, nc, nmu, danti, xim);
+    THC_LAUNCHED(c, "imag_part_c64");
+  }
+  assemble_m_m<<<nb2, 256, 0, s>>>(mre, h_anti > 0 ? xim : nullptr, nmu, mcx);
+  THC_LAUNCHED(c, "assemble_m");
+  init_cs<<<1, 1, 0, s>>>(csm);
+  THC_LAUNCHED(c, "init_cs");
+  double* Lout = Lw;
+  if (h_anti == 0) {
+    copy_lower_to_full_m<<<nb2, 256, 0, s>>>(mre, nmu, xim);
+    THC_LAUNCHED(c, "copy_lower_to_full");
+    if ((st = potrf(c, xim, nmu, nmu, zero, csm))) return st;
+    export_l_real_m<<<nb2, 256, 0, s>>>(xim, nmu, Lout);
+    THC_LAUNCHED(c, "export_l_real");
+  } else {
+    THC_CUDA(c, cudaMemcpyAsync(Lout, mcx, sizeof(double) * 2 * nn, cudaMemcpyDeviceToDevice, s));
+    if ((st = zpotrf_small(c, Lout, nmu, zero, csm))) return st;
+    zero_upper_complex_m<<<nb2, 256, 0, s>>>(Lout, nmu);
+    THC_LAUNCHED(c, "zero_upper_complex");
+  }
+  THC_CUDA(c, cudaEventRecord(c->ev1, s));
+  if (out_M) THC_CUDA(c, cudaMemcpyAsync(out_M, mcx, sizeof(double) * 2 * nn, cudaMemcpyDefault, s));
+  if (out_L) THC_CUDA(c, cudaMemcpyAsync(out_L, Lout, sizeof(double) * 2 * nn, cudaMemcpyDefault, s));
+  CholStatus hm{};
+  int hbad = 0;
+  double hshift = 0.0;
+  THC_CUDA(c, cudaMemcpyAsync(&hm, csm, sizeof(CholStatus), cudaMemcpyDeviceToHost, s));
+  THC_CUDA(c, cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  THC_CUDA(c, cudaMemcpyAsync(&hshift, shift_dev, sizeof(double), cudaMemcpyDeviceToHost, s));
+  THC_CUDA(c, cudaStreamSynchronize(s));
+  if (hbad) return set_error(c, THC_ERR_ARG, "thc_isdf: interpolating index out of range");
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    stats->chol_c_info = chol_c_info;
+    stats->chol_m_info = hm.flag ? hm.info : 0;
+    stats->rank_deficient = shifted ? 1 : 0;
+    stats->n_anti = h_anti;
+    stats->shift_used = hshift;
+    stats->c_min_pivot = hcs.max_piv > 0 ? hcs.min_piv / hcs.max_piv : 0.0;
+    stats->device_ms = ms;
+  }
+  if (hm.flag)
+    return set_error(c, THC_ERR_NOT_PD, "Cholesky decomposition failed: leading minor %d", hm.info);
+  return THC_OK;
+}
+
+}  // namespace thc

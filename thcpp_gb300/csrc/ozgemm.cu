@@ -1,0 +1,350 @@
+// Sliced-BF16 GEMM with exact chunk accumulation (see ozgemm.cuh for the scheme).
+//
+// Warp-level BF16 MMA (m16n8k16, FP32 accumulate), 4 warps per CTA, CTA tile 64 x 32,
+// warp tile 16 x 32; every level's FP32 accumulator is live for one 256-long k chunk and
+// is then folded into FP64 registers.  Operands are staged through shared memory with
+// cp.async (two stages) and read with ldmatrix.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "common.cuh"
+#include "ozgemm.cuh"
+
+namespace thc {
+
+namespace {
+
+constexpr int OBM = 64, OBN = 32, OBK = 32, OCHUNK = 256, OPAD = 8;
+constexpr int OLDA = OBK + OPAD;      // shared row length (bf16) of A and k-contiguous B
+constexpr int OLDBN = OBN + OPAD;     // shared row length of n-contiguous B
+
+__device__ __forceinline__ unsigned smem_u32(const void* p)
+{
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+__device__ __forceinline__ void ldsm_x4(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3,
+                                        const void* p)
+{
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x4_t(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3,
+                                          const void* p)
+{
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ void mma_bf16(float* d, const unsigned* a, unsigned b0, unsigned b1)
+{
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ double pow2(int e)
+{
+  // 2^e for the normal range; outside it fall back to ldexp.
+  if (e > -1022 && e < 1023) return __longlong_as_double((long long)(e + 1023) << 52);
+  return ldexp(1.0, e);
+}
+
+template <int LV, bool BK>
+__global__ void __launch_bounds__(128, 2) ozgemm_kernel(OzArgs g)
+{
+  const long long m0 = (long long)blockIdx.x * OBM;
+  const long long n0 = (long long)blockIdx.y * OBN;
+  if (g.lower_only && n0 > m0 + OBM - 1) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int a_stage = LV * OBM * OLDA;                       // bf16 elements per stage
+  const int b_stage = BK ? LV * OBN * OLDA : LV * OBK * OLDBN;
+  __nv_bfloat16* sA = (__nv_bfloat16*)smem;
+  __nv_bfloat16* sB = sA + 2 * a_stage;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  auto load_stage = [&](int buf, long long k0) {
+    __nv_bfloat16* dA = sA + buf * a_stage;
+    __nv_bfloat16* dB = sB + buf * b_stage;
+#pragma unroll
+    for (int s = 0; s < LV; s++) {
+      const __nv_bfloat16* ga = g.a.s + s * g.a.slice_stride + m0 * g.a.ld + k0;
+#pragma unroll
+      for (int r = 0; r < 2; r++) {
+        int ch = tid + 128 * r;        // 256 chunks of 16 B: 64 rows x 4
+        int row = ch >> 2, col = (ch & 3) * 8;
+        cp_async16(dA + (s * OBM + row) * OLDA + col, ga + row * g.a.ld + col);
+      }
+      if (BK) {
+        const __nv_bfloat16* gb = g.b.s + s * g.b.slice_stride + n0 * g.b.ld + k0;
+        int row = tid >> 2, col = (tid & 3) * 8;   // 32 rows (n) x 4 chunks
+        cp_async16(dB + (s * OBN + row) * OLDA + col, gb + row * g.b.ld + col);
+      } else {
+        const __nv_bfloat16* gb = g.b.s + s * g.b.slice_stride + k0 * g.b.ld + n0;
+        int row = tid >> 2, col = (tid & 3) * 8;   // 32 rows (k) x 4 chunks
+        cp_async16(dB + (s * OBK + row) * OLDBN + col, gb + row * g.b.ld + col);
+      }
+    }
+    cp_async_commit();
+  };
+
+  double acc64[4][4];
+#pragma unroll
+  for (int t = 0; t < 4; t++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc64[t][q] = 0.0;
+  float acc[LV][4][4];
+
+  const long long K = g.K;
+  long long nsteps = (K + OBK - 1) / OBK;
+  load_stage(0, 0);
+  int buf = 0;
+  for (long long st = 0; st < nsteps; st++) {
+    if ((st * OBK) % OCHUNK == 0) {
+#pragma unroll
+      for (int l = 0; l < LV; l++)
+#pragma unroll
+        for (int t = 0; t < 4; t++)
+#pragma unroll
+          for (int q = 0; q < 4; q++) acc[l][t][q] = 0.f;
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (st + 1 < nsteps) load_stage(buf ^ 1, (st + 1) * OBK);
+    const __nv_bfloat16* cA = sA + buf * a_stage;
+    const __nv_bfloat16* cB = sB + buf * b_stage;
+#pragma unroll
+    for (int kk = 0; kk < OBK; kk += 16) {
+      unsigned af[LV][4];
+#pragma unroll
+      for (int s = 0; s < LV; s++) {
+        const __nv_bfloat16* p = cA + (s * OBM + warp * 16 + (lane & 15)) * OLDA + kk + (lane >> 4) * 8;
+        ldsm_x4(af[s][0], af[s][1], af[s][2], af[s][3], p);
+      }
+#pragma unroll
+      for (int j = 0; j < LV; j++) {
+        unsigned bf[4][2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          unsigned r0, r1, r2, r3;
+          if (BK) {
+            int nrow = h * 16 + (lane >> 4) * 8 + (lane & 7);
+            int kof = kk + ((lane >> 3) & 1) * 8;
+            ldsm_x4(r0, r1, r2, r3, cB + (j * OBN + nrow) * OLDA + kof);
+          } else {
+            int krow = kk + ((lane >> 3) & 1) * 8 + (lane & 7);
+            int nof = h * 16 + (lane >> 4) * 8;
+            ldsm_x4_t(r0, r1, r2, r3, cB + (j * OBK + krow) * OLDBN + nof);
+          }
+          bf[2 * h][0] = r0; bf[2 * h][1] = r1;
+          bf[2 * h + 1][0] = r2; bf[2 * h + 1][1] = r3;
+        }
+#pragma unroll
+        for (int i = 0; i + j < LV; i++)
+#pragma unroll
+          for (int t = 0; t < 4; t++) mma_bf16(acc[i + j][t], af[i], bf[t][0], bf[t][1]);
+      }
+    }
+    if (((st + 1) * OBK) % OCHUNK == 0 || st + 1 == nsteps) {
+#pragma unroll
+      for (int l = 0; l < LV; l++) {
+        const double sc = pow2(-7 * l);
+#pragma unroll
+        for (int t = 0; t < 4; t++)
+#pragma unroll
+          for (int q = 0; q < 4; q++) acc64[t][q] = __fma_rn((double)acc[l][t][q], sc, acc64[t][q]);
+      }
+    }
+    buf ^= 1;
+  }
+  // Epilogue: thread holds rows (g, g+8) x cols (2t, 2t+1) of each n8 tile.
+  const int gr = lane >> 2, tc = (lane & 3) * 2;
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      long long m = m0 + warp * 16 + gr + (q >= 2 ? 8 : 0);
+      long long n = n0 + t * 8 + tc + (q & 1);
+      if (m >= g.M || n >= g.N) continue;
+      if (g.lower_only && n > m) continue;
+      double v = acc64[t][q] * pow2(g.a.e[m] + g.b.e[n] - 14);
+      if (g.epilogue == OZ_SQUARE_F64) v = v * v;
+      if (g.epilogue == OZ_STORE_F32)
+        ((float*)g.C)[m * g.ldc + n] = (float)v;
+      else
+        ((double*)g.C)[m * g.ldc + n] = v;
+    }
+  }
+}
+
+template <int LV>
+int launch_lv(Ctx* c, const OzArgs& g)
+{
+  size_t a_stage = (size_t)LV * OBM * OLDA;
+  size_t b_stage = g.b.k_contig ? (size_t)LV * OBN * OLDA : (size_t)LV * OBK * OLDBN;
+  size_t smem = 2 * (a_stage + b_stage) * sizeof(__nv_bfloat16);
+  dim3 grid((unsigned)cdiv(g.M, OBM), (unsigned)cdiv(g.N, OBN));
+  if (grid.y > 65535) return set_error(c, THC_ERR_SHAPE, "ozgemm: N too large");
+  if (g.b.k_contig) {
+    THC_CUDA(c, cudaFuncSetAttribute(ozgemm_kernel<LV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ozgemm_kernel<LV, true><<<grid, 128, smem, c->stream>>>(g);
+  } else {
+    THC_CUDA(c, cudaFuncSetAttribute(ozgemm_kernel<LV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ozgemm_kernel<LV, false><<<grid, 128, smem, c->stream>>>(g);
+  }
+  THC_LAUNCHED(c, "ozgemm");
+  return THC_OK;
+}
+
+// One warp per row: exponent from the row maximum, then the slices (FP64 input; every
+// step -- the power-of-two scaling, rint, the subtraction and the *128 -- is exact).
+__global__ void slice_rows_kernel(const double* __restrict__ X, long long rows, long long cols,
+                                  long long ldx, long long sc, const double* __restrict__ scale,
+                                  int shift, int ns, __nv_bfloat16* out, long long ldo,
+                                  long long sstride, int* exps, long long rows_pad)
+{
+  long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (r >= rows_pad) return;
+  auto val = [&](long long cidx) -> double {
+    double v = X[r * ldx + cidx * sc];
+    if (scale) v *= scale[cidx >> shift];
+    return v;
+  };
+  double mx = 0.0;
+  if (r < rows)
+    for (long long cc = lane; cc < cols; cc += 32) mx = fmax(mx, fabs(val(cc)));
+  for (int off = 16; off; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  int e = 0;
+  if (mx > 0.0) frexp(mx, &e);
+  if (lane == 0) exps[r] = e;
+  for (long long cc = lane; cc < ldo; cc += 32) {
+    double x = (r < rows && cc < cols) ? ldexp(val(cc), 7 - e) : 0.0;
+    for (int s = 0; s < ns; s++) {
+      double q = rint(x);
+      out[s * sstride + r * ldo + cc] = __double2bfloat16(q);
+      x = (x - q) * 128.0;
+    }
+  }
+}
+
+// FP32 input scaled by an FP32 copy of `scale`: the product is rounded once to FP32 and
+// then sliced exactly in FP32 arithmetic.
+__global__ void slice_rows_f32_kernel(const float* __restrict__ X, long long rows,
+                                      long long cols, long long ldx,
+                                      const float* __restrict__ scale, int shift, int ns,
+                                      __nv_bfloat16* out, long long ldo, long long sstride,
+                                      int* exps, long long rows_pad)
+{
+  long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (r >= rows_pad) return;
+  auto val = [&](long long cidx) -> float {
+    float v = X[r * ldx + cidx];
+    if (scale) v *= scale[cidx >> shift];
+    return v;
+  };
+  float mx = 0.f;
+  if (r < rows)
+    for (long long cc = lane; cc < cols; cc += 32) mx = fmaxf(mx, fabsf(val(cc)));
+  for (int off = 16; off; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  int e = 0;
+  if (mx > 0.f) frexpf(mx, &e);
+  if (lane == 0) exps[r] = e;
+  for (long long cc = lane; cc < ldo; cc += 32) {
+    float x = (r < rows && cc < cols) ? ldexpf(val(cc), 7 - e) : 0.f;
+    for (int s = 0; s < ns; s++) {
+      float q = rintf(x);
+      out[s * sstride + r * ldo + cc] = __float2bfloat16_rn(q);
+      x = (x - q) * 128.f;
+    }
+  }
+}
+
+// One thread per column: exponent from the column maximum, then the slices.
+__global__ void slice_cols_kernel(const double* __restrict__ X, long long rows, long long cols,
+                                  long long ldx, int ns, __nv_bfloat16* out, long long ldo,
+                                  long long sstride, int* exps, long long rows_pad,
+                                  long long cols_pad)
+{
+  long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (n >= cols_pad) return;
+  double mx = 0.0;
+  if (n < cols)
+    for (long long k = 0; k < rows; k++) mx = fmax(mx, fabs(X[k * ldx + n]));
+  int e = 0;
+  if (mx > 0.0) frexp(mx, &e);
+  exps[n] = e;
+  for (long long k = 0; k < rows_pad; k++) {
+    double x = (n < cols && k < rows) ? ldexp(X[k * ldx + n], 7 - e) : 0.0;
+    for (int s = 0; s < ns; s++) {
+      double q = rint(x);
+      out[s * sstride + k * ldo + n] = __double2bfloat16(q);
+      x = (x - q) * 128.0;
+    }
+  }
+}
+
+}  // namespace
+
+int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
+                      long long sc, const double* scale, int scale_shift, int nslices,
+                      __nv_bfloat16* out, long long ldo, long long slice_stride, int* exps,
+                      long long rows_pad)
+{
+  long long threads = rows_pad * 32;
+  slice_rows_kernel<<<(unsigned)cdiv(threads, 256), 256, 0, c->stream>>>(
+      X, rows, cols, ldx, sc, scale, scale_shift, nslices, out, ldo, slice_stride, exps, rows_pad);
+  THC_LAUNCHED(c, "slice_rows_f64");
+  return THC_OK;
+}
+
+int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, long long ldx,
+                      const float* scale, int scale_shift, int nslices, __nv_bfloat16* out,
+                      long long ldo, long long slice_stride, int* exps, long long rows_pad)
+{
+  long long threads = rows_pad * 32;
+  slice_rows_f32_kernel<<<(unsigned)cdiv(threads, 256), 256, 0, c->stream>>>(
+      X, rows, cols, ldx, scale, scale_shift, nslices, out, ldo, slice_stride, exps, rows_pad);
+  THC_LAUNCHED(c, "slice_rows_f32");
+  return THC_OK;
+}
+
+int oz_slice_cols_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
+                      int nslices, __nv_bfloat16* out, long long ldo, long long slice_stride,
+                      int* exps, long long rows_pad, long long cols_pad)
+{
+  slice_cols_kernel<<<(unsigned)cdiv(cols_pad, 256), 256, 0, c->stream>>>(
+      X, rows, cols, ldx, nslices, out, ldo, slice_stride, exps, rows_pad, cols_pad);
+  THC_LAUNCHED(c, "slice_cols_f64");
+  return THC_OK;
+}
+
+int ozgemm(Ctx* c, const OzArgs& g)
+{
+  if (g.M <= 0 || g.N <= 0) return THC_OK;
+  switch (g.levels) {
+    case 2: return launch_lv<2>(c, g);
+    case 3: return launch_lv<3>(c, g);
+    case 4: return launch_lv<4>(c, g);
+    case 5: return launch_lv<5>(c, g);
+    case 6: return launch_lv<6>(c, g);
+    case 7: return launch_lv<7>(c, g);
+    default: return set_error(c, THC_ERR_ARG, "ozgemm: levels must be 2..7");
+  }
+}
+
+}  // namespace thc

@@ -1,0 +1,64 @@
+// Error-free sliced-BF16 GEMM ("Ozaki"-style splitting onto BF16 tensor cores).
+//
+// Each row of A (each column of B) is scaled by a power of two 2^e so that its entries lie
+// in (-1, 1), then split into s integer slices of 7 bits:
+//     x = 2^e * sum_{i<s} S_i 2^{-7(i+1)},  |S_0| <= 128, |S_i| <= 64 (i >= 1),
+// every slice exactly representable in BF16.  The product keeps the slice pairs with
+// i + j <= L (L = s - 1):
+//     C[m,n] = 2^{eA[m] + eB[n] - 14} sum_{l<=L} 2^{-7 l} sum_{i+j=l} sum_k S_i[m,k] T_j[k,n].
+// Every slice product is an integer below 2^14 in magnitude and every level sum over a
+// chunk of 256 k is an integer below 2^24, so the tensor cores' FP32 accumulation of a
+// chunk is exact; chunks are combined in FP64.  The only error is the truncation of the
+// slice expansion, about (L+2) 2^{-7(L+1)} relative to sum_k |A||B|.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace thc {
+
+enum OzEpilogue : int { OZ_STORE_F64 = 0, OZ_SQUARE_F64 = 1, OZ_STORE_F32 = 2 };
+
+struct OzOperand {
+  const __nv_bfloat16* s = nullptr;  // slices
+  const int* e = nullptr;            // exponent per row (A) / per column (B)
+  long long ld = 0;                  // elements between consecutive rows of one slice
+  long long slice_stride = 0;        // elements between slices
+  bool k_contig = true;              // B only: true for [n][k] storage, false for [k][n]
+};
+
+struct OzArgs {
+  long long M = 0, N = 0, K = 0;     // logical sizes; slice buffers are zero padded to
+                                     // multiples of the tile sizes (64 in M/N, 32 in K)
+  OzOperand a, b;
+  int levels = 5;                    // L + 1 = number of slices used
+  int epilogue = OZ_STORE_F64;
+  void* C = nullptr;
+  long long ldc = 0;
+  int lower_only = 0;
+};
+
+// Padded sizes expected by ozgemm for the slice buffers.
+inline long long oz_pad_mn(long long x) { return (x + 63) / 64 * 64; }
+inline long long oz_pad_k(long long x) { return (x + 31) / 32 * 32; }
+
+// Slice rows of a matrix X (rows x cols, element (r, c) at X[r*ldx + c*sc]) into
+// out[slice][r][c] (row length ldo, padded entries zero) with one exponent per row.
+// `scale` (optional, length cols, indexed c >> scale_shift) multiplies entries first.
+int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
+                      long long sc, const double* scale, int scale_shift, int nslices,
+                      __nv_bfloat16* out, long long ldo, long long slice_stride, int* exps,
+                      long long rows_pad);
+int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, long long ldx,
+                      const float* scale, int scale_shift, int nslices, __nv_bfloat16* out,
+                      long long ldo, long long slice_stride, int* exps, long long rows_pad);
+// Slice columns of X (rows = k, cols = n, X[k*ldx + n]) into out[slice][k][n] with one
+// exponent per column n.
+int oz_slice_cols_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
+                      int nslices, __nv_bfloat16* out, long long ldo, long long slice_stride,
+                      int* exps, long long rows_pad, long long cols_pad);
+
+int ozgemm(Ctx* c, const OzArgs& g);
+
+}  // namespace thc
