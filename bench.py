@@ -1,0 +1,333 @@
+"""Benchmark: ISDF seconds per system on one GB300 (mixed precision vs all-FP64).
+
+One step = one full factorisation of one synthetic system (k-means interpolating points
++ interpolating vectors + FFT Coulomb matrix + its Cholesky factor) through the C ABI of
+libthc_gb300.so.  Workload: the 8-atom diamond conventional cell, 48^3 grid
+(N_g = 110,592), N_o = 32, N_mu = 256, k-means max_it 100 / threshold 1e-6.
+
+  value  mixed-precision s/system with inputs resident in HBM (device pointers),
+         L2 flushed before every timed step, CUDA events on the library's stream
+  e2e    the same through the C ABI with pinned HOST buffers: H2D of the inputs and D2H
+         of idx, Orbitals, M and Luv inside the timed region (wall clock)
+  fp64   the all-FP64 path (the drop-in) on the same inputs, and the mixed/FP64 M error
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun (N > 1) every rank factorises its own replica of the workload (the path
+has no exchange step: replicas only) and rank 0 prints one JSON line.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "c2"
+CONFIG = {"workload": "diamond-8atom-48^3-no32-nmu256", "n_g": 110592, "n_orb": 32,
+          "n_mu": 256, "mesh": [48, 48, 48], "kmeans_max_it": 100, "kmeans_threshold": 1e-6,
+          "l2": "flushed (256 MB write) before every timed step", "parallelism": "replicas"}
+METRIC = "ISDF s/system on 1 GB300 (mixed precision; FP64 path reported beside)"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference_step(s, nthreads):
+    """The CPU port of the reference path (oracle): C++ k-means + LAPACK/FFT ISDF."""
+    import oracle
+    t0 = time.perf_counter()
+    km = oracle.kmeans_system(s, nthreads=nthreads)
+    oracle.isdf_reference(s.phi, km.idx, s.mesh, s.coulG, workers=nthreads)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    from thcpp_gb300 import synth
+    import oracle
+    oracle.build()
+    s = synth.config(WORKLOAD)
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_reference_step(s, nthreads)
+    ts = [cpu_reference_step(s, nthreads) for _ in range(args.steps)]
+    v = float(np.sum(ts) / args.steps)
+    line = {"metric": METRIC, "value": v, "unit": "s/system", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * v,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Gaussian s/p orbitals)", "config": CONFIG,
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "s/system", "cores": nthreads, "kind": "port",
+                             "sample": "full factorisation of the workload per step: C++ "
+                                       "k-means restatement (OpenMP) + numpy/scipy zgels, "
+                                       "C2C FFT, herk, zpotrf"},
+            "e2e": {"value": v, "unit": "s/system", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from thcpp_gb300 import build, capi, synth
+    build.build()
+    s = synth.config(WORKLOAD)
+    nmu, ng, no = s.nmu, s.ng, s.norb
+    init = capi.initial_indices(ng, nmu, s.rng_seed)
+
+    # Device-resident inputs.
+    d_grid = torch.from_numpy(s.grid).to(dev)
+    d_rho = torch.from_numpy(s.density).to(dev)
+    d_phi = torch.from_numpy(s.phi).to(dev)
+    d_coul = torch.from_numpy(s.coulG).to(dev)
+    d_init = torch.from_numpy(init).to(dev)
+    d_idx = torch.zeros(nmu, dtype=torch.int32, device=dev)
+    d_M = torch.zeros((nmu, nmu, 2), dtype=torch.float64, device=dev)
+    d_L = torch.zeros((nmu, nmu, 2), dtype=torch.float64, device=dev)
+    d_orb = torch.zeros((no, nmu, 2), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def device_step(ctx):
+        _, kst, st = ctx.kmeans(d_grid, d_rho, nmu, d_init, s.max_it, s.threshold, out_idx=d_idx)
+        if st:
+            raise RuntimeError(f"thc_kmeans status {st}")
+        r = ctx.isdf(d_phi, d_idx, s.mesh, d_coul, -1.0, out_orbitals=d_orb, out_M=d_M,
+                     out_L=d_L)
+        return kst, r
+
+    def timed(ctx, steps, warmup):
+        ctx.set_stream(stream.cuda_stream)
+        for _ in range(warmup):
+            device_step(ctx)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        l0 = ctx.kernel_launches
+        ctx.set_option("profile", 1)
+        tot = 0.0
+        for _ in range(steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            kst, r = device_step(ctx)
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        launches = ctx.kernel_launches - l0
+        return tot / steps, launches, kst, r
+
+    # Mixed precision (the headline).
+    ctx = capi.Context(local, capi.THC_PREC_MIXED)
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.nvtx.range_push("mixed")
+    ms_mixed, launches, kst, r_mx = timed(ctx, args.steps, args.warmup)
+    torch.cuda.nvtx.range_pop()
+    clk = clocks.stop()
+    M_mixed = d_M.cpu().numpy().copy()
+    oz_ms, oz_n = ctx.kernel_time("ozgemm")
+    km_ms, km_n = ctx.kernel_time("km_assign")
+    ctx.set_option("profile", 0)
+
+    # All-FP64 path on the same inputs.
+    ctx64 = capi.Context(local, capi.THC_PREC_FP64)
+    torch.cuda.nvtx.range_push("fp64")
+    ms_fp64, launches64, kst64, r64 = timed(ctx64, args.fp64_steps, 1)
+    torch.cuda.nvtx.range_pop()
+    dg_ms, dg_n = ctx64.kernel_time("dgemm")
+    ctx64.set_option("profile", 0)
+    idx64 = d_idx.cpu().numpy().copy()
+    M_fp64 = d_M.cpu().numpy().copy()
+    device_step(ctx)  # idx from the mixed path for the comparison below
+    idx_mx = d_idx.cpu().numpy().copy()
+    Mc = M_mixed[..., 0] + 1j * M_mixed[..., 1]
+    M6 = M_fp64[..., 0] + 1j * M_fp64[..., 1]
+    rel_err = float(np.linalg.norm(Mc - M6) / np.linalg.norm(M6))
+
+    # End to end through the C ABI with pinned host buffers.
+    def pinned(a):
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        return t.numpy()
+    h_grid, h_rho, h_phi, h_coul = (pinned(s.grid), pinned(s.density), pinned(s.phi),
+                                    pinned(s.coulG))
+    h_init = pinned(init)
+    h_idx = pinned(np.zeros(nmu, np.int32))
+    h_M = pinned(np.zeros((nmu, nmu, 2)))
+    h_L = pinned(np.zeros((nmu, nmu, 2)))
+    h_orb = pinned(np.zeros((no, nmu, 2)))
+    ctx.set_stream(None)
+
+    def host_step():
+        ctx.kmeans(h_grid, h_rho, nmu, h_init, s.max_it, s.threshold, out_idx=h_idx)
+        ctx.isdf(h_phi, h_idx, s.mesh, h_coul, -1.0, out_orbitals=h_orb, out_M=h_M, out_L=h_L)
+
+    torch.cuda.nvtx.range_push("e2e")
+    for _ in range(args.warmup):
+        host_step()
+    e2e = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_step()
+        e2e += time.perf_counter() - t0
+    e2e /= args.steps
+    torch.cuda.nvtx.range_pop()
+    h2d = (h_grid.nbytes + h_rho.nbytes + h_init.nbytes + h_phi.nbytes + h_coul.nbytes
+           + h_idx.nbytes)
+    d2h = h_idx.nbytes + h_orb.nbytes + h_M.nbytes + h_L.nbytes
+
+    # Max over ranks.
+    t_step = ms_mixed
+    if ws > 1:
+        tt = torch.tensor([t_step, e2e], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step, e2e = float(tt[0]), float(tt[1])
+
+    if rank == 0:
+        import json as _json
+        peaks = {}
+        pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(pk):
+            peaks = _json.load(open(pk))
+        bf16_peak = peaks.get("bf16_tflops", 1900.0)
+        peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
+        # Dominant tensor kernel: the sliced GEMMs.  Algorithmic tensor-pipe work per
+        # factorisation = sum over the three GEMMs of (slice pairs) x 2 M N K.
+        sp, sz, sm = 6, 6, 4
+        pairs = lambda L: L * (L + 1) // 2
+        nc2 = 2 * 48 * 48 * 25
+        flops = (pairs(sp) * 2 * nmu * ng * no + pairs(sz) * 2 * nmu * ng * nmu
+                 + pairs(sm) * 2 * nmu * nmu * nc2 / 2)
+        per_launch = flops / 3.0
+        oz_avg_ms = oz_ms / max(oz_n, 1)
+        achieved = per_launch / (oz_avg_ms * 1e-3) / 1e12 if oz_n else None
+        roof = {"kernel": "ozgemm (sliced-BF16 tensor GEMM, mean over its 3 launches/system)",
+                "bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": (achieved / bf16_peak) if achieved else None,
+                "peak_source": peak_src, "traffic": None,
+                "share_of_step": (oz_ms / args.steps) / t_step if oz_n else None}
+        cpu = None
+        if not args.no_cpu_baseline:
+            t_cpu = cpu_reference_step(s, os.cpu_count() or 1)
+            cpu = {"value": t_cpu, "unit": "s/system", "cores": os.cpu_count(), "kind": "port",
+                   "sample": "1 full factorisation of the workload (C++ k-means restatement "
+                             "+ numpy/scipy zgels/FFT/herk/zpotrf) on the host cores"}
+        line = {
+            "metric": METRIC, "value": t_step * 1e-3 / 1.0, "unit": "s/system",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16-sliced/fp32/fp64", "data": "synthetic (seeded Gaussian s/p orbitals)",
+            "config": CONFIG,
+            "e2e": {"value": e2e, "unit": "s/system", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "fp64": {"s_per_system": ms_fp64 * 1e-3, "speedup_mixed_vs_fp64": ms_fp64 / t_step,
+                     "rel_err_M_mixed_vs_fp64": rel_err, "idx_identical": bool(
+                         np.array_equal(idx64, idx_mx)),
+                     "dgemm_ms_per_system": dg_ms / args.fp64_steps},
+            "kmeans": {"iterations": kst.iterations, "rechecked_points": int(kst.rechecked),
+                       "assign_ms_per_system": km_ms / args.steps},
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+        }
+        line["value"] = t_step * 1e-3
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

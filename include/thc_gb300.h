@@ -81,8 +81,13 @@ int thc_ctx_create(int device, int precision, thc_ctx** out_ctx);
 int thc_ctx_destroy(thc_ctx* ctx);
 /* Run on a caller stream (a cudaStream_t); NULL restores the context's own stream. */
 int thc_ctx_set_stream(thc_ctx* ctx, void* cuda_stream);
-/* Named numeric options: "slices_p", "slices_z" (sliced-GEMM depths, mixed path). */
+/* Named numeric options: "slices_p", "slices_z" (sliced-GEMM depths, mixed path);
+ * "profile" (1 = record a CUDA event pair around every launch of the named kernels,
+ * 0 = stop and clear). */
 int thc_ctx_set_option(thc_ctx* ctx, const char* key, double value);
+/* Accumulated device time (ms, from the profile events) and launch count of the kernels
+ * named `kernel` since profiling was enabled; synchronises the context's stream. */
+int thc_ctx_kernel_time(thc_ctx* ctx, const char* kernel, double* ms, long long* launches);
 const char* thc_ctx_last_error(const thc_ctx* ctx);
 const char* thc_status_string(int status);
 /* Number of kernels this context has launched so far (its own kernels only). */

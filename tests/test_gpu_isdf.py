@@ -74,18 +74,30 @@ def test_isdf_fp64_vs_reference_qr_c2(gpu_ctx_fp64):
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_isdf_rank_deficient_c1(request, prec):
+    """C1: N_mu = 64 exceeds the 36 independent orbital-pair products, so C is singular.
+
+    The shifted Cholesky pins M on range(C); the null-space block of M is amplified
+    rounding noise in any implementation (the reference's QR included).  Parity is checked
+    on M projected onto range(C) and on the invariant THC reconstruction of the
+    orbital-pair Coulomb integrals.
+    """
     ctx = request.getfixturevalue("gpu_ctx_fp64" if prec == "fp64" else "gpu_ctx_mixed")
     s, idx, r = _run(ctx, "c1")
     st = r["stats"]
     assert st.rank_deficient == 1 and st.chol_c_info > 0 and st.n_anti > 0
     pm = s.phi[idx]
-    tr = np.trace((pm @ pm.T) ** 2) / s.nmu
+    C = (pm @ pm.T) ** 2
+    tr = np.trace(C) / s.nmu
     assert abs(st.shift_used - 1e-10 * tr) < 1e-12 * tr
     ref = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG, shift=1e-10 * tr)
     M = _cplx(r["M"])
-    err = _rel(M, ref["M"])
-    print(f"c1 {prec}: ||dM||/||M|| = {err:.3e}")
-    assert err < 1e-6
+    w, V = np.linalg.eigh(C)
+    Vr = V[:, w > 1e-12 * w[-1]]
+    assert Vr.shape[1] == s.norb * (s.norb + 1) // 2
+    proj = lambda X: Vr.T @ X @ Vr
+    err = _rel(proj(M), proj(ref["M"]))
+    print(f"c1 {prec}: range(C) ||dM||/||M|| = {err:.3e}, full {_rel(M, ref['M']):.3e}")
+    assert err < (1e-9 if prec == "fp64" else 1e-6)
     pairs = [(i, j) for i in range(s.norb) for j in range(i, s.norb)]
     ex = oracle.pair_coulomb_exact(s.phi, s.mesh, s.coulG, pairs)
     th = oracle.thc_pair_coulomb(s.phi, idx, M, pairs)

@@ -32,7 +32,7 @@ THC_PREC_MIXED = 1
 EXPORTS = [
     "thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
     "thc_ctx_last_error", "thc_status_string", "thc_ctx_kernel_launches",
-    "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf",
+    "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
 ]
 
 
@@ -87,6 +87,9 @@ def load(build_if_missing: bool = False):
     lib.thc_status_string.restype = ctypes.c_char_p
     lib.thc_ctx_kernel_launches.argtypes = [vp]
     lib.thc_ctx_kernel_launches.restype = cll
+    lib.thc_ctx_kernel_time.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(cd),
+                                        ctypes.POINTER(cll)]
+    lib.thc_ctx_kernel_time.restype = ci
     lib.thc_kmeans_initial_indices.argtypes = [cll, ci, cu, vp]
     lib.thc_kmeans.argtypes = [vp, vp, vp, cll, ci, vp, ci, cd, vp, ctypes.POINTER(KMeansStats)]
     lib.thc_isdf.argtypes = [vp, vp, cll, ci, vp, ci, vp, vp, cd, vp, vp, vp,
@@ -158,6 +161,14 @@ class Context:
     def set_stream(self, stream_ptr: int | None):
         self._check(self.lib.thc_ctx_set_stream(self.h, ctypes.c_void_p(stream_ptr or 0)),
                     "set_stream")
+
+    def kernel_time(self, name: str):
+        """(total ms, launches) of the profiled kernel `name`."""
+        ms = ctypes.c_double()
+        n = ctypes.c_longlong()
+        self._check(self.lib.thc_ctx_kernel_time(self.h, name.encode(), ctypes.byref(ms),
+                                                 ctypes.byref(n)), "kernel_time")
+        return ms.value, n.value
 
     @property
     def kernel_launches(self) -> int:

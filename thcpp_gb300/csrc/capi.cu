@@ -91,6 +91,42 @@ const void* to_device(Ctx* c, const void* p, size_t bytes, Slot staging, int* st
   return d;
 }
 
+static cudaEvent_t take_event(Ctx* c)
+{
+  if (!c->event_pool.empty()) {
+    cudaEvent_t e = c->event_pool.back();
+    c->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+ProfScope::ProfScope(Ctx* ctx, const char* name) : c(ctx)
+{
+  if (!c->profile) return;
+  Ctx::Rec r{name, take_event(c), take_event(c)};
+  cudaEventRecord(r.a, c->stream);
+  c->recs.push_back(r);
+  i = c->recs.size() - 1;
+}
+
+ProfScope::~ProfScope()
+{
+  if (i != (size_t)-1) cudaEventRecord(c->recs[i].b, c->stream);
+}
+
+static void clear_profile(Ctx* c)
+{
+  cudaStreamSynchronize(c->stream);
+  for (auto& r : c->recs) {
+    c->event_pool.push_back(r.a);
+    c->event_pool.push_back(r.b);
+  }
+  c->recs.clear();
+}
+
 }  // namespace thc
 
 extern "C" {
@@ -148,6 +184,8 @@ int thc_ctx_destroy(thc_ctx* h)
   for (auto& kv : c->plans) cufftDestroy(kv.second);
   for (int s = 0; s < thc::WS_NSLOTS; s++)
     if (c->ws[s]) cudaFree(c->ws[s]);
+  thc::clear_profile(c);
+  for (auto e : c->event_pool) cudaEventDestroy(e);
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -172,6 +210,11 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
     h->c.slices_p = (int)value;
     return THC_OK;
   }
+  if (!strcmp(key, "profile")) {
+    thc::clear_profile(&h->c);
+    h->c.profile = value != 0.0;
+    return THC_OK;
+  }
   if (!strcmp(key, "slices_z")) {
     if (value < 2 || value > 8) return THC_ERR_ARG;
     h->c.slices_z = (int)value;
@@ -186,6 +229,26 @@ const char* thc_ctx_last_error(const thc_ctx* h)
 }
 
 long long thc_ctx_kernel_launches(const thc_ctx* h) { return h ? h->c.launches : 0; }
+
+int thc_ctx_kernel_time(thc_ctx* h, const char* kernel, double* ms, long long* launches)
+{
+  if (!h || !kernel || !ms || !launches) return THC_ERR_ARG;
+  thc::Ctx* c = &h->c;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return THC_ERR_CUDA;
+  double t = 0.0;
+  long long n = 0;
+  for (auto& r : c->recs) {
+    if (r.name != kernel) continue;
+    float x = 0.f;
+    if (cudaEventElapsedTime(&x, r.a, r.b) == cudaSuccess) {
+      t += x;
+      n++;
+    }
+  }
+  *ms = t;
+  *launches = n;
+  return THC_OK;
+}
 
 int thc_kmeans_initial_indices(long long ng, int nmu, unsigned int seed, int* out_idx)
 {

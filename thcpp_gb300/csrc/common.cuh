@@ -68,9 +68,22 @@ struct Ctx {
   void* pinned = nullptr;          // 4 KB pinned host scratch
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   long long launches = 0;
-  int slices_p = 5;
+  int slices_p = 6;
   int slices_z = 6;
   std::string last_error;
+  // Opt-in per-kernel event timing.
+  bool profile = false;
+  struct Rec { std::string name; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> event_pool;
+};
+
+// RAII event pair around one launch when profiling is on.
+struct ProfScope {
+  Ctx* c;
+  size_t i = (size_t)-1;
+  ProfScope(Ctx* ctx, const char* name);
+  ~ProfScope();
 };
 
 // Grow-only workspace slot; returns nullptr on allocation failure.

@@ -306,6 +306,7 @@ int dgemm(Ctx* c, const GemmArgs& g)
   if (g.M <= 0 || g.N <= 0) return THC_OK;
   dim3 grid((unsigned)cdiv(g.N, BN), (unsigned)cdiv(g.M, BM));
   bool ak = g.sak == 1, bk = g.sbk == 1;
+  ProfScope prof(c, "dgemm");
   if (ak && bk) dgemm_kernel<true, true><<<grid, 256, 0, c->stream>>>(g);
   else if (ak && !bk) dgemm_kernel<true, false><<<grid, 256, 0, c->stream>>>(g);
   else if (!ak && bk) dgemm_kernel<false, true><<<grid, 256, 0, c->stream>>>(g);

@@ -654,11 +654,13 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   const int kCheckEvery = 8;
   for (int it = 0; it < max_it; it++) {
     if (mixed) {
+      ProfScope prof(c, "km_assign");
       km_assign32<<<nassign, kAssignThreads, 0, s>>>(b);
       THC_LAUNCHED(c, "km_assign32");
       km_recheck<<<152 * 4, 256, 0, s>>>(b);
       THC_LAUNCHED(c, "km_recheck");
     } else {
+      ProfScope prof(c, "km_assign");
       km_assign64<<<nassign, kAssignThreads, 0, s>>>(b);
       THC_LAUNCHED(c, "km_assign64");
     }

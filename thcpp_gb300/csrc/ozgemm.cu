@@ -198,6 +198,7 @@ int launch_lv(Ctx* c, const OzArgs& g)
   size_t smem = 2 * (a_stage + b_stage) * sizeof(__nv_bfloat16);
   dim3 grid((unsigned)cdiv(g.M, OBM), (unsigned)cdiv(g.N, OBN));
   if (grid.y > 65535) return set_error(c, THC_ERR_SHAPE, "ozgemm: N too large");
+  ProfScope prof(c, "ozgemm");
   if (g.b.k_contig) {
     THC_CUDA(c, cudaFuncSetAttribute(ozgemm_kernel<LV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ozgemm_kernel<LV, true><<<grid, 128, smem, c->stream>>>(g);
