@@ -113,6 +113,13 @@ int thc_kmeans(thc_ctx* ctx, const double* grid, const double* rho, long long ng
                thc_kmeans_stats* stats);
 
 /*
+ * Per-iteration history of the last thc_kmeans call on this context: the normed
+ * difference and the % of labels changed (the reference prints every 10th,
+ * src/kmeans.cpp:238).  n must not exceed the last call's iteration count.
+ */
+int thc_kmeans_history(thc_ctx* ctx, double* diff, double* pct_changed, int n);
+
+/*
  * ISDF interpolating vectors + FFT Coulomb matrix + its Cholesky factor.
  *   phi           ng x norb doubles, C order: the real part of `aoR` (real orbitals)
  *   idx           nmu grid indices (the k-means output)

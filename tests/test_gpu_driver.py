@@ -1,0 +1,61 @@
+"""The drop-in C++ driver (thcpp_gb300.x: IPoints -> IVecs -> dump_qmcpack_data) end to end."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from thcpp_gb300 import build, capi, h5, synth
+from tests.conftest import system
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_driver_tiny(tmp_path, lib, precision):
+    build.build_host()
+    s = system("tiny")
+    orb = str(tmp_path / "orbitals.h5")
+    out = str(tmp_path / "thc.h5")
+    synth.write_orbital_file(s, orb)
+    inp = tmp_path / "input.json"
+    inp.write_text(json.dumps(synth.input_json(s, orb, out, precision=precision)))
+    r = subprocess.run([build.DRIVER, str(inp)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Finding interpolation points using K-Means" in r.stdout
+    ref = oracle.kmeans_system(s)
+    f = h5.Reader(out)
+    idx = f.read("/Hamiltonian/THC/InterpIndx")
+    assert np.array_equal(idx, ref.idx)
+    orbs = f.read("/Hamiltonian/THC/Orbitals")
+    assert orbs.shape == (s.norb, s.nmu, 2)
+    assert np.array_equal(orbs[..., 0], s.phi[ref.idx].T) and not orbs[..., 1].any()
+    L = f.read("/Hamiltonian/THC/Luv")
+    assert L.shape == (s.nmu, s.nmu, 2)
+    Lc = L[..., 0] + 1j * L[..., 1]
+    assert np.allclose(np.triu(Lc, 1), 0)
+    isd = oracle.isdf_real(s.phi, ref.idx, s.mesh, s.coulG)
+    M = Lc @ Lc.conj().T
+    assert np.linalg.norm(M - isd["M"]) / np.linalg.norm(isd["M"]) < 1e-6
+    assert f.read("/Hamiltonian/THC/dims").tolist() == [s.norb, s.nmu, s.nmu]
+    assert f.read("/Hamiltonian/dims").tolist() == [-1, 0, 0, s.norb, s.nocc, s.nocc, 0, 0]
+    assert f.read("/Hamiltonian/occups").tolist() == [0] * (2 * s.nocc)
+    assert f.read("/Hamiltonian/hcore").shape == (s.norb, s.norb, 2)
+    assert f.read("/Hamiltonian/Energies").shape == (1,)
+
+
+def test_driver_empty_cluster_exits(tmp_path, lib):
+    """Reference behaviour: CRITICAL ERROR message and exit(1) (src/kmeans.cpp:137-143)."""
+    s = system("tiny")
+    orb = str(tmp_path / "orbitals.h5")
+    out = str(tmp_path / "thc.h5")
+    # zero density everywhere -> every cluster weight falls below 1e-8
+    z = synth.System(**{**s.__dict__, "density": np.zeros_like(s.density)})
+    synth.write_orbital_file(z, orb)
+    inp = tmp_path / "input.json"
+    inp.write_text(json.dumps(synth.input_json(z, orb, out)))
+    r = subprocess.run([build.DRIVER, str(inp)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 1
+    assert "CRITICAL ERROR: Found centroid with weight ~ 0" in r.stdout

@@ -22,6 +22,12 @@ LIB = os.path.join(LIBDIR, "libthc_gb300.so")
 
 CUDA_SOURCES = ["capi.cu", "kmeans.cu", "dense64.cu", "isdf.cu", "mixed.cu", "ozgemm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+HOST = os.path.join(PKG, "host")
+HOST_SOURCES = ["h5lite.cpp", "h5lite_capi.cpp", "gpu_context.cpp", "kmeans.cpp", "interpolating_points.cpp",
+                "interpolating_vectors.cpp"]
+HOST_LIB = os.path.join(LIBDIR, "libthcpp_host.so")
+BINDIR = os.path.join(PKG, "bin")
+DRIVER = os.path.join(BINDIR, "thcpp_gb300.x")
 
 
 def nvcc() -> str:
@@ -78,7 +84,41 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
         os.replace(tmp, LIB)
+    build_host(force=force, verbose=verbose)
     return LIB
+
+
+def _have_zlib() -> bool:
+    return os.path.exists("/usr/include/zlib.h")
+
+
+def build_host(force: bool = False, verbose: bool = False) -> str:
+    """The C++ drop-in layer (solver classes + HDF5 I/O) and the thcpp_gb300.x driver."""
+    os.makedirs(BINDIR, exist_ok=True)
+    srcs = [os.path.join(HOST, f) for f in HOST_SOURCES]
+    hdrs = glob.glob(os.path.join(HOST, "*.h")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+    zlib = ["-lz"] if _have_zlib() else []
+    gxx = shutil.which("g++") or "g++"
+    if force or _stale(HOST_LIB, srcs + hdrs + [LIB]):
+        tmp = HOST_LIB + f".tmp{os.getpid()}"
+        cmd = [gxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-o", tmp, *srcs, "-L", LIBDIR,
+               "-lthc_gb300", "-Wl,-rpath,$ORIGIN", *zlib]
+        if verbose:
+            print(" ".join(cmd))
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host library build failed:\n{r.stderr}")
+        os.replace(tmp, HOST_LIB)
+    main = os.path.join(HOST, "main.cpp")
+    if force or _stale(DRIVER, [main, HOST_LIB] + hdrs):
+        tmp = DRIVER + f".tmp{os.getpid()}"
+        cmd = [gxx, "-O2", "-std=c++17", "-o", tmp, main, "-L", LIBDIR, "-lthcpp_host",
+               "-lthc_gb300", "-Wl,-rpath,$ORIGIN/../lib", *zlib]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stderr}")
+        os.replace(tmp, DRIVER)
+    return HOST_LIB
 
 
 if __name__ == "__main__":

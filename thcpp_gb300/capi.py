@@ -33,6 +33,7 @@ EXPORTS = [
     "thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
     "thc_ctx_last_error", "thc_status_string", "thc_ctx_kernel_launches",
     "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
+    "thc_kmeans_history",
 ]
 
 
@@ -90,6 +91,8 @@ def load(build_if_missing: bool = False):
     lib.thc_ctx_kernel_time.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(cd),
                                         ctypes.POINTER(cll)]
     lib.thc_ctx_kernel_time.restype = ci
+    lib.thc_kmeans_history.argtypes = [vp, vp, vp, ci]
+    lib.thc_kmeans_history.restype = ci
     lib.thc_kmeans_initial_indices.argtypes = [cll, ci, cu, vp]
     lib.thc_kmeans.argtypes = [vp, vp, vp, cll, ci, vp, ci, cd, vp, ctypes.POINTER(KMeansStats)]
     lib.thc_isdf.argtypes = [vp, vp, cll, ci, vp, ci, vp, vp, cd, vp, vp, vp,
@@ -185,6 +188,12 @@ class Context:
         if raise_on_error:
             self._check(st, "thc_kmeans")
         return out_idx, stats, st
+
+    def kmeans_history(self, n):
+        diff = np.zeros(n)
+        pct = np.zeros(n)
+        self._check(self.lib.thc_kmeans_history(self.h, _ptr(diff), _ptr(pct), n), "history")
+        return diff, pct
 
     def isdf(self, phi, idx, mesh, coulG, shift_rel=-1.0, out_orbitals=None, out_M=None,
              out_L=None, raise_on_error=True, want=("M", "L", "orbitals")):

@@ -275,6 +275,12 @@ int thc_kmeans(thc_ctx* h, const double* grid, const double* rho, long long ng, 
   return thc::kmeans_run(&h->c, grid, rho, ng, nmu, init_idx, max_it, threshold, out_idx, stats);
 }
 
+int thc_kmeans_history(thc_ctx* h, double* diff, double* pct_changed, int n)
+{
+  if (!h || (n > 0 && (!diff || !pct_changed))) return THC_ERR_ARG;
+  return thc::kmeans_history(&h->c, diff, pct_changed, n);
+}
+
 int thc_isdf(thc_ctx* h, const double* phi, long long ng, int norb, const int* idx, int nmu,
              const int* mesh, const double* coulG, double shift_rel, double* out_orbitals,
              double* out_M, double* out_L, thc_isdf_stats* stats)

@@ -71,6 +71,9 @@ struct Ctx {
   int slices_p = 6;
   int slices_z = 6;
   std::string last_error;
+  // History of the last k-means run (device buffer WS_KM_LOG: diff[max_it], pct[max_it]).
+  int km_last_iters = 0;
+  int km_last_max_it = 0;
   // Opt-in per-kernel event timing.
   bool profile = false;
   struct Rec { std::string name; cudaEvent_t a, b; };

@@ -19,4 +19,6 @@ int kmeans_run(Ctx* c, const double* grid, const double* rho, long long ng, int 
                const int* init, int max_it, double threshold, int* out_idx,
                thc_kmeans_stats* stats);
 
+int kmeans_history(Ctx* c, double* diff, double* pct, int n);
+
 }  // namespace thc

@@ -707,6 +707,8 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   if (didx != out_idx)
     THC_CUDA(c, cudaMemcpyAsync(out_idx, didx, sizeof(int) * nmu, cudaMemcpyDeviceToHost, s));
   THC_CUDA(c, cudaStreamSynchronize(s));
+  c->km_last_iters = hs.iter;
+  c->km_last_max_it = max_it;
   if (hs.bad_label) return set_error(c, THC_ERR_CUDA, "thc_kmeans: internal label out of range");
   if (hs.empty) {
     if (stats) stats->iterations = hs.iter;
@@ -730,6 +732,18 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     stats->rechecked = hs.rechecked_total;
     stats->device_ms = ms;
   }
+  return THC_OK;
+}
+
+int kmeans_history(Ctx* c, double* diff, double* pct, int n)
+{
+  if (n < 0 || n > c->km_last_iters || !c->ws[WS_KM_LOG]) return THC_ERR_ARG;
+  if (n == 0) return THC_OK;
+  const double* logb = (const double*)c->ws[WS_KM_LOG];
+  THC_CUDA(c, cudaMemcpyAsync(diff, logb, sizeof(double) * n, cudaMemcpyDefault, c->stream));
+  THC_CUDA(c, cudaMemcpyAsync(pct, logb + c->km_last_max_it, sizeof(double) * n, cudaMemcpyDefault,
+                              c->stream));
+  THC_CUDA(c, cudaStreamSynchronize(c->stream));
   return THC_OK;
 }
 

@@ -1,0 +1,51 @@
+// InterpolatingPoints::IPoints (reference: src/interpolating_points.cpp:11-63): solver
+// selection from the JSON and dispatch.  Only the k-means selector is built for the GPU.
+#include "interpolating_points.h"
+
+#include <cstdlib>
+#include <iostream>
+
+#include "kmeans.h"
+
+namespace InterpolatingPoints {
+
+IPoints::IPoints(nlohmann::json& input, ContextHandler::BlacsHandler& BH)
+{
+  (void)BH;
+  std::cout << "#################################################" << std::endl;
+  std::cout << "##   Setting up interpolating point solver.    ##" << std::endl;
+  std::cout << "#################################################" << std::endl;
+  std::cout << std::endl;
+  nlohmann::json base = input.at("interpolating_points");
+  try {
+    nlohmann::json kmeans_dict = base.at("kmeans");
+    solver = "kmeans";
+  } catch (nlohmann::json::out_of_range& error) {
+    try {
+      nlohmann::json qrcp = base.at("qrcp");
+      solver = "qrcp";
+    } catch (nlohmann::json::out_of_range& error) {
+      std::cout << "No solver specified." << std::endl;
+      solver = "kmeans";
+    }
+  }
+}
+
+std::vector<int> IPoints::kernel(nlohmann::json& input, ContextHandler::BlacsHandler& BH,
+                                 int thc_cfac, bool half_rotate)
+{
+  (void)half_rotate;
+  std::vector<int> interp_indxs;
+  if (solver == "qrcp") {
+    std::cerr << " * ERROR: the QRCP interpolating-point solver is not part of the GPU build;"
+                 " use \"kmeans\"." << std::endl;
+    exit(1);
+  }
+  std::cout << " * Using K-Means solver." << std::endl;
+  std::cout << std::endl;
+  KMeans::KMeansSolver KM(input, BH);
+  KM.kernel(BH, interp_indxs, thc_cfac);
+  return interp_indxs;
+}
+
+}  // namespace InterpolatingPoints

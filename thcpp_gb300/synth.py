@@ -265,3 +265,42 @@ def c4_system(s: int) -> System:
             break
     lat = edge * np.eye(3)
     return make_system(f"c4_{s}", lat, np.array(pos), (n, n, n), norb, cfac, 5000 + s, 17 + 4)
+
+
+def write_orbital_file(system: System, path: str, half_rotate: bool = False) -> None:
+    """Write ``system`` in the orbital-file layout of ``transform_basis.write_orbitals``.
+
+    Datasets (``tools/thcpy/thcpy/transform_basis.py:74-95``): real_space_grid, kmesh,
+    fft_grid (3, 1), hcore, constant_energy_factors (1, 1), num_electrons (1, 2),
+    fft_coulomb (N_g, 1), density and density_occ (N_g, 1), aoR (N_g, N_o) complex128,
+    aoR_half (N_g, nup) complex128.
+    """
+    from . import h5
+    nup = system.nocc
+    full = np.einsum("ij,ij->i", system.phi, system.phi)
+    with h5.Writer(path, truncate=True) as w:
+        w.write("real_space_grid", system.grid)
+        w.write("kmesh", np.ones(3, dtype=np.int32))
+        w.write("fft_grid", np.asarray(system.mesh, dtype=np.int32).reshape(3, 1))
+        w.write("hcore", np.zeros((system.norb, system.norb), dtype=np.complex128))
+        w.write("constant_energy_factors", np.zeros((1, 1)))
+        w.write("num_electrons", np.array([[nup, nup]], dtype=np.int32))
+        w.write("fft_coulomb", system.coulG.reshape(-1, 1))
+        w.write("density", full.reshape(-1, 1))
+        w.write("density_occ", system.density.reshape(-1, 1))
+        w.write("aoR", system.phi.astype(np.complex128))
+        if half_rotate:
+            w.write("aoR_half", system.phi[:, :nup].astype(np.complex128))
+
+
+def input_json(system: System, orbital_file: str, output_file: str, **gpu) -> dict:
+    """The thcpp input JSON for ``system`` (keys of src/utils.h:73-113, src/kmeans.cpp:16-44)."""
+    d = {"orbital_file": orbital_file, "output_file": output_file,
+         "thc_cfac": system.thc_cfac,
+         "interpolating_points": {"kmeans": {"max_it": system.max_it,
+                                             "threshold": system.threshold,
+                                             "rng_seed": system.rng_seed,
+                                             "density": system.density_label}}}
+    if gpu:
+        d["gpu"] = gpu
+    return d
