@@ -81,7 +81,9 @@ int thc_ctx_create(int device, int precision, thc_ctx** out_ctx);
 int thc_ctx_destroy(thc_ctx* ctx);
 /* Run on a caller stream (a cudaStream_t); NULL restores the context's own stream. */
 int thc_ctx_set_stream(thc_ctx* ctx, void* cuda_stream);
-/* Named numeric options: "slices_p", "slices_z" (sliced-GEMM depths, mixed path);
+/* Named numeric options: "slices_p", "slices_z", "slices_m" (sliced-GEMM depths of the
+ * P, zeta and Coulomb products, 2..6); "gemm_tc" (1 = tcgen05 tensor-core kernel, the
+ * default; 0 = warp-level mma.sync kernel);
  * "profile" (1 = record a CUDA event pair around every launch of the named kernels,
  * 0 = stop and clear). */
 int thc_ctx_set_option(thc_ctx* ctx, const char* key, double value);

@@ -20,7 +20,8 @@ BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libthc_gb300.so")
 
-CUDA_SOURCES = ["capi.cu", "kmeans.cu", "dense64.cu", "isdf.cu", "mixed.cu", "ozgemm.cu"]
+CUDA_SOURCES = ["capi.cu", "kmeans.cu", "dense64.cu", "isdf.cu", "mixed.cu", "ozgemm.cu",
+                "ozgemm_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST = os.path.join(PKG, "host")
 HOST_SOURCES = ["h5lite.cpp", "h5lite_capi.cpp", "gpu_context.cpp", "kmeans.cpp", "interpolating_points.cpp",

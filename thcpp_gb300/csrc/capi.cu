@@ -206,8 +206,17 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
 {
   if (!h || !key) return THC_ERR_ARG;
   if (!strcmp(key, "slices_p")) {
-    if (value < 2 || value > 8) return THC_ERR_ARG;
+    if (value < 2 || value > 6) return THC_ERR_ARG;
     h->c.slices_p = (int)value;
+    return THC_OK;
+  }
+  if (!strcmp(key, "slices_m")) {
+    if (value < 2 || value > 6) return THC_ERR_ARG;
+    h->c.slices_m = (int)value;
+    return THC_OK;
+  }
+  if (!strcmp(key, "gemm_tc")) {
+    h->c.gemm_tc = value != 0.0;
     return THC_OK;
   }
   if (!strcmp(key, "profile")) {
@@ -216,7 +225,7 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
     return THC_OK;
   }
   if (!strcmp(key, "slices_z")) {
-    if (value < 2 || value > 8) return THC_ERR_ARG;
+    if (value < 2 || value > 6) return THC_ERR_ARG;
     h->c.slices_z = (int)value;
     return THC_OK;
   }

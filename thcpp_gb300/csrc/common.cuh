@@ -54,6 +54,7 @@ enum Slot : int {
   WS_SLICE_B,
   WS_SLICE_E,
   WS_OUT,           // staging of caller outputs
+  WS_PART,          // split-K partial sums
   WS_NSLOTS
 };
 
@@ -70,6 +71,8 @@ struct Ctx {
   long long launches = 0;
   int slices_p = 6;
   int slices_z = 6;
+  int slices_m = 4;
+  int gemm_tc = 1;      // 1: tcgen05 sliced GEMM, 0: mma.sync sliced GEMM
   std::string last_error;
   // History of the last k-means run (device buffer WS_KM_LOG: diff[max_it], pct[max_it]).
   int km_last_iters = 0;

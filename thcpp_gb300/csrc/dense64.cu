@@ -33,7 +33,13 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
   __shared__ double Bs[BK][BN + 1];
   int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   double acc[4][4] = {};
-  for (int k0 = 0; k0 < g.K; k0 += BK) {
+  int kbeg = 0, kend = g.K;
+  if (g.ksplit > 1) {
+    int kc = ((g.K + g.ksplit - 1) / g.ksplit + BK - 1) / BK * BK;
+    kbeg = blockIdx.z * kc;
+    kend = min(g.K, kbeg + kc);
+  }
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
     // 1024 elements of each tile, 4 per thread.
 #pragma unroll
     for (int r = 0; r < 4; r++) {
@@ -43,7 +49,7 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
       long long m = m0 + mm;
       int k = k0 + kk;
       double av = 0.0;
-      if (m < g.M && k < g.K) {
+      if (m < g.M && k < kend) {
         av = g.A[m * g.sam + (long long)k * g.sak];
         if (g.dk) av *= g.dk[k >> g.dk_shift];
       }
@@ -52,7 +58,7 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
       if (BK_) { nn = e / BK; kb = e % BK; } else { kb = e / BN; nn = e % BN; }
       long long n = n0 + nn;
       int kq = k0 + kb;
-      Bs[kb][nn] = (n < g.N && kq < g.K) ? g.B[n * g.sbn + (long long)kq * g.sbk] : 0.0;
+      Bs[kb][nn] = (n < g.N && kq < kend) ? g.B[n * g.sbn + (long long)kq * g.sbk] : 0.0;
     }
     __syncthreads();
 #pragma unroll
@@ -79,6 +85,10 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
       if (n >= g.N) continue;
       if (g.lower_only && n > m) continue;
       double v = acc[i][j];
+      if (g.ksplit > 1) {
+        g.part[((long long)blockIdx.z * g.M + m) * g.N + n] = v;
+        continue;
+      }
       double* cp = g.C + m * g.ldc + n;
       if (g.mode == GEMM_SQUARE) v = v * v;
       else v = g.alpha * v;
@@ -86,6 +96,22 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
       *cp = v;
     }
   }
+}
+
+// Sum split-K partials in split order, then apply the epilogue.
+__global__ void dgemm_reduce(GemmArgs g)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= g.M * g.N) return;
+  long long m = e / g.N, n = e % g.N;
+  if (g.lower_only && n > m) return;
+  double v = 0.0;
+  for (int z = 0; z < g.ksplit; z++) v += g.part[((long long)z * g.M + m) * g.N + n];
+  double* cp = g.C + m * g.ldc + n;
+  if (g.mode == GEMM_SQUARE) v = v * v;
+  else v = g.alpha * v;
+  if (g.beta != 0.0) v += g.beta * *cp;
+  *cp = v;
 }
 
 // ---- Cholesky (lower, in place, row-major) --------------------------------------
@@ -304,7 +330,7 @@ __global__ void zpotrf_small_k(double* A, int n, const double* thr_p, CholStatus
 int dgemm(Ctx* c, const GemmArgs& g)
 {
   if (g.M <= 0 || g.N <= 0) return THC_OK;
-  dim3 grid((unsigned)cdiv(g.N, BN), (unsigned)cdiv(g.M, BM));
+  dim3 grid((unsigned)cdiv(g.N, BN), (unsigned)cdiv(g.M, BM), (unsigned)std::max(1, g.ksplit));
   bool ak = g.sak == 1, bk = g.sbk == 1;
   ProfScope prof(c, "dgemm");
   if (ak && bk) dgemm_kernel<true, true><<<grid, 256, 0, c->stream>>>(g);
@@ -312,6 +338,10 @@ int dgemm(Ctx* c, const GemmArgs& g)
   else if (!ak && bk) dgemm_kernel<false, true><<<grid, 256, 0, c->stream>>>(g);
   else dgemm_kernel<false, false><<<grid, 256, 0, c->stream>>>(g);
   THC_LAUNCHED(c, "dgemm");
+  if (g.ksplit > 1) {
+    dgemm_reduce<<<(unsigned)cdiv(g.M * g.N, 256), 256, 0, c->stream>>>(g);
+    THC_LAUNCHED(c, "dgemm_reduce");
+  }
   return THC_OK;
 }
 

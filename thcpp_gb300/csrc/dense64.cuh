@@ -25,6 +25,8 @@ struct GemmArgs {
   int mode = GEMM_STORE;
   int lower_only = 0;
   const int* skip_flag = nullptr;   // if non-null and set, the kernel does nothing
+  int ksplit = 1;                    // > 1: K is split over blockIdx.z into FP64 partials
+  double* part = nullptr;            // ksplit x M x N partial buffer (row-major, ld = N)
 };
 
 struct CholStatus {

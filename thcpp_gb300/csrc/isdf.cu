@@ -311,6 +311,13 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
     g.dk = dsym; g.dk_shift = 1;
     g.C = mre; g.ldc = nmu; g.lower_only = 1;
     if (2 * nc > 0x7fffffffLL) return set_error(c, THC_ERR_SHAPE, "thc_isdf: mesh too large");
+    // Long K, small output: split K over CTAs (deterministic reduction in split order).
+    long long tiles = cdiv(nmu, 64) * (cdiv(nmu, 64) + 1) / 2;
+    g.ksplit = (int)std::max<long long>(1, std::min<long long>(cdiv(2 * 152, tiles), cdiv(2 * nc, 4096)));
+    if (g.ksplit > 1) {
+      g.part = (double*)ws_get(c, WS_PART, sizeof(double) * g.ksplit * nn);
+      if (!g.part) return set_error(c, THC_ERR_NOMEM, "thc_isdf: split-K buffer");
+    }
     if ((st = dgemm(c, g))) return st;
   }
   THC_CUDA(c, cudaStreamSynchronize(s));

@@ -45,8 +45,9 @@ namespace {
 
 constexpr int kAssignThreads = 256;
 constexpr int kTile = 1024;       // centroids staged per shared-memory tile
-constexpr int kBP = 1024;         // points per histogram / scatter block
+constexpr int kBP = 512;          // points per histogram / scatter block
 constexpr int kMapChunk = 1024;   // grid points per map_to_grid block
+constexpr int kNormSmem = 6144;   // terms of the normed difference staged in shared memory
 
 struct KmState {
   int iter;
@@ -406,28 +407,50 @@ __global__ void km_scatter(KmBufs b)
   }
 }
 
-// One thread per cluster: sequential sums over members in ascending grid order.
-__global__ void km_sums(KmBufs b)
+// One warp per cluster.  Lanes load 32 members at a time and form the products rho_i * g_i
+// (each rounded on its own, as the reference's `rho[i] * grid[i*ndim]`); four lanes then
+// add them into w, x, y, z strictly in ascending member order from shared memory, so the
+// sums round exactly as the reference's sequential loop (src/kmeans.cpp:121-126).
+constexpr int kSumWarps = 4;
+__global__ void __launch_bounds__(32 * kSumWarps) km_sums(KmBufs b)
 {
   KmState* st = b.st;
   if (st->done) return;
+  __shared__ double sv[kSumWarps][4][33];
   int it = st->iter;
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int k = blockIdx.x * kSumWarps + w;
   if (k >= b.nmu) return;
   int s = b.start[k], n = b.total[k];
-  double w = 0.0, x = 0.0, y = 0.0, z = 0.0;
-  for (int m = s; m < s + n; m++) {
-    int i = b.member[m];
-    double r = b.rho[i];
-    w = __dadd_rn(w, r);
-    x = __dadd_rn(x, __dmul_rn(r, b.gx[i]));
-    y = __dadd_rn(y, __dmul_rn(r, b.gy[i]));
-    z = __dadd_rn(z, __dmul_rn(r, b.gz[i]));
+  double acc = 0.0;  // lane q < 4 owns quantity q: 0 = w, 1 = x, 2 = y, 3 = z
+  for (int base = 0; base < n; base += 32) {
+    int m = base + lane;
+    if (m < n) {
+      int i = b.member[s + m];
+      double r = b.rho[i];
+      sv[w][0][lane] = r;
+      sv[w][1][lane] = __dmul_rn(r, b.gx[i]);
+      sv[w][2][lane] = __dmul_rn(r, b.gy[i]);
+      sv[w][3][lane] = __dmul_rn(r, b.gz[i]);
+    }
+    __syncwarp();
+    if (lane < 4) {
+      int cnt = min(32, n - base);
+      const double* v = sv[w][lane];
+#pragma unroll 8
+      for (int j = 0; j < cnt; j++) acc = __dadd_rn(acc, v[j]);
+    }
+    __syncwarp();
   }
-  if (w < 1e-8) atomicExch(&st->empty, 1);
+  double wsum = __shfl_sync(0xffffffffu, acc, 0);
+  double x = __shfl_sync(0xffffffffu, acc, 1);
+  double y = __shfl_sync(0xffffffffu, acc, 2);
+  double z = __shfl_sync(0xffffffffu, acc, 3);
+  if (lane != 0) return;
+  if (wsum < 1e-8) atomicExch(&st->empty, 1);
   double* nc = b.cen + (size_t)((it + 1) & 1) * 3 * b.nmu;
   float* nc32 = b.cen32 + (size_t)((it + 1) & 1) * 3 * b.nmu;
-  double cx = __ddiv_rn(x, w), cy = __ddiv_rn(y, w), cz = __ddiv_rn(z, w);
+  double cx = __ddiv_rn(x, wsum), cy = __ddiv_rn(y, wsum), cz = __ddiv_rn(z, wsum);
   nc[k] = cx; nc[b.nmu + k] = cy; nc[2 * b.nmu + k] = cz;
   nc32[k] = (float)cx; nc32[b.nmu + k] = (float)cy; nc32[2 * b.nmu + k] = (float)cz;
 }
@@ -471,15 +494,26 @@ __global__ void km_normdiff(KmBufs b)
   ma = block_max(ma, red);
   mc = block_max(mc, red);
   double scale = __dadd_rn(ma, mc);
+  extern __shared__ double sterm[];
+  const bool in_smem = n3 <= kNormSmem;
+  double* terms = in_smem ? sterm : b.terms;
   for (int i = threadIdx.x; i < n3; i += blockDim.x) {
     int k = i / 3, d = i - 3 * k;
     double q = __ddiv_rn(__dsub_rn(a[d * b.nmu + k], c[d * b.nmu + k]), scale);
-    b.terms[i] = __dmul_rn(q, q);
+    terms[i] = __dmul_rn(q, q);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    // One thread, index order: the reference's `diff += ...` loop.
     double s = 0.0;
-    for (int i = 0; i < n3; i++) s = __dadd_rn(s, b.terms[i]);
+    int i = 0;
+    for (; i + 8 <= n3; i += 8) {
+      double t0 = terms[i], t1 = terms[i + 1], t2 = terms[i + 2], t3 = terms[i + 3];
+      double t4 = terms[i + 4], t5 = terms[i + 5], t6 = terms[i + 6], t7 = terms[i + 7];
+      s = __dadd_rn(s, t0); s = __dadd_rn(s, t1); s = __dadd_rn(s, t2); s = __dadd_rn(s, t3);
+      s = __dadd_rn(s, t4); s = __dadd_rn(s, t5); s = __dadd_rn(s, t6); s = __dadd_rn(s, t7);
+    }
+    for (; i < n3; i++) s = __dadd_rn(s, terms[i]);
     double diff = __dmul_rn(scale, __dsqrt_rn(s));
     st->diff = diff;
     st->pct = 100.0 * (double)st->changed / (double)b.ng;
@@ -650,6 +684,9 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     THC_CUDA(c, cudaFuncSetAttribute(km_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
     THC_CUDA(c, cudaFuncSetAttribute(km_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
   }
+  size_t norm_smem = 3 * (size_t)nmu <= kNormSmem ? sizeof(double) * 3 * nmu : 0;
+  if (norm_smem > 48 * 1024)
+    THC_CUDA(c, cudaFuncSetAttribute(km_normdiff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)norm_smem));
   int* hflag = (int*)c->pinned;
   const int kCheckEvery = 8;
   for (int it = 0; it < max_it; it++) {
@@ -673,9 +710,9 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     THC_LAUNCHED(c, "km_kscan");
     km_scatter<<<b.nb, 128, hist_smem, s>>>(b);
     THC_LAUNCHED(c, "km_scatter");
-    km_sums<<<(int)cdiv(nmu, 128), 128, 0, s>>>(b);
+    km_sums<<<(int)cdiv(nmu, kSumWarps), 32 * kSumWarps, 0, s>>>(b);
     THC_LAUNCHED(c, "km_sums");
-    km_normdiff<<<1, 1024, 0, s>>>(b);
+    km_normdiff<<<1, 1024, norm_smem, s>>>(b);
     THC_LAUNCHED(c, "km_normdiff");
     if ((it + 1) % kCheckEvery == 0 && it + 1 < max_it) {
       THC_CUDA(c, cudaMemcpyAsync(hflag, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -1,6 +1,6 @@
 // Mixed-precision ISDF: the same quantities as isdf.cu with the three large products on
 // the BF16 tensor cores through error-free slicing (ozgemm):
-//   Z^T    = (Phi_mu Phi^T)^2      sliced GEMM, FP64 result, squared in the epilogue
+//   Z      = (Phi Phi_mu^T)^2      sliced GEMM, FP64 result, squared in the epilogue
 //   zeta^T = C^{-1} Z^T            sliced GEMM, FP32 result (input of the FP32 FFT)
 //   Re M   = A A^T, A = zeta_hat * sqrt(w v_sym)  sliced GEMM over the half spectrum
 // C, its Cholesky factor and C^{-1} stay FP64 (C is ill-conditioned: cond ~1e6-1e9), and
@@ -148,7 +148,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   const int n0 = mesh[0], n1 = mesh[1], n2 = mesh[2];
   const long long nc = (long long)n0 * n1 * (n2 / 2 + 1);
   const long long nn = (long long)nmu * nmu;
-  const int sp = c->slices_p, sz = c->slices_z, sm = 4;
+  const int sp = c->slices_p, sz = c->slices_z, sm = c->slices_m;
   const long long mu_pad = oz_pad_mn(nmu), mu_kpad = oz_pad_k(nmu);
   const long long ng_pad = oz_pad_mn(ng), no_kpad = oz_pad_k(no);
   const long long k2_pad = oz_pad_k(2 * nc);
@@ -156,7 +156,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   double* phimu = (double*)ws_get(c, WS_PHIMU, sizeof(double) * nmu * no);
   double* C = (double*)ws_get(c, WS_C, sizeof(double) * 2 * nn);
   double* Cinv = (double*)ws_get(c, WS_CINV, sizeof(double) * nn);
-  double* zt = (double*)ws_get(c, WS_ZT, sizeof(double) * nmu * ng);
+  double* zg = (double*)ws_get(c, WS_ZT, sizeof(double) * nmu * ng);   // Z: N_g x N_mu
   float* zeta = (float*)ws_get(c, WS_ZETA, sizeof(float) * nmu * ng);
   float2* zhat = (float2*)ws_get(c, WS_ZHAT, sizeof(float2) * nmu * nc);
   double* dsym = (double*)ws_get(c, WS_DSYM, (sizeof(double) + sizeof(float)) * nc + 64);
@@ -164,13 +164,13 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   double* Mw = (double*)ws_get(c, WS_M, sizeof(double) * 4 * nn);
   double* Lw = (double*)ws_get(c, WS_L, sizeof(double) * 2 * nn);
   char* scr = (char*)ws_get(c, WS_SCRATCH, 4096);
-  size_t a_elems = std::max({(size_t)sp * mu_pad * no_kpad, (size_t)sz * mu_pad * mu_kpad,
+  size_t a_elems = std::max({(size_t)sp * ng_pad * no_kpad, (size_t)sz * mu_pad * mu_kpad,
                              (size_t)sm * mu_pad * k2_pad});
-  size_t b_elems = std::max((size_t)sp * ng_pad * no_kpad, (size_t)sz * mu_kpad * ng_pad);
+  size_t b_elems = std::max((size_t)sp * mu_pad * no_kpad, (size_t)sz * ng_pad * mu_kpad);
   __nv_bfloat16* sa = (__nv_bfloat16*)ws_get(c, WS_SLICE_A, sizeof(__nv_bfloat16) * a_elems);
   __nv_bfloat16* sb = (__nv_bfloat16*)ws_get(c, WS_SLICE_B, sizeof(__nv_bfloat16) * b_elems);
   int* ex = (int*)ws_get(c, WS_SLICE_E, sizeof(int) * (mu_pad + ng_pad + 64));
-  if (!phimu || !C || !Cinv || !zt || !zeta || !zhat || !dsym || !danti || !Mw || !Lw || !scr ||
+  if (!phimu || !C || !Cinv || !zg || !zeta || !zhat || !dsym || !danti || !Mw || !Lw || !scr ||
       !sa || !sb || !ex)
     return set_error(c, THC_ERR_NOMEM, "thc_isdf (mixed): workspace allocation failed");
   float* sq = (float*)(dsym + nc);
@@ -184,9 +184,11 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   double* zero = dmean + 3;
   int* bad = (int*)(scr + 512);
   int* n_anti = bad + 1;
+  int* gemm_err = bad + 2;
   double* orb_dev = nullptr;
   if (out_orb) orb_dev = is_device_ptr(out_orb) ? out_orb : Lw;
   THC_CUDA(c, cudaMemsetAsync(scr + 512, 0, 64, s));
+  auto gemm = [&](const OzArgs& g) { return c->gemm_tc ? ozgemm_tc(c, g, gemm_err) : ozgemm(c, g); };
   THC_CUDA(c, cudaEventRecord(c->ev0, s));
 
   gather_rows_m<<<(int)cdiv((long long)nmu * no, 256), 256, 0, s>>>(phi, ng, no, idx, nmu, phimu,
@@ -218,21 +220,22 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     THC_LAUNCHED(c, "init_cs");
     return potrf(c, Lc, nmu, nmu, thr, cs);
   };
-  // Z^T via the sliced GEMM, overlapping nothing yet: it does not depend on C.
-  if ((st = oz_slice_rows_f64(c, phimu, nmu, no, no, 1, nullptr, 0, sp, sa, no_kpad,
-                              mu_pad * no_kpad, ea, mu_pad)))
-    return st;
-  if ((st = oz_slice_rows_f64(c, phi, ng, no, no, 1, nullptr, 0, sp, sb, no_kpad,
+  // Z = (Phi Phi_mu^T)^2 (N_g x N_mu) via the sliced GEMM: A = Phi sliced by grid point,
+  // B = Phi_mu sliced by interpolating point; Z's rows are then K-contiguous for the solve.
+  if ((st = oz_slice_rows_f64(c, phi, ng, no, no, 1, nullptr, 0, sp, sa, no_kpad,
                               ng_pad * no_kpad, eb, ng_pad)))
+    return st;
+  if ((st = oz_slice_rows_f64(c, phimu, nmu, no, no, 1, nullptr, 0, sp, sb, no_kpad,
+                              mu_pad * no_kpad, ea, mu_pad)))
     return st;
   {
     OzArgs g;
-    g.M = nmu; g.N = ng; g.K = no;
-    g.a.s = sa; g.a.e = ea; g.a.ld = no_kpad; g.a.slice_stride = mu_pad * no_kpad;
-    g.b.s = sb; g.b.e = eb; g.b.ld = no_kpad; g.b.slice_stride = ng_pad * no_kpad;
+    g.M = ng; g.N = nmu; g.K = no;
+    g.a.s = sa; g.a.e = eb; g.a.ld = no_kpad; g.a.slice_stride = ng_pad * no_kpad;
+    g.b.s = sb; g.b.e = ea; g.b.ld = no_kpad; g.b.slice_stride = mu_pad * no_kpad;
     g.b.k_contig = true;
-    g.levels = sp; g.epilogue = OZ_SQUARE_F64; g.C = zt; g.ldc = ng;
-    if ((st = ozgemm(c, g))) return st;
+    g.levels = sp; g.epilogue = OZ_SQUARE_F64; g.C = zg; g.ldc = nmu;
+    if ((st = gemm(g))) return st;
   }
   CholStatus hcs{};
   int chol_c_info = 0;
@@ -253,21 +256,21 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   }
   if ((st = set_identity(c, Cinv, nmu, nmu))) return st;
   if ((st = potrs(c, Lc, nmu, nmu, Cinv, nmu, nmu, cs))) return st;
-  // zeta^T = C^{-1} Z^T: A = C^{-1} sliced by rows, B = Z^T sliced by columns (grid points).
+  // zeta^T = C^{-1} Z^T: A = C^{-1} sliced by rows, B = Z sliced by rows (grid points).
   if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, sz, sa, mu_kpad,
                               mu_pad * mu_kpad, ea, mu_pad)))
     return st;
-  if ((st = oz_slice_cols_f64(c, zt, nmu, ng, ng, sz, sb, ng_pad, mu_kpad * ng_pad, eb, mu_kpad,
-                              ng_pad)))
+  if ((st = oz_slice_rows_f64(c, zg, ng, nmu, nmu, 1, nullptr, 0, sz, sb, mu_kpad,
+                              ng_pad * mu_kpad, eb, ng_pad)))
     return st;
   {
     OzArgs g;
     g.M = nmu; g.N = ng; g.K = nmu;
     g.a.s = sa; g.a.e = ea; g.a.ld = mu_kpad; g.a.slice_stride = mu_pad * mu_kpad;
-    g.b.s = sb; g.b.e = eb; g.b.ld = ng_pad; g.b.slice_stride = mu_kpad * ng_pad;
-    g.b.k_contig = false;
+    g.b.s = sb; g.b.e = eb; g.b.ld = mu_kpad; g.b.slice_stride = ng_pad * mu_kpad;
+    g.b.k_contig = true;
     g.levels = sz; g.epilogue = OZ_STORE_F32; g.C = zeta; g.ldc = ng;
-    if ((st = ozgemm(c, g))) return st;
+    if ((st = gemm(g))) return st;
   }
   // FP32 R2C FFT of every interpolating vector.
   cufftHandle plan;
@@ -293,7 +296,13 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     g.b = g.a;
     g.b.k_contig = true;
     g.levels = sm; g.epilogue = OZ_STORE_F64; g.C = mre; g.ldc = nmu; g.lower_only = 1;
-    if ((st = ozgemm(c, g))) return st;
+    // Long K (2 N_c) and a small N_mu x N_mu output: split K over CTAs.
+    g.ksplit = oz_choose_split(nmu, nmu, 2 * nc, true);
+    if (g.ksplit > 1) {
+      g.part = (double*)ws_get(c, WS_PART, sizeof(double) * g.ksplit * nn);
+      if (!g.part) return set_error(c, THC_ERR_NOMEM, "thc_isdf: split-K buffer");
+    }
+    if ((st = gemm(g))) return st;
   }
   THC_CUDA(c, cudaStreamSynchronize(s));
   int nb2 = (int)cdiv(nn, 256);
@@ -322,13 +331,15 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   if (out_M) THC_CUDA(c, cudaMemcpyAsync(out_M, mcx, sizeof(double) * 2 * nn, cudaMemcpyDefault, s));
   if (out_L) THC_CUDA(c, cudaMemcpyAsync(out_L, Lout, sizeof(double) * 2 * nn, cudaMemcpyDefault, s));
   CholStatus hm{};
-  int hbad = 0;
+  int hbad = 0, herr = 0;
   double hshift = 0.0;
+  THC_CUDA(c, cudaMemcpyAsync(&herr, gemm_err, sizeof(int), cudaMemcpyDeviceToHost, s));
   THC_CUDA(c, cudaMemcpyAsync(&hm, csm, sizeof(CholStatus), cudaMemcpyDeviceToHost, s));
   THC_CUDA(c, cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
   THC_CUDA(c, cudaMemcpyAsync(&hshift, shift_dev, sizeof(double), cudaMemcpyDeviceToHost, s));
   THC_CUDA(c, cudaStreamSynchronize(s));
   if (hbad) return set_error(c, THC_ERR_ARG, "thc_isdf: interpolating index out of range");
+  if (herr) return set_error(c, THC_ERR_TIMEOUT, "thc_isdf: tensor-core GEMM wait timed out");
   if (stats) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);

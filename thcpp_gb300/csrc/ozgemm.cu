@@ -7,6 +7,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -108,9 +109,15 @@ __global__ void __launch_bounds__(128, 2) ozgemm_kernel(OzArgs g)
     for (int q = 0; q < 4; q++) acc64[t][q] = 0.0;
   float acc[LV][4][4];
 
-  const long long K = g.K;
-  long long nsteps = (K + OBK - 1) / OBK;
-  load_stage(0, 0);
+  long long kbeg = 0, kend = g.K;
+  if (g.ksplit > 1) {
+    long long kc = ((g.K + g.ksplit - 1) / g.ksplit + 511) / 512 * 512;
+    kbeg = blockIdx.z * kc;
+    kend = kbeg + kc < g.K ? kbeg + kc : g.K;
+  }
+  const long long K = kend - kbeg;
+  long long nsteps = K > 0 ? (K + OBK - 1) / OBK : 0;
+  if (nsteps > 0) load_stage(0, kbeg);
   int buf = 0;
   for (long long st = 0; st < nsteps; st++) {
     if ((st * OBK) % OCHUNK == 0) {
@@ -123,7 +130,7 @@ __global__ void __launch_bounds__(128, 2) ozgemm_kernel(OzArgs g)
     }
     cp_async_wait_all();
     __syncthreads();
-    if (st + 1 < nsteps) load_stage(buf ^ 1, (st + 1) * OBK);
+    if (st + 1 < nsteps) load_stage(buf ^ 1, kbeg + (st + 1) * OBK);
     const __nv_bfloat16* cA = sA + buf * a_stage;
     const __nv_bfloat16* cB = sB + buf * b_stage;
 #pragma unroll
@@ -181,6 +188,10 @@ __global__ void __launch_bounds__(128, 2) ozgemm_kernel(OzArgs g)
       if (m >= g.M || n >= g.N) continue;
       if (g.lower_only && n > m) continue;
       double v = acc64[t][q] * pow2(g.a.e[m] + g.b.e[n] - 14);
+      if (g.ksplit > 1) {
+        g.part[((long long)blockIdx.z * g.M + m) * g.N + n] = v;
+        continue;
+      }
       if (g.epilogue == OZ_SQUARE_F64) v = v * v;
       if (g.epilogue == OZ_STORE_F32)
         ((float*)g.C)[m * g.ldc + n] = (float)v;
@@ -196,7 +207,7 @@ int launch_lv(Ctx* c, const OzArgs& g)
   size_t a_stage = (size_t)LV * OBM * OLDA;
   size_t b_stage = g.b.k_contig ? (size_t)LV * OBN * OLDA : (size_t)LV * OBK * OLDBN;
   size_t smem = 2 * (a_stage + b_stage) * sizeof(__nv_bfloat16);
-  dim3 grid((unsigned)cdiv(g.M, OBM), (unsigned)cdiv(g.N, OBN));
+  dim3 grid((unsigned)cdiv(g.M, OBM), (unsigned)cdiv(g.N, OBN), (unsigned)std::max(1, g.ksplit));
   if (grid.y > 65535) return set_error(c, THC_ERR_SHAPE, "ozgemm: N too large");
   ProfScope prof(c, "ozgemm");
   if (g.b.k_contig) {
@@ -207,7 +218,23 @@ int launch_lv(Ctx* c, const OzArgs& g)
     ozgemm_kernel<LV, false><<<grid, 128, smem, c->stream>>>(g);
   }
   THC_LAUNCHED(c, "ozgemm");
+  if (g.ksplit > 1) return oz_split_reduce(c, g);
   return THC_OK;
+}
+
+__global__ void oz_reduce_kernel(OzArgs g)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= g.M * g.N) return;
+  long long m = e / g.N, n = e % g.N;
+  if (g.lower_only && n > m) return;
+  double v = 0.0;
+  for (int z = 0; z < g.ksplit; z++) v += g.part[((long long)z * g.M + m) * g.N + n];
+  if (g.epilogue == OZ_SQUARE_F64) v = v * v;
+  if (g.epilogue == OZ_STORE_F32)
+    ((float*)g.C)[m * g.ldc + n] = (float)v;
+  else
+    ((double*)g.C)[m * g.ldc + n] = v;
 }
 
 // One warp per row: exponent from the row maximum, then the slices (FP64 input; every
@@ -300,6 +327,22 @@ __global__ void slice_cols_kernel(const double* __restrict__ X, long long rows, 
 }
 
 }  // namespace
+
+int oz_choose_split(long long M, long long N, long long K, bool lower)
+{
+  long long tiles = cdiv(M, 128) * cdiv(N, 64);
+  if (lower) tiles = (tiles + cdiv(M, 128)) / 2;
+  long long chunks = cdiv(K, 512);
+  long long want = cdiv(2 * 152, std::max(1LL, tiles));
+  return (int)std::max(1LL, std::min(want, chunks));
+}
+
+int oz_split_reduce(Ctx* c, const OzArgs& g)
+{
+  oz_reduce_kernel<<<(unsigned)cdiv(g.M * g.N, 256), 256, 0, c->stream>>>(g);
+  THC_LAUNCHED(c, "oz_split_reduce");
+  return THC_OK;
+}
 
 int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
                       long long sc, const double* scale, int scale_shift, int nslices,

@@ -37,10 +37,17 @@ struct OzArgs {
   void* C = nullptr;
   long long ldc = 0;
   int lower_only = 0;
+  int ksplit = 1;                    // > 1: K split over blockIdx.z (multiples of 512)
+  double* part = nullptr;            // ksplit x M x N FP64 partials (scaled, pre-epilogue)
 };
 
-// Padded sizes expected by ozgemm for the slice buffers.
-inline long long oz_pad_mn(long long x) { return (x + 63) / 64 * 64; }
+// Number of k-splits that fills the GPU for an M x N output with long K (chunk = 512).
+int oz_choose_split(long long M, long long N, long long K, bool lower);
+// part[z] summed in split order, then the epilogue, into C.
+int oz_split_reduce(Ctx* c, const OzArgs& g);
+
+// Padded sizes expected by both sliced-GEMM kernels for the slice buffers.
+inline long long oz_pad_mn(long long x) { return (x + 127) / 128 * 128; }
 inline long long oz_pad_k(long long x) { return (x + 31) / 32 * 32; }
 
 // Slice rows of a matrix X (rows x cols, element (r, c) at X[r*ldx + c*sc]) into
@@ -59,6 +66,10 @@ int oz_slice_cols_f64(Ctx* c, const double* X, long long rows, long long cols, l
                       int nslices, __nv_bfloat16* out, long long ldo, long long slice_stride,
                       int* exps, long long rows_pad, long long cols_pad);
 
+// Warp-level mma.sync implementation (reference for the tensor-core kernel below).
 int ozgemm(Ctx* c, const OzArgs& g);
+// tcgen05 / TMEM / TMA implementation; both operands K-contiguous.  err_flag (device int)
+// is set when a bounded wait inside the kernel gave up.
+int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag);
 
 }  // namespace thc

@@ -1,0 +1,435 @@
+// Sliced-BF16 GEMM on the 5th-generation tensor cores (tcgen05 + TMEM + TMA).
+//
+// Same arithmetic as ozgemm.cu (see ozgemm.cuh): C = sum over slice pairs (i, j), i + j < LV,
+// of 2^{-7(i+j)} S_i T_j, with exact FP32 chunk sums folded into FP64.
+//
+// CTA tile 128 x 64, k-step 32 per pipeline stage, all LV slices of A and B per stage.
+// Warp roles (320 threads):
+//   warp 0      TMA producer: 2*LV tiled loads per stage (SWIZZLE_64B, K-major)
+//   warp 1      TMEM allocator + single-thread MMA issuer
+//   warps 2-9   epilogue: two warps per TMEM lane quadrant, 32 columns each
+// TMEM holds one 128 x 64 FP32 accumulator per level (LV x 64 columns).  Levels 0-2 carry
+// the bulk of the value and are drained every 512 k (16 stages) while each of their sums
+// is still an exact integer below 2^24; levels >= 3 weigh <= 2^-21 of the total and
+// accumulate in FP32 over the whole K (rounding <= 2^-45 of the total).  The drain copies
+// levels 0-2 to registers and releases TMEM at once, so the FP64 folding overlaps the next
+// chunk's MMAs; within a stage the MMA thread issues the level >= 3 pairs first, which
+// covers the drain.
+// Every mbarrier wait is bounded; on timeout the kernel records an error, stops issuing,
+// and every role falls through to the teardown, which frees TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+#include "ozgemm.cuh"
+
+namespace thc {
+
+namespace {
+
+constexpr int TBM = 128, TBN = 64, TBK = 32, TSTAGES = 3, TCHUNK = 16;  // 16 stages = 512 k
+constexpr int TEPI_WARPS = 8;
+constexpr int TTHREADS = 32 * (2 + TEPI_WARPS);
+constexpr long long kSpinLimit = 1LL << 24;
+
+__device__ __forceinline__ uint32_t su32(const void* p)
+{
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(su32(b)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(su32(b)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* b)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(su32(b)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false (and *abort set) when the barrier phase never completes.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort)
+{
+  for (long long i = 0; i < kSpinLimit; i++) {
+    if (mbar_try(b, parity)) return true;
+    if (*abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+          su32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(su32(bar))
+      : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major, SWIZZLE_64B, 8-row groups 512 B apart.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
+{
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;                // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;       // stride byte offset
+  d |= (uint64_t)1 << 46;                // descriptor version
+  d |= (uint64_t)4 << 61;                // layout: 64-byte swizzle
+  return d;
+}
+
+// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 64.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TBN >> 3) << 17) |
+                            ((uint32_t)(TBM >> 4) << 24);
+
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc)
+{
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                   su32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+{
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ double pow2d(int e)
+{
+  if (e > -1022 && e < 1023) return __longlong_as_double((long long)(e + 1023) << 52);
+  return ldexp(1.0, e);
+}
+
+struct TcArgs {
+  long long M, N, K;
+  long long a_rows_pad, b_rows_pad;   // rows of one slice in the 2-D tensor maps
+  const int* ea;
+  const int* eb;
+  void* C;
+  long long ldc;
+  int epilogue;
+  int lower_only;
+  int* error;                         // set to 1 when a bounded wait gave up
+  int ksplit;
+  double* part;
+};
+
+template <int LV>
+__global__ void __launch_bounds__(TTHREADS, 1)
+    ozgemm_tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+                     TcArgs g)
+{
+  const long long m0 = (long long)blockIdx.x * TBM;
+  const long long n0 = (long long)blockIdx.y * TBN;
+  if (g.lower_only && n0 > m0 + TBM - 1) return;
+
+  constexpr int A_BYTES = TBM * TBK * 2;          // 8 KB per slice tile
+  constexpr int B_BYTES = TBN * TBK * 2;          // 4 KB per slice tile
+  constexpr int STAGE_BYTES = LV * (A_BYTES + B_BYTES);
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + TSTAGES * STAGE_BYTES);
+  uint64_t* empty = full + TSTAGES;
+  uint64_t* acc_full = empty + TSTAGES;
+  uint64_t* acc_empty = acc_full + 1;
+  uint32_t* tmem_slot = (uint32_t*)(acc_empty + 1);
+  volatile int* abort = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  long long kbeg = 0, kend = g.K;
+  if (g.ksplit > 1) {
+    long long kc = ((g.K + g.ksplit - 1) / g.ksplit + 511) / 512 * 512;
+    kbeg = blockIdx.z * kc;
+    kend = kbeg + kc < g.K ? kbeg + kc : g.K;
+  }
+  const int nstages = kend > kbeg ? (int)((kend - kbeg + TBK - 1) / TBK) : 0;
+  const int nchunks = (nstages + TCHUNK - 1) / TCHUNK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TSTAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(acc_full, 1);
+    mbar_init(acc_empty, TEPI_WARPS);
+    *abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                     su32(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------------ TMA producer
+    if (lane == 0) {
+      for (int it = 0; it < nstages; it++) {
+        int s = it % TSTAGES;
+        uint32_t ph = (uint32_t)((it / TSTAGES) & 1);
+        if (!mbar_wait(&empty[s], ph ^ 1, abort)) break;
+        unsigned char* st = smem + s * STAGE_BYTES;
+        mbar_expect_tx(&full[s], STAGE_BYTES);
+        int kx = (int)(kbeg + (long long)it * TBK);
+#pragma unroll
+        for (int sl = 0; sl < LV; sl++) {
+          tma_load_2d(st + sl * A_BYTES, &ta, kx, (int)(sl * g.a_rows_pad + m0), &full[s]);
+          tma_load_2d(st + LV * A_BYTES + sl * B_BYTES, &tb, kx, (int)(sl * g.b_rows_pad + n0),
+                      &full[s]);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      bool started_hi = false;
+      for (int it = 0; it < nstages && !*abort; it++) {
+        int s = it % TSTAGES;
+        uint32_t ph = (uint32_t)((it / TSTAGES) & 1);
+        int chunk = it / TCHUNK;
+        bool chunk_first = (it % TCHUNK) == 0;
+        bool chunk_last = ((it + 1) % TCHUNK) == 0 || it + 1 == nstages;
+        if (!mbar_wait(&full[s], ph, abort)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        unsigned char* st = smem + s * STAGE_BYTES;
+        uint32_t a0 = su32(st), b0 = su32(st + LV * A_BYTES);
+        // Levels >= 3: accumulate over the whole K.
+#pragma unroll
+        for (int l = 3; l < LV; l++) {
+          bool first = !started_hi;
+#pragma unroll
+          for (int i = 0; i <= l; i++) {
+            int j = l - i;
+#pragma unroll
+            for (int kk = 0; kk < 2; kk++) {
+              uint64_t ad = sdesc(a0 + i * A_BYTES + kk * 32);
+              uint64_t bd = sdesc(b0 + j * B_BYTES + kk * 32);
+              umma(tmem + l * TBN, ad, bd, first ? 0u : 1u);
+              first = false;
+            }
+          }
+        }
+        if (LV > 3) started_hi = true;
+        // Levels 0-2: exact per chunk; wait until the previous chunk has been drained.
+        if (chunk_first && chunk > 0) {
+          if (!mbar_wait(acc_empty, (uint32_t)((chunk - 1) & 1), abort)) break;
+          asm volatile("tcgen05.fence::after_thread_sync;\n");
+        }
+#pragma unroll
+        for (int l = 0; l < (LV < 3 ? LV : 3); l++) {
+          bool first = chunk_first;
+#pragma unroll
+          for (int i = 0; i <= l; i++) {
+            int j = l - i;
+#pragma unroll
+            for (int kk = 0; kk < 2; kk++) {
+              uint64_t ad = sdesc(a0 + i * A_BYTES + kk * 32);
+              uint64_t bd = sdesc(b0 + j * B_BYTES + kk * 32);
+              umma(tmem + l * TBN, ad, bd, first ? 0u : 1u);
+              first = false;
+            }
+          }
+        }
+        umma_commit(&empty[s]);
+        if (chunk_last) umma_commit(acc_full);
+      }
+    }
+  } else {
+    // ------------------------------------------------------------------ epilogue
+    const int ew = warp - 2;                 // 0..7
+    const int quad = warp & 3;               // TMEM lane quadrant this warp may access
+    const int half = ew >> 2;                // which 32-column half of the 64-wide tile
+    const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
+    const int col0 = half * 32;
+    double acc[32];
+#pragma unroll
+    for (int q = 0; q < 32; q++) acc[q] = 0.0;
+    float v[32];
+    bool ok = true;
+    for (int ch = 0; ch < nchunks; ch++) {
+      if (!mbar_wait(acc_full, (uint32_t)(ch & 1), abort)) { ok = false; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;\n");
+      float l0[32], l1[32], l2[32];
+      tmem_ld32(tmem + lane_base + 0 * TBN + col0, l0);
+      if (LV > 1) tmem_ld32(tmem + lane_base + 1 * TBN + col0, l1);
+      if (LV > 2) tmem_ld32(tmem + lane_base + 2 * TBN + col0, l2);
+      asm volatile("tcgen05.fence::before_thread_sync;\n");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_empty);
+#pragma unroll
+      for (int q = 0; q < 32; q++) {
+        double t = (double)l0[q];
+        if (LV > 1) t = __fma_rn((double)l1[q], 0x1p-7, t);
+        if (LV > 2) t = __fma_rn((double)l2[q], 0x1p-14, t);
+        acc[q] += t;
+      }
+    }
+    if (ok && LV > 3 && nstages > 0) {
+      for (int l = 3; l < LV; l++) {
+        tmem_ld32(tmem + lane_base + l * TBN + col0, v);
+        double sc = pow2d(-7 * l);
+#pragma unroll
+        for (int q = 0; q < 32; q++) acc[q] = __fma_rn((double)v[q], sc, acc[q]);
+      }
+    }
+    if (ok && !*abort) {
+      long long m = m0 + quad * 32 + lane;
+      if (m < g.M) {
+        int ea = g.ea[m];
+#pragma unroll 4
+        for (int q = 0; q < 32; q++) {
+          long long n = n0 + col0 + q;
+          if (n >= g.N) break;
+          if (g.lower_only && n > m) break;
+          double val = acc[q] * pow2d(ea + g.eb[n] - 14);
+          if (g.ksplit > 1) {
+            g.part[((long long)blockIdx.z * g.M + m) * g.N + n] = val;
+            continue;
+          }
+          if (g.epilogue == OZ_SQUARE_F64) val = val * val;
+          if (g.epilogue == OZ_STORE_F32)
+            ((float*)g.C)[m * g.ldc + n] = (float)val;
+          else
+            ((double*)g.C)[m * g.ldc + n] = val;
+        }
+      }
+    }
+  }
+  // ---------------------------------------------------------------------- teardown
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  if (*abort && threadIdx.x == 0) atomicExch(g.error, 1);
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encoder()
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// 2-D bf16 tensor map over `rows` x `kpad` (row pitch kpad elements), box 32 x box_rows.
+int make_map(Ctx* c, CUtensorMap* map, const void* base, long long kpad, long long rows,
+             int box_rows)
+{
+  auto enc = get_encoder();
+  if (!enc) return set_error(c, THC_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kpad * 2};
+  cuuint32_t box[2] = {(cuuint32_t)TBK, (cuuint32_t)box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+                   box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(c, THC_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return THC_OK;
+}
+
+template <int LV>
+int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
+{
+  CUtensorMap ta, tb;
+  long long a_rows = g.a.slice_stride / g.a.ld, b_rows = g.b.slice_stride / g.b.ld;
+  int st = make_map(c, &ta, g.a.s, g.a.ld, a_rows * LV, TBM);
+  if (st) return st;
+  st = make_map(c, &tb, g.b.s, g.b.ld, b_rows * LV, TBN);
+  if (st) return st;
+  TcArgs t;
+  t.M = g.M; t.N = g.N; t.K = g.K;
+  t.a_rows_pad = a_rows; t.b_rows_pad = b_rows;
+  t.ea = g.a.e; t.eb = g.b.e; t.C = g.C; t.ldc = g.ldc;
+  t.epilogue = g.epilogue; t.lower_only = g.lower_only; t.error = err_flag;
+  t.ksplit = std::max(1, g.ksplit); t.part = g.part;
+  size_t smem = (size_t)TSTAGES * LV * (TBM + TBN) * TBK * 2 + 1024 + 256;
+  THC_CUDA(c, cudaFuncSetAttribute(ozgemm_tc_kernel<LV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  dim3 grid((unsigned)cdiv(g.M, TBM), (unsigned)cdiv(g.N, TBN), (unsigned)t.ksplit);
+  if (grid.y > 65535) return set_error(c, THC_ERR_SHAPE, "ozgemm_tc: N too large");
+  {
+    ProfScope prof(c, "ozgemm");
+    ozgemm_tc_kernel<LV><<<grid, TTHREADS, smem, c->stream>>>(ta, tb, t);
+    THC_LAUNCHED(c, "ozgemm_tc");
+  }
+  if (t.ksplit > 1) return oz_split_reduce(c, g);
+  return THC_OK;
+}
+
+}  // namespace
+
+int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
+{
+  if (g.M <= 0 || g.N <= 0) return THC_OK;
+  if (!g.b.k_contig) return set_error(c, THC_ERR_ARG, "ozgemm_tc: B must be K-contiguous");
+  if (g.a.ld % 32 || g.b.ld % 32 || (g.a.slice_stride / g.a.ld) % TBM ||
+      (g.b.slice_stride / g.b.ld) % TBN)
+    return set_error(c, THC_ERR_ARG, "ozgemm_tc: operand padding");
+  switch (g.levels) {
+    case 2: return launch_tc<2>(c, g, err_flag);
+    case 3: return launch_tc<3>(c, g, err_flag);
+    case 4: return launch_tc<4>(c, g, err_flag);
+    case 5: return launch_tc<5>(c, g, err_flag);
+    case 6: return launch_tc<6>(c, g, err_flag);
+    default: return set_error(c, THC_ERR_ARG, "ozgemm_tc: levels must be 2..6");
+  }
+}
+
+}  // namespace thc
