@@ -31,10 +31,15 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+WORKLOADS = {
+    "c2": {"workload": "diamond-8atom-48^3-no32-nmu256", "n_g": 110592, "n_orb": 32,
+           "n_mu": 256, "mesh": [48, 48, 48]},
+    "c3": {"workload": "diamond-64atom-72^3-no256-nmu2048", "n_g": 373248, "n_orb": 256,
+           "n_mu": 2048, "mesh": [72, 72, 72]},
+}
 WORKLOAD = "c2"
-CONFIG = {"workload": "diamond-8atom-48^3-no32-nmu256", "n_g": 110592, "n_orb": 32,
-          "n_mu": 256, "mesh": [48, 48, 48], "kmeans_max_it": 100, "kmeans_threshold": 1e-6,
-          "l2": "flushed (256 MB write) before every timed step", "parallelism": "replicas"}
+CONFIG = dict(WORKLOADS[WORKLOAD], kmeans_max_it=100, kmeans_threshold=1e-6,
+              l2="flushed (256 MB write) before every timed step", parallelism="replicas")
 METRIC = "ISDF s/system on 1 GB300 (mixed precision; FP64 path reported beside)"
 
 
@@ -143,7 +148,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--paths", default="mixed,fp64,e2e",
+                    help="comma list of measured paths (a profiling run may keep only 'mixed')")
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS),
+                    help="c2 is the benchmark workload; c3 is reported separately")
     args = ap.parse_args()
+    global WORKLOAD, CONFIG
+    WORKLOAD = args.workload
+    CONFIG = dict(WORKLOADS[WORKLOAD], kmeans_max_it=100, kmeans_threshold=1e-6,
+                  l2="flushed (256 MB write) before every timed step", parallelism="replicas")
     if args.impl == "reference":
         return run_reference(args)
 
@@ -172,7 +185,8 @@ def main():
     d_L = torch.zeros((nmu, nmu, 2), dtype=torch.float64, device=dev)
     d_orb = torch.zeros((no, nmu, 2), dtype=torch.float64, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    # A dedicated stream: the library launches on it and the CUDA events are recorded on it.
+    stream = torch.cuda.Stream(dev)
 
     def device_step(ctx):
         _, kst, st = ctx.kmeans(d_grid, d_rho, nmu, d_init, s.max_it, s.threshold, out_idx=d_idx)
@@ -194,7 +208,8 @@ def main():
         ctx.set_option("profile", 1)
         tot = 0.0
         for _ in range(steps):
-            flush.fill_(1)
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -221,20 +236,27 @@ def main():
     km_ms, km_n = ctx.kernel_time("km_assign")
     ctx.set_option("profile", 0)
 
+    paths = set(args.paths.split(","))
     # All-FP64 path on the same inputs.
-    ctx64 = capi.Context(local, capi.THC_PREC_FP64)
-    torch.cuda.nvtx.range_push("fp64")
-    ms_fp64, launches64, kst64, r64 = timed(ctx64, args.fp64_steps, 1)
-    torch.cuda.nvtx.range_pop()
-    dg_ms, dg_n = ctx64.kernel_time("dgemm")
-    ctx64.set_option("profile", 0)
-    idx64 = d_idx.cpu().numpy().copy()
-    M_fp64 = d_M.cpu().numpy().copy()
-    device_step(ctx)  # idx from the mixed path for the comparison below
-    idx_mx = d_idx.cpu().numpy().copy()
-    Mc = M_mixed[..., 0] + 1j * M_mixed[..., 1]
-    M6 = M_fp64[..., 0] + 1j * M_fp64[..., 1]
-    rel_err = float(np.linalg.norm(Mc - M6) / np.linalg.norm(M6))
+    ms_fp64 = float("nan")
+    rel_err = None
+    dg_ms = 0.0
+    idx_same = None
+    if "fp64" in paths:
+        ctx64 = capi.Context(local, capi.THC_PREC_FP64)
+        torch.cuda.nvtx.range_push("fp64")
+        ms_fp64, launches64, kst64, r64 = timed(ctx64, args.fp64_steps, 1)
+        torch.cuda.nvtx.range_pop()
+        dg_ms, dg_n = ctx64.kernel_time("dgemm")
+        ctx64.set_option("profile", 0)
+        idx64 = d_idx.cpu().numpy().copy()
+        M_fp64 = d_M.cpu().numpy().copy()
+        device_step(ctx)  # idx from the mixed path for the comparison below
+        idx_mx = d_idx.cpu().numpy().copy()
+        Mc = M_mixed[..., 0] + 1j * M_mixed[..., 1]
+        M6 = M_fp64[..., 0] + 1j * M_fp64[..., 1]
+        rel_err = float(np.linalg.norm(Mc - M6) / np.linalg.norm(M6))
+        idx_same = bool(np.array_equal(idx64, idx_mx))
 
     # End to end through the C ABI with pinned host buffers.
     def pinned(a):
@@ -253,18 +275,20 @@ def main():
         ctx.kmeans(h_grid, h_rho, nmu, h_init, s.max_it, s.threshold, out_idx=h_idx)
         ctx.isdf(h_phi, h_idx, s.mesh, h_coul, -1.0, out_orbitals=h_orb, out_M=h_M, out_L=h_L)
 
-    torch.cuda.nvtx.range_push("e2e")
-    for _ in range(args.warmup):
-        host_step()
-    e2e = 0.0
-    for _ in range(args.steps):
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        host_step()
-        e2e += time.perf_counter() - t0
-    e2e /= args.steps
-    torch.cuda.nvtx.range_pop()
+    e2e = float("nan")
+    if "e2e" in paths:
+        torch.cuda.nvtx.range_push("e2e")
+        for _ in range(args.warmup):
+            host_step()
+        e2e = 0.0
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            host_step()
+            e2e += time.perf_counter() - t0
+        e2e /= args.steps
+        torch.cuda.nvtx.range_pop()
     h2d = (h_grid.nbytes + h_rho.nbytes + h_init.nbytes + h_phi.nbytes + h_coul.nbytes
            + h_idx.nbytes)
     d2h = h_idx.nbytes + h_orb.nbytes + h_M.nbytes + h_L.nbytes
@@ -288,7 +312,8 @@ def main():
         # factorisation = sum over the three GEMMs of (slice pairs) x 2 M N K.
         sp, sz, sm = 6, 6, 4
         pairs = lambda L: L * (L + 1) // 2
-        nc2 = 2 * 48 * 48 * 25
+        n0, n1, n2 = s.mesh
+        nc2 = 2 * n0 * n1 * (n2 // 2 + 1)
         flops = (pairs(sp) * 2 * nmu * ng * no + pairs(sz) * 2 * nmu * ng * nmu
                  + pairs(sm) * 2 * nmu * nmu * nc2 / 2)
         per_launch = flops / 3.0
@@ -315,9 +340,8 @@ def main():
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
             "fp64": {"s_per_system": ms_fp64 * 1e-3, "speedup_mixed_vs_fp64": ms_fp64 / t_step,
-                     "rel_err_M_mixed_vs_fp64": rel_err, "idx_identical": bool(
-                         np.array_equal(idx64, idx_mx)),
-                     "dgemm_ms_per_system": dg_ms / args.fp64_steps},
+                     "rel_err_M_mixed_vs_fp64": rel_err, "idx_identical": idx_same,
+                     "dgemm_ms_per_system": dg_ms / max(args.fp64_steps, 1)},
             "kmeans": {"iterations": kst.iterations, "rechecked_points": int(kst.rechecked),
                        "assign_ms_per_system": km_ms / args.steps},
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk,

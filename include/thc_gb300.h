@@ -83,7 +83,9 @@ int thc_ctx_destroy(thc_ctx* ctx);
 int thc_ctx_set_stream(thc_ctx* ctx, void* cuda_stream);
 /* Named numeric options: "slices_p", "slices_z", "slices_m" (sliced-GEMM depths of the
  * P, zeta and Coulomb products, 2..6); "gemm_tc" (1 = tcgen05 tensor-core kernel, the
- * default; 0 = warp-level mma.sync kernel);
+ * default; 0 = warp-level mma.sync kernel); "km_prune" (1 = spatially pruned k-means
+ * assignment, the default; 0 = exhaustive scan -- both exact); "graphs" (1 = replay the
+ * k-means iteration block as a CUDA graph, the default);
  * "profile" (1 = record a CUDA event pair around every launch of the named kernels,
  * 0 = stop and clear). */
 int thc_ctx_set_option(thc_ctx* ctx, const char* key, double value);

@@ -88,3 +88,27 @@ def test_kmeans_argument_errors(gpu_ctx_fp64):
     init = capi.initial_indices(s.ng, s.nmu, s.rng_seed)
     _, _, st = gpu_ctx_fp64.kmeans(s.grid, s.density, s.nmu, init, 0, 1e-6, raise_on_error=False)
     assert st == capi.THC_ERR_ARG
+
+
+@pytest.mark.parametrize("prec", [capi.THC_PREC_FP64, capi.THC_PREC_MIXED])
+@pytest.mark.parametrize("opts", [{"km_prune": 0}, {"graphs": 0}, {"km_prune": 0, "graphs": 0}])
+def test_kmeans_options_identical(lib, prec, opts):
+    """Pruned / exhaustive assignment and graph / eager launches give identical results."""
+    s = system("c2")
+    ref = oracle.kmeans_system(s)
+    init = capi.initial_indices(s.ng, s.nmu, s.rng_seed)
+    with capi.Context(0, prec) as ctx:
+        for k, v in opts.items():
+            ctx.set_option(k, v)
+        idx, st, status = ctx.kmeans(s.grid, s.density, s.nmu, init, s.max_it, s.threshold)
+    assert status == 0 and np.array_equal(idx, ref.idx) and st.final_diff == ref.diff
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_kmeans_exact_ties_pruned(request, prec):
+    """Integer lattice with 64 centroids (pruned path) and many exact ties."""
+    g, rho = kmeans_cases.exact_tie_grid(12)
+    init = oracle.initial_indices(g.shape[0], 64, 7)
+    ref = oracle.kmeans(g, rho, 64, init, 40, 1e-12)
+    idx, st, status = _ctx(request, prec).kmeans(g, rho, 64, init, 40, 1e-12)
+    assert status == 0 and np.array_equal(idx, ref.idx) and st.iterations == ref.iters

@@ -105,7 +105,7 @@ static cudaEvent_t take_event(Ctx* c)
 
 ProfScope::ProfScope(Ctx* ctx, const char* name) : c(ctx)
 {
-  if (!c->profile) return;
+  if (!c || !c->profile) return;
   Ctx::Rec r{name, take_event(c), take_event(c)};
   cudaEventRecord(r.a, c->stream);
   c->recs.push_back(r);
@@ -186,6 +186,7 @@ int thc_ctx_destroy(thc_ctx* h)
     if (c->ws[s]) cudaFree(c->ws[s]);
   thc::clear_profile(c);
   for (auto e : c->event_pool) cudaEventDestroy(e);
+  if (c->km_graph) cudaGraphExecDestroy(c->km_graph);
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -213,6 +214,14 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
   if (!strcmp(key, "slices_m")) {
     if (value < 2 || value > 6) return THC_ERR_ARG;
     h->c.slices_m = (int)value;
+    return THC_OK;
+  }
+  if (!strcmp(key, "graphs")) {
+    h->c.use_graphs = value != 0.0;
+    return THC_OK;
+  }
+  if (!strcmp(key, "km_prune")) {
+    h->c.km_prune = value != 0.0;
     return THC_OK;
   }
   if (!strcmp(key, "gemm_tc")) {

@@ -35,6 +35,7 @@ enum Slot : int {
   WS_KM_LOG,        // per-iteration diff / pct
   WS_KM_IO,         // staging of caller arrays
   WS_KM_IDX,
+  WS_KM_PERM,       // spatial binning: perm[ng], bin of each point, bin counts / offsets
   // ISDF
   WS_PHI,           // ng x norb doubles
   WS_PHIMU,         // nmu x norb doubles
@@ -55,6 +56,9 @@ enum Slot : int {
   WS_SLICE_E,
   WS_OUT,           // staging of caller outputs
   WS_PART,          // split-K partial sums
+  WS_DINV,          // inverted diagonal blocks + L^{-1} + scratch of the inverse
+  WS_ROWMAX,        // per-row maxima for slicing
+  WS_ZTMP,          // FP64 zeta of the rank-deficient fallback
   WS_NSLOTS
 };
 
@@ -73,6 +77,10 @@ struct Ctx {
   int slices_z = 6;
   int slices_m = 4;
   int gemm_tc = 1;      // 1: tcgen05 sliced GEMM, 0: mma.sync sliced GEMM
+  int km_prune = 1;     // 1: spatially pruned k-means assign, 0: exhaustive
+  int use_graphs = 1;   // capture the k-means iteration block in a CUDA graph
+  cudaGraphExec_t km_graph = nullptr;
+  std::vector<long long> km_graph_key;
   std::string last_error;
   // History of the last k-means run (device buffer WS_KM_LOG: diff[max_it], pct[max_it]).
   int km_last_iters = 0;

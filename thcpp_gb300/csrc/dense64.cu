@@ -167,6 +167,72 @@ __global__ void potrf_diag(double* A, long long ld, int n, int k0, const double*
   }
 }
 
+// Factor the diagonal block at (k0, k0) and invert its triangle: writes L_kk into A
+// (upper part zeroed) and L_kk^{-1} into dinv (nb x nb, row-major, zero above the diagonal).
+// Pivots at or below thr stop the factorisation (info = global 1-based index).
+__global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, int n, int k0,
+                                                      const double* thr_p, CholStatus* cs,
+                                                      double* dinv)
+{
+  if (cs->flag) return;
+  double thr = thr_p ? *thr_p : 0.0;
+  extern __shared__ double dsm[];                       // 2 x NB x (NB + 1) doubles
+  double (*a)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm);
+  double (*v)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm + NB * (NB + 1));
+  __shared__ double rinv;
+  __shared__ int bad;
+  const int nb = min(NB, n - k0);
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads
+  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
+    int r = e / NB, c = e % NB;
+    a[r][c] = (r < nb && c < nb) ? A[(long long)(k0 + r) * ld + k0 + c] : (r == c ? 1.0 : 0.0);
+    v[r][c] = 0.0;
+  }
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int j = 0; j < nb; j++) {
+    if (threadIdx.x == 0) {
+      double d = a[j][j];
+      if (!(d > thr)) {
+        bad = 1;
+        cs->flag = 1;
+        cs->info = k0 + j + 1;
+      } else {
+        double r = sqrt(d);
+        a[j][j] = r;
+        rinv = 1.0 / r;
+        if (d < cs->min_piv) cs->min_piv = d;
+        if (d > cs->max_piv) cs->max_piv = d;
+      }
+    }
+    __syncthreads();
+    if (bad) return;
+    double ri = rinv;
+    for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) a[i][j] *= ri;
+    __syncthreads();
+    // trailing lower update a[i][c] -= a[i][j] a[c][j], j < c <= i
+    for (int i = j + 1 + ty; i < nb; i += 16)
+      for (int c = j + 1 + tx; c <= i; c += 16) a[i][c] = __fma_rn(-a[i][j], a[c][j], a[i][c]);
+    __syncthreads();
+  }
+  // Triangular inverse by columns: for column c, v[c][c] = 1/a[c][c] and
+  // v[i][c] = -(sum_{k=c}^{i-1} a[i][k] v[k][c]) / a[i][i], i > c (one thread per column).
+  for (int c = threadIdx.x; c < nb; c += blockDim.x) {
+    v[c][c] = 1.0 / a[c][c];
+    for (int i = c + 1; i < nb; i++) {
+      double sacc = 0.0;
+      for (int k = c; k < i; k++) sacc = __fma_rn(a[i][k], v[k][c], sacc);
+      v[i][c] = -sacc / a[i][i];
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    int r = e / nb, c = e % nb;
+    A[(long long)(k0 + r) * ld + k0 + c] = c <= r ? a[r][c] : 0.0;
+    dinv[(long long)r * nb + c] = c <= r ? v[r][c] : 0.0;
+  }
+}
+
 // Rows below the diagonal block: x L_kk^T = a, one thread per row.
 __global__ void potrf_panel(double* A, long long ld, int n, int k0, CholStatus* cs)
 {
@@ -343,6 +409,88 @@ int dgemm(Ctx* c, const GemmArgs& g)
     THC_LAUNCHED(c, "dgemm_reduce");
   }
   return THC_OK;
+}
+
+// Blocked Cholesky whose panel solve is a GEMM with the inverted diagonal block; the
+// inverted diagonal blocks are kept in dinv (nblk x 64 x 64) for the triangular inverse.
+int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs,
+              double* dinv)
+{
+  cudaStream_t s = c->stream;
+  for (int k0 = 0; k0 < n; k0 += NB) {
+    int nb = std::min(NB, n - k0);
+    double* di = dinv + (long long)(k0 / NB) * NB * NB;
+    const int smem = 2 * NB * (NB + 1) * (int)sizeof(double);
+    THC_CUDA(c, cudaFuncSetAttribute(potrf_diag_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    potrf_diag_inv<<<1, 256, smem, s>>>(A, ld, n, k0, thr, cs, di);
+    THC_LAUNCHED(c, "potrf_diag_inv");
+    int rest = n - k0 - nb;
+    if (rest <= 0) break;
+    {
+      // L_panel = A_panel L_kk^{-T}, in place (each CTA owns its rows; N = nb <= 64).
+      GemmArgs g{};
+      g.M = rest; g.N = nb; g.K = nb;
+      g.A = A + (long long)(k0 + nb) * ld + k0; g.sam = ld; g.sak = 1;
+      g.B = di; g.sbn = nb; g.sbk = 1;
+      g.C = A + (long long)(k0 + nb) * ld + k0; g.ldc = ld;
+      g.skip_flag = &cs->flag;
+      int st = dgemm(c, g);
+      if (st) return st;
+    }
+    GemmArgs g{};
+    g.M = rest; g.N = rest; g.K = nb;
+    g.A = A + (long long)(k0 + nb) * ld + k0; g.sam = ld; g.sak = 1;
+    g.B = A + (long long)(k0 + nb) * ld + k0; g.sbn = ld; g.sbk = 1;
+    g.C = A + (long long)(k0 + nb) * ld + k0 + nb; g.ldc = ld;
+    g.alpha = -1.0; g.beta = 1.0; g.lower_only = 1; g.mode = GEMM_STORE;
+    g.skip_flag = &cs->flag;
+    int st = dgemm(c, g);
+    if (st) return st;
+  }
+  return THC_OK;
+}
+
+// X = L^{-1} (lower, n x n, ld) from the factor L and its inverted diagonal blocks, block row
+// by block row: X_ii = dinv_i, X[i, 0:i] = -dinv_i (L[i, 0:i] X[0:i, 0:i]).  T is an
+// NB x n scratch.  Then Cinv = X^T X.
+int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* dinv, double* X,
+                 double* T, double* Cinv, const CholStatus* cs)
+{
+  cudaStream_t s = c->stream;
+  THC_CUDA(c, cudaMemsetAsync(X, 0, sizeof(double) * (size_t)n * ld, s));
+  int nblk = (n + NB - 1) / NB;
+  for (int bi = 0; bi < nblk; bi++) {
+    int i0 = bi * NB, nb = std::min(NB, n - i0);
+    const double* di = dinv + (long long)bi * NB * NB;
+    THC_CUDA(c, cudaMemcpy2DAsync(X + (long long)i0 * ld + i0, sizeof(double) * ld, di,
+                                  sizeof(double) * nb, sizeof(double) * nb, nb,
+                                  cudaMemcpyDeviceToDevice, s));
+    if (bi == 0) continue;
+    GemmArgs g{};
+    g.M = nb; g.N = i0; g.K = i0;                       // T = L[i, 0:i] X[0:i, 0:i]
+    g.A = L + (long long)i0 * ld; g.sam = ld; g.sak = 1;
+    g.B = X; g.sbn = 1; g.sbk = ld;
+    g.C = T; g.ldc = n;
+    g.skip_flag = cs ? &cs->flag : nullptr;
+    int st = dgemm(c, g);
+    if (st) return st;
+    GemmArgs h{};
+    h.M = nb; h.N = i0; h.K = nb;                       // X[i, 0:i] = -dinv_i T
+    h.A = di; h.sam = nb; h.sak = 1;
+    h.B = T; h.sbn = 1; h.sbk = n;
+    h.C = X + (long long)i0 * ld; h.ldc = ld;
+    h.alpha = -1.0;
+    h.skip_flag = cs ? &cs->flag : nullptr;
+    st = dgemm(c, h);
+    if (st) return st;
+  }
+  GemmArgs g{};
+  g.M = n; g.N = n; g.K = n;                            // Cinv = X^T X
+  g.A = X; g.sam = 1; g.sak = ld;
+  g.B = X; g.sbn = 1; g.sbk = ld;
+  g.C = Cinv; g.ldc = n;
+  g.skip_flag = cs ? &cs->flag : nullptr;
+  return dgemm(c, g);
 }
 
 int potrf(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs)

@@ -38,6 +38,13 @@ struct CholStatus {
 
 int dgemm(Ctx* c, const GemmArgs& g);
 int potrf(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs);
+// Cholesky with GEMM panels; dinv receives the inverted 64 x 64 diagonal blocks
+// (ceil(n/64) x 64 x 64 doubles).
+int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs,
+              double* dinv);
+// Cinv = (L L^T)^{-1} via X = L^{-1}; X (n x ld) and T (64 x n) are scratch.
+int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* dinv, double* X,
+                 double* T, double* Cinv, const CholStatus* cs);
 int potrs(Ctx* c, const double* L, long long ld, int n, double* B, long long ldb,
           long long nrhs, const CholStatus* cs);
 int set_identity(Ctx* c, double* A, long long ld, int n);

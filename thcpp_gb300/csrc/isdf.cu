@@ -204,7 +204,11 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
   double* Mw = (double*)ws_get(c, WS_M, sizeof(double) * 4 * nn);  // Re M lower, X, complex M
   double* Lw = (double*)ws_get(c, WS_L, sizeof(double) * 2 * nn);
   char* scr = (char*)ws_get(c, WS_SCRATCH, 4096);
-  if (!phimu || !C || !Cinv || !zt || !zeta || !zhat || !dsym || !danti || !Mw || !Lw || !scr)
+  const long long nblk64 = (nmu + 63) / 64;
+  double* dinv = (double*)ws_get(c, WS_DINV, sizeof(double) * (nblk64 * 64 * 64 + nn + 64 * (long long)nmu));
+  double* Xinv = dinv + nblk64 * 64 * 64;
+  double* Tinv = Xinv + nn;
+  if (!phimu || !C || !Cinv || !zt || !zeta || !zhat || !dsym || !danti || !Mw || !Lw || !scr || !dinv)
     return set_error(c, THC_ERR_NOMEM, "thc_isdf: workspace allocation failed");
   CholStatus* cs = (CholStatus*)scr;
   CholStatus* csm = cs + 1;
@@ -260,7 +264,7 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
     }
     init_chol_status<<<1, 1, 0, s>>>(cs);
     THC_LAUNCHED(c, "init_chol_status");
-    return potrf(c, Lc, nmu, nmu, thr, cs);
+    return potrf_inv(c, Lc, nmu, nmu, thr, cs, dinv);
   };
   CholStatus hcs{};
   if ((st = factor(shift_rel > 0.0 ? shift_rel : 0.0))) return st;
@@ -279,8 +283,7 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
       return set_error(c, THC_ERR_NOT_PD, "thc_isdf: Cholesky of C failed at pivot %d", hcs.info);
   }
   // C^{-1} and zeta^T = C^{-1} Z^T.
-  if ((st = set_identity(c, Cinv, nmu, nmu))) return st;
-  if ((st = potrs(c, Lc, nmu, nmu, Cinv, nmu, nmu, cs))) return st;
+  if ((st = chol_inverse(c, Lc, nmu, nmu, dinv, Xinv, Tinv, Cinv, cs))) return st;
   {
     GemmArgs g;
     g.M = nmu; g.N = ng; g.K = nmu;
@@ -343,7 +346,7 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
   if (h_anti == 0) {
     copy_lower_to_full<<<nb2, 256, 0, s>>>(mre, nmu, xim);
     THC_LAUNCHED(c, "copy_lower_to_full");
-    if ((st = potrf(c, xim, nmu, nmu, zero, csm))) return st;
+    if ((st = potrf_inv(c, xim, nmu, nmu, zero, csm, dinv))) return st;
     export_l_real<<<nb2, 256, 0, s>>>(xim, nmu, Lout);
     THC_LAUNCHED(c, "export_l_real");
   } else {

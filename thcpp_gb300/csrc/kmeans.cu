@@ -67,6 +67,13 @@ struct KmState {
   unsigned long long absmax[3];
   int bad_label;
   int pad2;
+  unsigned long long bmin[3], bmax[3];   // grid bounding box (order-preserving bit patterns)
+  int nbin[3];
+  int nbins;
+  double blo[3], binv[3];                // bin origin and inverse bin width
+  double slack32;                        // absolute slack of the FP32 candidate bound
+  int diff_exact;                        // st->diff came from the sequential sum
+  int pad3;
 };
 
 struct KmBufs {
@@ -87,6 +94,10 @@ struct KmBufs {
   long long ng;
   int nmu;
   int nb;
+  int* perm;       // [ng] point indices grouped by spatial bin
+  int* pbin;       // [ng] bin of each point
+  int* bcount;     // [nbins_max] counts, then offsets, then cursors
+  int nbins_max;
 };
 
 __device__ __forceinline__ double d2_exact(double cx, double cy, double cz, double gx,
@@ -118,6 +129,18 @@ struct ArgMin {
   }
 };
 
+// Order-preserving map of a double to an unsigned key (for atomic min / max).
+__device__ __forceinline__ unsigned long long dkey(double x)
+{
+  unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double dunkey(unsigned long long k)
+{
+  unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
 __global__ void km_prep(const double* __restrict__ grid, const double* __restrict__ rho_in,
                         const int* __restrict__ init_idx, KmBufs b)
 {
@@ -148,6 +171,20 @@ __global__ void km_prep(const double* __restrict__ grid, const double* __restric
     atomicMax(&b.st->absmax[1], (unsigned long long)__double_as_longlong(ay));
     atomicMax(&b.st->absmax[2], (unsigned long long)__double_as_longlong(az));
   }
+  for (int d = 0; d < 3; d++) {
+    unsigned long long mn = ~0ULL, mx = 0ULL;
+    if (i < b.ng) mn = mx = dkey(grid[3 * i + d]);
+    for (int off = 16; off; off >>= 1) {
+      unsigned long long o1 = __shfl_xor_sync(0xffffffffu, mn, off);
+      unsigned long long o2 = __shfl_xor_sync(0xffffffffu, mx, off);
+      mn = o1 < mn ? o1 : mn;
+      mx = o2 > mx ? o2 : mx;
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&b.st->bmin[d], mn);
+      atomicMax(&b.st->bmax[d], mx);
+    }
+  }
   if (i < b.nmu) {
     long long g = init_idx[i];
     for (int d = 0; d < 3; d++) {
@@ -158,7 +195,7 @@ __global__ void km_prep(const double* __restrict__ grid, const double* __restric
   }
 }
 
-__global__ void km_finish_prep(KmState* st)
+__global__ void km_finish_prep(KmState* st, long long ng, int nbins_max)
 {
   // |a| <= |c| + |g| per component; centroids stay inside the grid's bounding box.
   double a2 = 0.0;
@@ -167,6 +204,321 @@ __global__ void km_finish_prep(KmState* st)
     a2 += 4.0 * m * m;
   }
   st->abound = sqrt(a2);
+  st->slack32 = 1e-4 * a2;
+  // Spatial bins of ~128 points: cubic cells over the bounding box.
+  double ext[3], vol = 1.0;
+  for (int d = 0; d < 3; d++) {
+    ext[d] = dunkey(st->bmax[d]) - dunkey(st->bmin[d]);
+    if (!(ext[d] > 0.0)) ext[d] = 1.0;
+    vol *= ext[d];
+  }
+  double h = cbrt(vol * 128.0 / (double)ng);
+  int nb = 1;
+  for (int d = 0; d < 3; d++) {
+    int n = (int)ceil(ext[d] / h);
+    n = n < 1 ? 1 : (n > 1024 ? 1024 : n);
+    st->nbin[d] = n;
+    nb *= n;
+  }
+  while (nb > nbins_max) {   // coarsen if the bin table would overflow
+    nb = 1;
+    for (int d = 0; d < 3; d++) {
+      st->nbin[d] = (st->nbin[d] + 1) / 2;
+      nb *= st->nbin[d];
+    }
+  }
+  st->nbins = nb;
+  for (int d = 0; d < 3; d++) {
+    st->blo[d] = dunkey(st->bmin[d]);
+    st->binv[d] = st->nbin[d] / ext[d];
+  }
+}
+
+__global__ void km_bin_count(const double* __restrict__ grid, KmBufs b)
+{
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= b.ng) return;
+  const KmState* st = b.st;
+  int bin = 0;
+  for (int d = 0; d < 3; d++) {
+    int q = (int)((grid[3 * i + d] - st->blo[d]) * st->binv[d]);
+    q = q < 0 ? 0 : (q >= st->nbin[d] ? st->nbin[d] - 1 : q);
+    bin = bin * st->nbin[d] + q;
+  }
+  b.pbin[i] = bin;
+  atomicAdd(&b.bcount[bin], 1);
+}
+
+// Single block: counts -> exclusive offsets (bcount[0..nbins)), cursors zeroed after.
+__global__ void km_bin_scan(KmBufs b)
+{
+  __shared__ int warp_sums[32];
+  int n = b.st->nbins;
+  int per = (n + blockDim.x - 1) / blockDim.x;
+  int lo = threadIdx.x * per, hi = min(n, lo + per);
+  int s = 0;
+  for (int k = lo; k < hi; k++) s += b.bcount[k];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = s;
+  for (int off = 1; off < 32; off <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+    int xw = w;
+    for (int off = 1; off < 32; off <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, xw, off);
+      if (lane >= off) xw += y;
+    }
+    warp_sums[lane] = xw - w;
+  }
+  __syncthreads();
+  int run = warp_sums[wid] + x - s;
+  for (int k = lo; k < hi; k++) {
+    int c = b.bcount[k];
+    b.bcount[k] = run;
+    b.bcount[b.nbins_max + k] = 0;
+    run += c;
+  }
+}
+
+__global__ void km_bin_scatter(KmBufs b)
+{
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= b.ng) return;
+  int bin = b.pbin[i];
+  int pos = b.bcount[bin] + atomicAdd(&b.bcount[b.nbins_max + bin], 1);
+  b.perm[pos] = (int)i;
+}
+
+// Ordered block-wide compaction of `flag` over the block's threads: returns this thread's
+// slot (or -1) and adds the block's count to *total (all threads see the new total).
+__device__ __forceinline__ int block_compact(bool flag, int* wsum, int* total)
+{
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned bal = __ballot_sync(0xffffffffu, flag);
+  if (lane == 0) wsum[wid] = __popc(bal);
+  __syncthreads();
+  int before = *total;
+  for (int w = 0; w < wid; w++) before += wsum[w];
+  int slot = flag ? before + __popc(bal & ((1u << lane) - 1u)) : -1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = *total;
+    for (int w = 0; w < nw; w++) t += wsum[w];
+    *total = t;
+  }
+  __syncthreads();
+  return slot;
+}
+
+constexpr int kPruneMax = 2048;   // candidate centroids kept in shared memory per tile
+
+// FP64 assign with exact spatial pruning.  A tile is 256 consecutive points of the
+// binned order.  With lb(c) / ub(c) the smallest / largest squared distance from centroid
+// c to the tile's bounding box and U = min_c ub(c), every point's nearest centroid has
+// squared distance <= U; a centroid with lb(c) > U (1 + 1e-9) is farther from every point
+// of the tile than its nearest centroid by a relative margin far above the rounding of
+// either bound or of the distance itself, so it can neither win nor tie after sqrt.  The
+// kept centroids are scanned in ascending index order with the exact semantics.
+__global__ void __launch_bounds__(kAssignThreads) km_assign64p(KmBufs b)
+{
+  const KmState* st = b.st;
+  if (st->done) return;
+  int it = st->iter;
+  const double* cx = b.cen + (size_t)(it & 1) * 3 * b.nmu;
+  const double* cy = cx + b.nmu;
+  const double* cz = cy + b.nmu;
+  extern __shared__ unsigned char sm[];
+  int* cand = (int*)sm;
+  double* ccx = (double*)(sm + sizeof(int) * kPruneMax);
+  double* ccy = ccx + kPruneMax;
+  double* ccz = ccy + kPruneMax;
+  __shared__ double red[3][2][kAssignThreads / 32];
+  __shared__ double uw[kAssignThreads / 32];
+  __shared__ int wsum[kAssignThreads / 32];
+  __shared__ int ncand;
+  long long t = blockIdx.x * (long long)kAssignThreads + threadIdx.x;
+  bool valid = t < b.ng;
+  long long i = valid ? b.perm[t] : 0;
+  double g[3] = {0, 0, 0};
+  if (valid) { g[0] = b.gx[i]; g[1] = b.gy[i]; g[2] = b.gz[i]; }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; d++) {
+    double mn = valid ? g[d] : CUDART_INF, mx = valid ? g[d] : -CUDART_INF;
+    for (int off = 16; off; off >>= 1) {
+      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, off));
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    }
+    if (lane == 0) { red[d][0][wid] = mn; red[d][1][wid] = mx; }
+  }
+  if (threadIdx.x == 0) ncand = 0;
+  __syncthreads();
+  for (int d = 0; d < 3; d++) {
+    lo[d] = red[d][0][0];
+    hi[d] = red[d][1][0];
+    for (int w = 1; w < kAssignThreads / 32; w++) {
+      lo[d] = fmin(lo[d], red[d][0][w]);
+      hi[d] = fmax(hi[d], red[d][1][w]);
+    }
+  }
+  // U = min over centroids of the largest squared distance to the box.
+  double u = CUDART_INF;
+  for (int k = threadIdx.x; k < b.nmu; k += kAssignThreads) {
+    double c3[3] = {cx[k], cy[k], cz[k]}, ub = 0.0;
+    for (int d = 0; d < 3; d++) {
+      double a = c3[d] - lo[d], e = c3[d] - hi[d];
+      ub += fmax(a * a, e * e);
+    }
+    u = fmin(u, ub);
+  }
+  for (int off = 16; off; off >>= 1) u = fmin(u, __shfl_xor_sync(0xffffffffu, u, off));
+  if (lane == 0) uw[wid] = u;
+  __syncthreads();
+  double U = uw[0];
+  for (int w = 1; w < kAssignThreads / 32; w++) U = fmin(U, uw[w]);
+  double cut = U * (1.0 + 1e-9);
+  for (int kb = 0; kb < b.nmu; kb += kAssignThreads) {
+    int k = kb + threadIdx.x;
+    bool keep = false;
+    double c3[3] = {0, 0, 0};
+    if (k < b.nmu) {
+      c3[0] = cx[k]; c3[1] = cy[k]; c3[2] = cz[k];
+      double lb = 0.0;
+      for (int d = 0; d < 3; d++) {
+        double v = fmax(0.0, fmax(lo[d] - c3[d], c3[d] - hi[d]));
+        lb += v * v;
+      }
+      keep = lb <= cut;
+    }
+    int slot = block_compact(keep, wsum, &ncand);
+    if (slot >= 0 && slot < kPruneMax) {
+      cand[slot] = k; ccx[slot] = c3[0]; ccy[slot] = c3[1]; ccz[slot] = c3[2];
+    }
+  }
+  int nc = ncand;
+  ArgMin am;
+  am.init();
+  if (nc <= kPruneMax) {
+    if (valid)
+      for (int j = 0; j < nc; j++) am.push(d2_exact(ccx[j], ccy[j], ccz[j], g[0], g[1], g[2]), cand[j]);
+  } else if (valid) {
+    for (int k = 0; k < b.nmu; k++) am.push(d2_exact(cx[k], cy[k], cz[k], g[0], g[1], g[2]), k);
+  }
+  if (valid) b.labels[(size_t)(it & 1) * b.ng + i] = am.k;
+}
+
+// FP32 filter with pruning.  Bounds are computed in FP32 with a relative margin 1e-4 and
+// an absolute slack 1e-4 |a|^2, far above their FP32 rounding, so the FP64 nearest
+// centroid is always kept; the margin test and the FP64 recheck then work as in km_assign32.
+__global__ void __launch_bounds__(kAssignThreads) km_assign32p(KmBufs b)
+{
+  KmState* st = b.st;
+  if (st->done) return;
+  int it = st->iter;
+  const float* cx = b.cen32 + (size_t)(it & 1) * 3 * b.nmu;
+  const float* cy = cx + b.nmu;
+  const float* cz = cy + b.nmu;
+  extern __shared__ unsigned char sm[];
+  int* cand = (int*)sm;
+  float* ccx = (float*)(sm + sizeof(int) * kPruneMax);
+  float* ccy = ccx + kPruneMax;
+  float* ccz = ccy + kPruneMax;
+  __shared__ float red[3][2][kAssignThreads / 32];
+  __shared__ float uw[kAssignThreads / 32];
+  __shared__ int wsum[kAssignThreads / 32];
+  __shared__ int ncand;
+  long long t = blockIdx.x * (long long)kAssignThreads + threadIdx.x;
+  bool valid = t < b.ng;
+  long long i = valid ? b.perm[t] : 0;
+  float g[3] = {0, 0, 0};
+  if (valid) { g[0] = b.fx[i]; g[1] = b.fy[i]; g[2] = b.fz[i]; }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float lo[3], hi[3];
+  for (int d = 0; d < 3; d++) {
+    float mn = valid ? g[d] : INFINITY, mx = valid ? g[d] : -INFINITY;
+    for (int off = 16; off; off >>= 1) {
+      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, off));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    }
+    if (lane == 0) { red[d][0][wid] = mn; red[d][1][wid] = mx; }
+  }
+  if (threadIdx.x == 0) ncand = 0;
+  __syncthreads();
+  for (int d = 0; d < 3; d++) {
+    lo[d] = red[d][0][0];
+    hi[d] = red[d][1][0];
+    for (int w = 1; w < kAssignThreads / 32; w++) {
+      lo[d] = fminf(lo[d], red[d][0][w]);
+      hi[d] = fmaxf(hi[d], red[d][1][w]);
+    }
+  }
+  float u = INFINITY;
+  for (int k = threadIdx.x; k < b.nmu; k += kAssignThreads) {
+    float c3[3] = {cx[k], cy[k], cz[k]}, ub = 0.f;
+    for (int d = 0; d < 3; d++) {
+      float a = c3[d] - lo[d], e = c3[d] - hi[d];
+      ub += fmaxf(a * a, e * e);
+    }
+    u = fminf(u, ub);
+  }
+  for (int off = 16; off; off >>= 1) u = fminf(u, __shfl_xor_sync(0xffffffffu, u, off));
+  if (lane == 0) uw[wid] = u;
+  __syncthreads();
+  float U = uw[0];
+  for (int w = 1; w < kAssignThreads / 32; w++) U = fminf(U, uw[w]);
+  float cut = U * (1.0f + 1e-4f) + (float)st->slack32;
+  for (int kb = 0; kb < b.nmu; kb += kAssignThreads) {
+    int k = kb + threadIdx.x;
+    bool keep = false;
+    float c3[3] = {0, 0, 0};
+    if (k < b.nmu) {
+      c3[0] = cx[k]; c3[1] = cy[k]; c3[2] = cz[k];
+      float lb = 0.f;
+      for (int d = 0; d < 3; d++) {
+        float v = fmaxf(0.f, fmaxf(lo[d] - c3[d], c3[d] - hi[d]));
+        lb += v * v;
+      }
+      keep = lb <= cut;
+    }
+    int slot = block_compact(keep, wsum, &ncand);
+    if (slot >= 0 && slot < kPruneMax) {
+      cand[slot] = k; ccx[slot] = c3[0]; ccy[slot] = c3[1]; ccz[slot] = c3[2];
+    }
+  }
+  int nc = ncand;
+  if (!valid) return;
+  float m1 = INFINITY, m2 = INFINITY;
+  int k1 = 0;
+  if (nc <= kPruneMax) {
+    for (int j = 0; j < nc; j++) {
+      float dx = ccx[j] - g[0], dy = ccy[j] - g[1], dz = ccz[j] - g[2];
+      float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+      if (d2 < m1) { m2 = m1; m1 = d2; k1 = cand[j]; }
+      else if (d2 < m2) { m2 = d2; }
+    }
+  } else {
+    for (int k = 0; k < b.nmu; k++) {
+      float dx = cx[k] - g[0], dy = cy[k] - g[1], dz = cz[k] - g[2];
+      float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+      if (d2 < m1) { m2 = m1; m1 = d2; k1 = k; }
+      else if (d2 < m2) { m2 = d2; }
+    }
+  }
+  const double uu = 5.9604644775390625e-08;
+  double a = st->abound;
+  double e1 = 2.0 * uu * (2.0 * sqrt((double)m1) * a + 5.0 * (double)m1);
+  double e2 = 2.0 * uu * (2.0 * sqrt((double)m2) * a + 5.0 * (double)m2);
+  if ((double)m2 - (double)m1 > e1 + e2 + 1e-300) {
+    b.labels[(size_t)(it & 1) * b.ng + i] = k1;
+  } else {
+    int slot = atomicAdd(&st->recheck_n, 1);
+    b.recheck[slot] = (int)i;
+  }
 }
 
 // FP64 assign: one thread per grid point, centroids staged through shared memory.
@@ -411,34 +763,44 @@ __global__ void km_scatter(KmBufs b)
 // (each rounded on its own, as the reference's `rho[i] * grid[i*ndim]`); four lanes then
 // add them into w, x, y, z strictly in ascending member order from shared memory, so the
 // sums round exactly as the reference's sequential loop (src/kmeans.cpp:121-126).
-constexpr int kSumWarps = 4;
+constexpr int kSumWarps = 1;
+constexpr int kSumChunk = 512;
 __global__ void __launch_bounds__(32 * kSumWarps) km_sums(KmBufs b)
 {
   KmState* st = b.st;
   if (st->done) return;
-  __shared__ double sv[kSumWarps][4][33];
+  // Products of up to kSumChunk members are formed by all lanes first (their loads are
+  // independent), then four lanes run the in-order FP64 chains from shared memory.
+  __shared__ double sv[4][kSumChunk];
   int it = st->iter;
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int k = blockIdx.x * kSumWarps + w;
+  int lane = threadIdx.x & 31;
+  int k = blockIdx.x;
   if (k >= b.nmu) return;
   int s = b.start[k], n = b.total[k];
   double acc = 0.0;  // lane q < 4 owns quantity q: 0 = w, 1 = x, 2 = y, 3 = z
-  for (int base = 0; base < n; base += 32) {
-    int m = base + lane;
-    if (m < n) {
-      int i = b.member[s + m];
+  for (int base = 0; base < n; base += kSumChunk) {
+    int cnt = min(kSumChunk, n - base);
+#pragma unroll 4
+    for (int m = lane; m < cnt; m += 32) {
+      int i = b.member[s + base + m];
       double r = b.rho[i];
-      sv[w][0][lane] = r;
-      sv[w][1][lane] = __dmul_rn(r, b.gx[i]);
-      sv[w][2][lane] = __dmul_rn(r, b.gy[i]);
-      sv[w][3][lane] = __dmul_rn(r, b.gz[i]);
+      sv[0][m] = r;
+      sv[1][m] = __dmul_rn(r, b.gx[i]);
+      sv[2][m] = __dmul_rn(r, b.gy[i]);
+      sv[3][m] = __dmul_rn(r, b.gz[i]);
     }
     __syncwarp();
     if (lane < 4) {
-      int cnt = min(32, n - base);
-      const double* v = sv[w][lane];
-#pragma unroll 8
-      for (int j = 0; j < cnt; j++) acc = __dadd_rn(acc, v[j]);
+      const double* v = sv[lane];
+      int j = 0;
+      for (; j + 4 <= cnt; j += 4) {
+        double t0 = v[j], t1 = v[j + 1], t2 = v[j + 2], t3 = v[j + 3];
+        acc = __dadd_rn(acc, t0);
+        acc = __dadd_rn(acc, t1);
+        acc = __dadd_rn(acc, t2);
+        acc = __dadd_rn(acc, t3);
+      }
+      for (; j < cnt; j++) acc = __dadd_rn(acc, v[j]);
     }
     __syncwarp();
   }
@@ -503,18 +865,26 @@ __global__ void km_normdiff(KmBufs b)
     terms[i] = __dmul_rn(q, q);
   }
   __syncthreads();
+  // Fixed-order tree sum of the terms (deterministic); it differs from the reference's
+  // sequential sum by at most ~(n + log n) u relative, so it decides `diff < threshold`
+  // identically unless the two are within 1e-10 of each other -- then, and for the value
+  // finally reported, the sequential sum is evaluated exactly (km_normdiff_exact).
+  double part = 0.0;
+  for (int i = threadIdx.x; i < n3; i += blockDim.x) part += terms[i];
+  for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    // One thread, index order: the reference's `diff += ...` loop.
-    double s = 0.0;
-    int i = 0;
-    for (; i + 8 <= n3; i += 8) {
-      double t0 = terms[i], t1 = terms[i + 1], t2 = terms[i + 2], t3 = terms[i + 3];
-      double t4 = terms[i + 4], t5 = terms[i + 5], t6 = terms[i + 6], t7 = terms[i + 7];
-      s = __dadd_rn(s, t0); s = __dadd_rn(s, t1); s = __dadd_rn(s, t2); s = __dadd_rn(s, t3);
-      s = __dadd_rn(s, t4); s = __dadd_rn(s, t5); s = __dadd_rn(s, t6); s = __dadd_rn(s, t7);
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
+    double diff = scale * sqrt(tot);
+    bool exact = fabs(diff - st->threshold) <= 1e-10 * st->threshold;
+    if (exact) {
+      double s = 0.0;
+      for (int i = 0; i < n3; i++) s = __dadd_rn(s, terms[i]);
+      diff = __dmul_rn(scale, __dsqrt_rn(s));
     }
-    for (; i < n3; i++) s = __dadd_rn(s, terms[i]);
-    double diff = __dmul_rn(scale, __dsqrt_rn(s));
+    st->diff_exact = exact;
     st->diff = diff;
     st->pct = 100.0 * (double)st->changed / (double)b.ng;
     b.log[it] = diff;
@@ -532,6 +902,33 @@ __global__ void km_normdiff(KmBufs b)
     }
     st->iter = it + 1;
   }
+}
+
+// The reference's sequential normed difference of the last iteration (one thread).
+__global__ void km_normdiff_exact(KmBufs b)
+{
+  KmState* st = b.st;
+  if (st->diff_exact || st->empty || st->iter < 1) return;
+  int it = st->iter - 1;
+  int n3 = 3 * b.nmu;
+  const double* a = b.cen + (size_t)((it + 1) & 1) * 3 * b.nmu;
+  const double* c = b.cen + (size_t)(it & 1) * 3 * b.nmu;
+  double ma = 0.0, mc = 0.0;
+  for (int i = 0; i < b.nmu * 3; i++) {
+    ma = fmax(ma, fabs(a[i]));
+    mc = fmax(mc, fabs(c[i]));
+  }
+  double scale = __dadd_rn(ma, mc);
+  double s = 0.0;
+  for (int i = 0; i < n3; i++) {
+    int k = i / 3, d = i - 3 * k;
+    double q = __ddiv_rn(__dsub_rn(a[d * b.nmu + k], c[d * b.nmu + k]), scale);
+    s = __dadd_rn(s, __dmul_rn(q, q));
+  }
+  double diff = __dmul_rn(scale, __dsqrt_rn(s));
+  st->diff = diff;
+  b.log[it] = diff;
+  st->diff_exact = 1;
 }
 
 // map_to_grid, part 1: each thread owns one centroid and scans one chunk of grid points.
@@ -656,9 +1053,15 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   double* logb = (double*)ws_get(c, WS_KM_LOG, sizeof(double) * 2 * max_it);
   int nch = (int)cdiv(ng, kMapChunk);
   double* part_s = (double*)ws_get(c, WS_KM_PART, (sizeof(double) + sizeof(int)) * (size_t)nmu * nch + 64);
+  const int nbins_max = (int)std::max<long long>(1024, ng / 32);
+  int* permw = (int*)ws_get(c, WS_KM_PERM, sizeof(int) * (2 * (size_t)ng + 2 * (size_t)nbins_max));
   if (!g64 || !g32 || !cen || !cen32 || !labels || !hist || !tot || !member || !terms ||
-      !recheck || !st || !logb || !part_s)
+      !recheck || !st || !logb || !part_s || !permw)
     return set_error(c, THC_ERR_NOMEM, "thc_kmeans: workspace allocation failed");
+  b.perm = permw;
+  b.pbin = permw + ng;
+  b.bcount = permw + 2 * ng;
+  b.nbins_max = nbins_max;
   int* part_i = (int*)(part_s + (size_t)nmu * nch);
   b.gx = g64; b.gy = g64 + ng; b.gz = g64 + 2 * ng; b.rho = g64 + 3 * ng;
   b.fx = g32; b.fy = g32 + ng; b.fz = g32 + 2 * ng;
@@ -669,13 +1072,33 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   KmState h{};
   h.max_it = max_it;
   h.threshold = threshold;
+  for (int d = 0; d < 3; d++) h.bmin[d] = ~0ULL;
   THC_CUDA(c, cudaMemcpyAsync(st, &h, sizeof(KmState), cudaMemcpyHostToDevice, s));
   THC_CUDA(c, cudaEventRecord(c->ev0, s));
   int nprep = (int)cdiv(std::max<long long>(ng, nmu), 256);
   km_prep<<<nprep, 256, 0, s>>>(grid, rho, init, b);
   THC_LAUNCHED(c, "km_prep");
-  km_finish_prep<<<1, 1, 0, s>>>(st);
+  km_finish_prep<<<1, 1, 0, s>>>(st, ng, nbins_max);
   THC_LAUNCHED(c, "km_finish_prep");
+  // Spatial binning of the grid (once per call): perm lists the points bin by bin.
+  const bool prune = c->km_prune && nmu >= 64;
+  if (prune) {
+    THC_CUDA(c, cudaMemsetAsync(b.bcount, 0, sizeof(int) * 2 * (size_t)nbins_max, s));
+    km_bin_count<<<(int)cdiv(ng, 256), 256, 0, s>>>(grid, b);
+    THC_LAUNCHED(c, "km_bin_count");
+    km_bin_scan<<<1, 1024, 0, s>>>(b);
+    THC_LAUNCHED(c, "km_bin_scan");
+    km_bin_scatter<<<(int)cdiv(ng, 256), 256, 0, s>>>(b);
+    THC_LAUNCHED(c, "km_bin_scatter");
+  }
+  const size_t prune64_smem = (size_t)kPruneMax * (sizeof(int) + 3 * sizeof(double));
+  const size_t prune32_smem = (size_t)kPruneMax * (sizeof(int) + 3 * sizeof(float));
+  if (prune) {
+    THC_CUDA(c, cudaFuncSetAttribute(km_assign64p, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)prune64_smem));
+    THC_CUDA(c, cudaFuncSetAttribute(km_assign32p, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)prune32_smem));
+  }
 
   const bool mixed = c->precision == THC_PREC_MIXED;
   int nassign = (int)cdiv(ng, kAssignThreads);
@@ -689,16 +1112,24 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     THC_CUDA(c, cudaFuncSetAttribute(km_normdiff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)norm_smem));
   int* hflag = (int*)c->pinned;
   const int kCheckEvery = 8;
-  for (int it = 0; it < max_it; it++) {
+  // One k-means iteration; every kernel reads the iteration index from device state and
+  // returns at once after convergence, so the same launch sequence serves any iteration.
+  auto iteration = [&](bool prof) -> int {
     if (mixed) {
-      ProfScope prof(c, "km_assign");
-      km_assign32<<<nassign, kAssignThreads, 0, s>>>(b);
+      {
+        ProfScope p(prof ? c : nullptr, "km_assign");
+        if (prune) km_assign32p<<<nassign, kAssignThreads, prune32_smem, s>>>(b);
+        else km_assign32<<<nassign, kAssignThreads, 0, s>>>(b);
+      }
       THC_LAUNCHED(c, "km_assign32");
       km_recheck<<<152 * 4, 256, 0, s>>>(b);
       THC_LAUNCHED(c, "km_recheck");
     } else {
-      ProfScope prof(c, "km_assign");
-      km_assign64<<<nassign, kAssignThreads, 0, s>>>(b);
+      {
+        ProfScope p(prof ? c : nullptr, "km_assign");
+        if (prune) km_assign64p<<<nassign, kAssignThreads, prune64_smem, s>>>(b);
+        else km_assign64<<<nassign, kAssignThreads, 0, s>>>(b);
+      }
       THC_LAUNCHED(c, "km_assign64");
     }
     THC_CUDA(c, cudaMemsetAsync(hist, 0, sizeof(int) * (size_t)nmu * b.nb, s));
@@ -710,16 +1141,62 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     THC_LAUNCHED(c, "km_kscan");
     km_scatter<<<b.nb, 128, hist_smem, s>>>(b);
     THC_LAUNCHED(c, "km_scatter");
-    km_sums<<<(int)cdiv(nmu, kSumWarps), 32 * kSumWarps, 0, s>>>(b);
+    km_sums<<<nmu, 32 * kSumWarps, 0, s>>>(b);
     THC_LAUNCHED(c, "km_sums");
     km_normdiff<<<1, 1024, norm_smem, s>>>(b);
     THC_LAUNCHED(c, "km_normdiff");
-    if ((it + 1) % kCheckEvery == 0 && it + 1 < max_it) {
+    return THC_OK;
+  };
+  // A CUDA graph of kCheckEvery iterations, cached on the context for these buffers.
+  const bool graphs = c->use_graphs && !c->profile;
+  cudaGraphExec_t gexec = nullptr;
+  if (graphs) {
+    std::vector<long long> key = {ng, nmu, mixed, prune, (long long)(uintptr_t)g64,
+                                  (long long)(uintptr_t)cen, (long long)(uintptr_t)hist,
+                                  (long long)(uintptr_t)st, (long long)(uintptr_t)permw,
+                                  (long long)(uintptr_t)member, (long long)(uintptr_t)logb,
+                                  (long long)(uintptr_t)s};
+    if (c->km_graph && c->km_graph_key == key) {
+      gexec = c->km_graph;
+    } else {
+      if (c->km_graph) {
+        cudaGraphExecDestroy(c->km_graph);
+        c->km_graph = nullptr;
+      }
+      cudaGraph_t graph;
+      THC_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      int rc = THC_OK;
+      for (int k = 0; k < kCheckEvery && rc == THC_OK; k++) rc = iteration(false);
+      cudaError_t ce = cudaStreamEndCapture(s, &graph);
+      if (rc) return rc;
+      if (ce != cudaSuccess) return set_error(c, THC_ERR_CUDA, "k-means graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) return set_error(c, THC_ERR_CUDA, "k-means graph instantiate: %s", cudaGetErrorString(ce));
+      c->km_graph = gexec;
+      c->km_graph_key = key;
+    }
+  }
+  for (int it = 0; it < max_it;) {
+    int nblock = std::min(kCheckEvery, max_it - it);
+    if (gexec && nblock == kCheckEvery) {
+      THC_CUDA(c, cudaGraphLaunch(gexec, s));
+      c->launches += (mixed ? 8LL : 7LL) * kCheckEvery;  // kernels per captured iteration
+    } else {
+      for (int k = 0; k < nblock; k++) {
+        int rc = iteration(true);
+        if (rc) return rc;
+      }
+    }
+    it += nblock;
+    if (it < max_it) {
       THC_CUDA(c, cudaMemcpyAsync(hflag, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
       THC_CUDA(c, cudaStreamSynchronize(s));
       if (*hflag) break;
     }
   }
+  km_normdiff_exact<<<1, 1, 0, s>>>(b);
+  THC_LAUNCHED(c, "km_normdiff_exact");
   // Map the final centroids to the grid, sort, count duplicates.
   int* didx = is_device_ptr(out_idx) ? out_idx : (int*)((char*)hist);  // hist is free now
   int* dups = (int*)(part_i + (size_t)nmu * nch);

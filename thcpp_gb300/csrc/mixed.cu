@@ -123,6 +123,12 @@ __global__ void mixed_scalars(double* dmean, double* thr, double* shift, double*
   *zero = 0.0;
 }
 
+__global__ void to_f32(const double* __restrict__ x, long long n, float* y)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e < n) y[e] = (float)x[e];
+}
+
 __global__ void init_cs(CholStatus* cs)
 {
   cs->flag = 0;
@@ -164,13 +170,17 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   double* Mw = (double*)ws_get(c, WS_M, sizeof(double) * 4 * nn);
   double* Lw = (double*)ws_get(c, WS_L, sizeof(double) * 2 * nn);
   char* scr = (char*)ws_get(c, WS_SCRATCH, 4096);
+  const long long nblk64 = (nmu + 63) / 64;
+  double* dinv = (double*)ws_get(c, WS_DINV, sizeof(double) * (nblk64 * 64 * 64 + nn + 64 * (long long)nmu));
+  double* Xinv = dinv + nblk64 * 64 * 64;
+  double* Tinv = Xinv + nn;
   size_t a_elems = std::max({(size_t)sp * ng_pad * no_kpad, (size_t)sz * mu_pad * mu_kpad,
                              (size_t)sm * mu_pad * k2_pad});
   size_t b_elems = std::max((size_t)sp * mu_pad * no_kpad, (size_t)sz * ng_pad * mu_kpad);
   __nv_bfloat16* sa = (__nv_bfloat16*)ws_get(c, WS_SLICE_A, sizeof(__nv_bfloat16) * a_elems);
   __nv_bfloat16* sb = (__nv_bfloat16*)ws_get(c, WS_SLICE_B, sizeof(__nv_bfloat16) * b_elems);
   int* ex = (int*)ws_get(c, WS_SLICE_E, sizeof(int) * (mu_pad + ng_pad + 64));
-  if (!phimu || !C || !Cinv || !zg || !zeta || !zhat || !dsym || !danti || !Mw || !Lw || !scr ||
+  if (!phimu || !C || !Cinv || !zg || !zeta || !zhat || !dsym || !danti || !Mw || !Lw || !scr || !dinv ||
       !sa || !sb || !ex)
     return set_error(c, THC_ERR_NOMEM, "thc_isdf (mixed): workspace allocation failed");
   float* sq = (float*)(dsym + nc);
@@ -218,7 +228,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     }
     init_cs<<<1, 1, 0, s>>>(cs);
     THC_LAUNCHED(c, "init_cs");
-    return potrf(c, Lc, nmu, nmu, thr, cs);
+    return potrf_inv(c, Lc, nmu, nmu, thr, cs, dinv);
   };
   // Z = (Phi Phi_mu^T)^2 (N_g x N_mu) via the sliced GEMM: A = Phi sliced by grid point,
   // B = Phi_mu sliced by interpolating point; Z's rows are then K-contiguous for the solve.
@@ -254,16 +264,28 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     if (hcs.flag)
       return set_error(c, THC_ERR_NOT_PD, "thc_isdf: Cholesky of C failed at pivot %d", hcs.info);
   }
-  if ((st = set_identity(c, Cinv, nmu, nmu))) return st;
-  if ((st = potrs(c, Lc, nmu, nmu, Cinv, nmu, nmu, cs))) return st;
+  if ((st = chol_inverse(c, Lc, nmu, nmu, dinv, Xinv, Tinv, Cinv, cs))) return st;
   // zeta^T = C^{-1} Z^T: A = C^{-1} sliced by rows, B = Z sliced by rows (grid points).
-  if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, sz, sa, mu_kpad,
-                              mu_pad * mu_kpad, ea, mu_pad)))
-    return st;
-  if ((st = oz_slice_rows_f64(c, zg, ng, nmu, nmu, 1, nullptr, 0, sz, sb, mu_kpad,
-                              ng_pad * mu_kpad, eb, ng_pad)))
-    return st;
-  {
+  // A rank-deficient C (shifted) has an inverse whose null-space entries are ~1/shift, so
+  // the product cancels by far more than any slice depth resolves: it runs in FP64 then.
+  if (shifted) {
+    double* z64 = (double*)ws_get(c, WS_ZTMP, sizeof(double) * nmu * ng);
+    if (!z64) return set_error(c, THC_ERR_NOMEM, "thc_isdf: FP64 zeta buffer");
+    GemmArgs g;
+    g.M = nmu; g.N = ng; g.K = nmu;
+    g.A = Cinv; g.sam = nmu; g.sak = 1;
+    g.B = zg; g.sbn = nmu; g.sbk = 1;
+    g.C = z64; g.ldc = ng;
+    if ((st = dgemm(c, g))) return st;
+    to_f32<<<(unsigned)cdiv((long long)nmu * ng, 256), 256, 0, s>>>(z64, (long long)nmu * ng, zeta);
+    THC_LAUNCHED(c, "to_f32");
+  } else {
+    if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, sz, sa, mu_kpad,
+                                mu_pad * mu_kpad, ea, mu_pad)))
+      return st;
+    if ((st = oz_slice_rows_f64(c, zg, ng, nmu, nmu, 1, nullptr, 0, sz, sb, mu_kpad,
+                                ng_pad * mu_kpad, eb, ng_pad)))
+      return st;
     OzArgs g;
     g.M = nmu; g.N = ng; g.K = nmu;
     g.a.s = sa; g.a.e = ea; g.a.ld = mu_kpad; g.a.slice_stride = mu_pad * mu_kpad;
@@ -318,7 +340,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   if (h_anti == 0) {
     copy_lower_to_full_m<<<nb2, 256, 0, s>>>(mre, nmu, xim);
     THC_LAUNCHED(c, "copy_lower_to_full");
-    if ((st = potrf(c, xim, nmu, nmu, zero, csm))) return st;
+    if ((st = potrf_inv(c, xim, nmu, nmu, zero, csm, dinv))) return st;
     export_l_real_m<<<nb2, 256, 0, s>>>(xim, nmu, Lout);
     THC_LAUNCHED(c, "export_l_real");
   } else {

@@ -269,36 +269,50 @@ __global__ void slice_rows_kernel(const double* __restrict__ X, long long rows, 
   }
 }
 
-// FP32 input scaled by an FP32 copy of `scale`: the product is rounded once to FP32 and
-// then sliced exactly in FP32 arithmetic.
+// FP32 input scaled by an FP32 copy of `scale` (rounded once to FP32, then sliced exactly
+// in FP32 arithmetic).  Two passes so that long rows use the whole GPU: per-row maxima by
+// column chunks (atomicMax on the bit pattern, valid for non-negative floats), then the
+// slices with one thread per element.
+__global__ void rowmax_f32_kernel(const float* __restrict__ X, long long rows, long long cols,
+                                  long long ldx, const float* __restrict__ scale, int shift,
+                                  unsigned* rowmax)
+{
+  long long r = blockIdx.y;
+  long long c0 = (long long)blockIdx.x * 4096;
+  float mx = 0.f;
+  if (r < rows)
+    for (long long cc = c0 + threadIdx.x; cc < cols && cc < c0 + 4096; cc += blockDim.x) {
+      float v = X[r * ldx + cc];
+      if (scale) v *= scale[cc >> shift];
+      mx = fmaxf(mx, fabsf(v));
+    }
+  for (int off = 16; off; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(&rowmax[r], __float_as_uint(mx));
+}
+
 __global__ void slice_rows_f32_kernel(const float* __restrict__ X, long long rows,
                                       long long cols, long long ldx,
                                       const float* __restrict__ scale, int shift, int ns,
                                       __nv_bfloat16* out, long long ldo, long long sstride,
-                                      int* exps, long long rows_pad)
+                                      const unsigned* __restrict__ rowmax, int* exps)
 {
-  long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (r >= rows_pad) return;
-  auto val = [&](long long cidx) -> float {
-    float v = X[r * ldx + cidx];
-    if (scale) v *= scale[cidx >> shift];
-    return v;
-  };
-  float mx = 0.f;
-  if (r < rows)
-    for (long long cc = lane; cc < cols; cc += 32) mx = fmaxf(mx, fabsf(val(cc)));
-  for (int off = 16; off; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  long long r = blockIdx.y;
+  long long cc = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  float mx = __uint_as_float(rowmax[r]);
   int e = 0;
   if (mx > 0.f) frexpf(mx, &e);
-  if (lane == 0) exps[r] = e;
-  for (long long cc = lane; cc < ldo; cc += 32) {
-    float x = (r < rows && cc < cols) ? ldexpf(val(cc), 7 - e) : 0.f;
-    for (int s = 0; s < ns; s++) {
-      float q = rintf(x);
-      out[s * sstride + r * ldo + cc] = __float2bfloat16_rn(q);
-      x = (x - q) * 128.f;
-    }
+  if (cc == 0) exps[r] = e;
+  if (cc >= ldo) return;
+  float x = 0.f;
+  if (r < rows && cc < cols) {
+    float v = X[r * ldx + cc];
+    if (scale) v *= scale[cc >> shift];
+    x = ldexpf(v, 7 - e);
+  }
+  for (int s = 0; s < ns; s++) {
+    float q = rintf(x);
+    out[s * sstride + r * ldo + cc] = __float2bfloat16_rn(q);
+    x = (x - q) * 128.f;
   }
 }
 
@@ -360,9 +374,16 @@ int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, lo
                       const float* scale, int scale_shift, int nslices, __nv_bfloat16* out,
                       long long ldo, long long slice_stride, int* exps, long long rows_pad)
 {
-  long long threads = rows_pad * 32;
-  slice_rows_f32_kernel<<<(unsigned)cdiv(threads, 256), 256, 0, c->stream>>>(
-      X, rows, cols, ldx, scale, scale_shift, nslices, out, ldo, slice_stride, exps, rows_pad);
+  unsigned* rowmax = (unsigned*)ws_get(c, WS_ROWMAX, sizeof(unsigned) * rows_pad);
+  if (!rowmax) return set_error(c, THC_ERR_NOMEM, "slice_rows_f32: row maxima");
+  THC_CUDA(c, cudaMemsetAsync(rowmax, 0, sizeof(unsigned) * rows_pad, c->stream));
+  if (rows_pad > 65535) return set_error(c, THC_ERR_SHAPE, "slice_rows_f32: too many rows");
+  dim3 g1((unsigned)cdiv(cols, 4096), (unsigned)rows_pad);
+  rowmax_f32_kernel<<<g1, 256, 0, c->stream>>>(X, rows, cols, ldx, scale, scale_shift, rowmax);
+  THC_LAUNCHED(c, "rowmax_f32");
+  dim3 g2((unsigned)cdiv(ldo, 256), (unsigned)rows_pad);
+  slice_rows_f32_kernel<<<g2, 256, 0, c->stream>>>(X, rows, cols, ldx, scale, scale_shift,
+                                                   nslices, out, ldo, slice_stride, rowmax, exps);
   THC_LAUNCHED(c, "slice_rows_f32");
   return THC_OK;
 }

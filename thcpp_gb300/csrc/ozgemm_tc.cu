@@ -139,6 +139,32 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// Error-free transformations in FP32 (Knuth's TwoSum; Dekker's FastTwoSum for |a| >= |b|).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e)
+{
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+// (h, l) += x for a double-word accumulator (error ~2^-48 relative).
+__device__ __forceinline__ void dw_add(float& h, float& l, float x)
+{
+  float s, e;
+  two_sum(h, x, s, e);
+  e = __fadd_rn(e, l);
+  fast_two_sum(s, e, h, l);
+}
+__device__ __forceinline__ float pow2f(int e)
+{
+  if (e > -127 && e < 128) return __int_as_float((e + 127) << 23);
+  return ldexpf(1.f, e);
+}
+
 __device__ __forceinline__ double pow2d(int e)
 {
   if (e > -1022 && e < 1023) return __longlong_as_double((long long)(e + 1023) << 52);
@@ -290,9 +316,10 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     const int half = ew >> 2;                // which 32-column half of the 64-wide tile
     const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
     const int col0 = half * 32;
-    double acc[32];
+    // Double-word FP32 accumulators: no FP64 arithmetic until the final FP64 stores.
+    float ah[32], al[32];
 #pragma unroll
-    for (int q = 0; q < 32; q++) acc[q] = 0.0;
+    for (int q = 0; q < 32; q++) { ah[q] = 0.f; al[q] = 0.f; }
     float v[32];
     bool ok = true;
     for (int ch = 0; ch < nchunks; ch++) {
@@ -305,32 +332,45 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       asm volatile("tcgen05.fence::before_thread_sync;\n");
       __syncwarp();
       if (lane == 0) mbar_arrive(acc_empty);
+      // l0, 2^-7 l1, 2^-14 l2 are exact floats (integers below 2^24, scaled by powers of
+      // two); their sum needs <= 38 bits and is carried exactly in (s, e).
 #pragma unroll
       for (int q = 0; q < 32; q++) {
-        double t = (double)l0[q];
-        if (LV > 1) t = __fma_rn((double)l1[q], 0x1p-7, t);
-        if (LV > 2) t = __fma_rn((double)l2[q], 0x1p-14, t);
-        acc[q] += t;
+        float s1 = l0[q], e1 = 0.f;
+        if (LV > 1) two_sum(l0[q], l1[q] * 0x1p-7f, s1, e1);
+        if (LV > 2) {
+          float s2, e2;
+          two_sum(s1, l2[q] * 0x1p-14f, s2, e2);
+          s1 = s2;
+          e1 = __fadd_rn(e1, e2);
+        }
+        dw_add(ah[q], al[q], s1);
+        dw_add(ah[q], al[q], e1);
       }
     }
     if (ok && LV > 3 && nstages > 0) {
       for (int l = 3; l < LV; l++) {
         tmem_ld32(tmem + lane_base + l * TBN + col0, v);
-        double sc = pow2d(-7 * l);
+        float sc = pow2f(-7 * l);
 #pragma unroll
-        for (int q = 0; q < 32; q++) acc[q] = __fma_rn((double)v[q], sc, acc[q]);
+        for (int q = 0; q < 32; q++) al[q] = __fmaf_rn(v[q], sc, al[q]);
       }
     }
     if (ok && !*abort) {
       long long m = m0 + quad * 32 + lane;
       if (m < g.M) {
-        int ea = g.ea[m];
-#pragma unroll 4
+        int ea = g.ea[m] - 14;
+#pragma unroll
         for (int q = 0; q < 32; q++) {
           long long n = n0 + col0 + q;
-          if (n >= g.N) break;
-          if (g.lower_only && n > m) break;
-          double val = acc[q] * pow2d(ea + g.eb[n] - 14);
+          if (n >= g.N || (g.lower_only && n > m)) continue;
+          int ex = ea + g.eb[n];
+          if (g.epilogue == OZ_STORE_F32 && g.ksplit <= 1 && ex > -126 && ex < 127) {
+            float sc = pow2f(ex);
+            ((float*)g.C)[m * g.ldc + n] = __fadd_rn(ah[q], al[q]) * sc;
+            continue;
+          }
+          double val = ((double)ah[q] + (double)al[q]) * pow2d(ex);
           if (g.ksplit > 1) {
             g.part[((long long)blockIdx.z * g.M + m) * g.N + n] = val;
             continue;
