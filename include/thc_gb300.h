@@ -142,6 +142,44 @@ int thc_isdf(thc_ctx* ctx, const double* phi, long long ng, int norb, const int*
              const int* mesh, const double* coulG, double shift_rel, double* out_orbitals,
              double* out_M, double* out_L, thc_isdf_stats* stats);
 
+/*
+ * One system of a batch: the inputs of thc_kmeans (grid, rho, init_idx, max_it, threshold)
+ * and of thc_isdf (phi, norb, mesh, coulG, shift_rel), with nmu shared; outputs as in those
+ * calls (out_idx required, the others optional).  status / stats are written back.
+ */
+typedef struct thc_system {
+  const double* grid;
+  const double* rho;
+  long long ng;
+  int nmu;
+  const int* init_idx;
+  int max_it;
+  double threshold;
+  const double* phi;
+  int norb;
+  const int* mesh;
+  const double* coulG;
+  double shift_rel;
+  int* out_idx;
+  double* out_orbitals;
+  double* out_M;
+  double* out_L;
+  int status;
+  thc_kmeans_stats kmeans_stats;
+  thc_isdf_stats isdf_stats;
+} thc_system;
+
+/*
+ * Factorise nsys independent systems (k-means points, then ISDF) on one device.  Work is
+ * spread over nstreams worker contexts, each with its own CUDA stream, workspace and host
+ * thread, so that the kernels of small systems overlap on the GPU; nstreams = 1 runs the
+ * systems one after another.  Worker contexts are cached per (device, precision) and
+ * reused by later calls.  Returns THC_OK if every system succeeded (each system's own
+ * status is in systems[i].status).  The reference factorises one system per run of
+ * thcpp.x (src/main.cpp:18-77); this batches that sequence.
+ */
+int thc_factorize_batched(int device, int precision, thc_system* systems, int nsys, int nstreams);
+
 #ifdef __cplusplus
 }
 #endif

@@ -100,12 +100,18 @@ def test_isdf_rank_deficient_c1(request, prec):
     inv, inv_ref = _rel(th, ex), _rel(th_ref, ex)
     print(f"c1 {prec}: ||dM||/||M|| = {_rel(M, ref['M']):.3e}; pair-Coulomb error "
           f"{inv:.3e} (oracle {inv_ref:.3e})")
-    assert _rel(M, ref["M"]) < (1e-3 if prec == "fp64" else 1e-1)
+    assert _rel(M, ref["M"]) < (1e-3 if prec == "fp64" else 1e-2)
     assert inv < 1e-4
 
 
 def test_sliced_gemm_tc_matches_mma_sync(lib):
-    """The tcgen05 sliced GEMM against the warp-level mma.sync one (same slicing)."""
+    """The tcgen05 sliced GEMM against the warp-level mma.sync one (same slicing).
+
+    Both sum the same exact slice products, but in a different order and precision (the
+    tcgen05 epilogue folds in double-word FP32, the mma.sync one in FP64); zeta is then
+    rounded to FP32 in both, where a one-ulp flip (2^-24 = 6e-8 relative) of single entries
+    is expected.  The two must agree far inside the 1e-6 budget against the FP64 path.
+    """
     s = system("c2")
     idx = kmeans_idx("c2")
     out = {}
@@ -115,7 +121,7 @@ def test_sliced_gemm_tc_matches_mma_sync(lib):
             out[tc] = _cplx(ctx.isdf(s.phi, idx, s.mesh, s.coulG)["M"])
     d = _rel(out[1], out[0])
     print(f"tc vs mma.sync ||dM||/||M|| = {d:.3e}")
-    assert d < 1e-9
+    assert d < 1e-7
 
 
 def test_isdf_mesh_mismatch(gpu_ctx_fp64):

@@ -33,7 +33,7 @@ EXPORTS = [
     "thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
     "thc_ctx_last_error", "thc_status_string", "thc_ctx_kernel_launches",
     "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
-    "thc_kmeans_history",
+    "thc_kmeans_history", "thc_factorize_batched",
 ]
 
 
@@ -49,6 +49,18 @@ class IsdfStats(ctypes.Structure):
                 ("rank_deficient", ctypes.c_int), ("n_anti", ctypes.c_int),
                 ("shift_used", ctypes.c_double), ("c_min_pivot", ctypes.c_double),
                 ("device_ms", ctypes.c_double)]
+
+
+class System(ctypes.Structure):
+    """One system of thc_factorize_batched (include/thc_gb300.h: thc_system)."""
+    _fields_ = [("grid", ctypes.c_void_p), ("rho", ctypes.c_void_p), ("ng", ctypes.c_longlong),
+                ("nmu", ctypes.c_int), ("init_idx", ctypes.c_void_p), ("max_it", ctypes.c_int),
+                ("threshold", ctypes.c_double), ("phi", ctypes.c_void_p),
+                ("norb", ctypes.c_int), ("mesh", ctypes.c_void_p), ("coulG", ctypes.c_void_p),
+                ("shift_rel", ctypes.c_double), ("out_idx", ctypes.c_void_p),
+                ("out_orbitals", ctypes.c_void_p), ("out_M", ctypes.c_void_p),
+                ("out_L", ctypes.c_void_p), ("status", ctypes.c_int),
+                ("kmeans_stats", KMeansStats), ("isdf_stats", IsdfStats)]
 
 
 class ThcError(RuntimeError):
@@ -91,6 +103,8 @@ def load(build_if_missing: bool = False):
     lib.thc_ctx_kernel_time.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(cd),
                                         ctypes.POINTER(cll)]
     lib.thc_ctx_kernel_time.restype = ci
+    lib.thc_factorize_batched.argtypes = [ci, ci, ctypes.POINTER(System), ci, ci]
+    lib.thc_factorize_batched.restype = ci
     lib.thc_kmeans_history.argtypes = [vp, vp, vp, ci]
     lib.thc_kmeans_history.restype = ci
     lib.thc_kmeans_initial_indices.argtypes = [cll, ci, cu, vp]
@@ -114,6 +128,23 @@ def _ptr(a):
             raise ValueError("arrays must be C-contiguous")
         return a.ctypes.data_as(ctypes.c_void_p)
     raise TypeError(f"unsupported array type {type(a)}")
+
+
+def factorize_batched(systems, device=0, precision=THC_PREC_MIXED, nstreams=8):
+    """Run thc_factorize_batched on a list of dicts with the thc_system fields.
+
+    Array fields hold numpy arrays or device tensors (kept alive by the caller).
+    Returns (status, array of System).
+    """
+    arr = (System * len(systems))()
+    for i, d in enumerate(systems):
+        for k, v in d.items():
+            if hasattr(v, "data_ptr") or isinstance(v, np.ndarray):
+                setattr(arr[i], k, _ptr(v).value if _ptr(v) is not None else None)
+            else:
+                setattr(arr[i], k, v)
+    st = load().thc_factorize_batched(device, precision, arr, len(systems), nstreams)
+    return st, arr
 
 
 def initial_indices(ng: int, nmu: int, seed: int) -> np.ndarray:

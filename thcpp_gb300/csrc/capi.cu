@@ -3,7 +3,11 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
+#include <memory>
+#include <mutex>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -308,6 +312,55 @@ int thc_isdf(thc_ctx* h, const double* phi, long long ng, int norb, const int* i
   if (stats) memset(stats, 0, sizeof(*stats));
   return thc::isdf_run(&h->c, phi, ng, norb, idx, nmu, mesh, coulG, shift_rel, out_orbitals,
                        out_M, out_L, stats);
+}
+
+namespace {
+std::mutex g_pool_mu;
+std::map<std::pair<int, int>, std::vector<thc_ctx*>> g_pool;
+}  // namespace
+
+int thc_factorize_batched(int device, int precision, thc_system* sys, int nsys, int nstreams)
+{
+  if (!sys || nsys < 0 || nstreams < 1 || nstreams > 64) return THC_ERR_ARG;
+  if (nsys == 0) return THC_OK;
+  nstreams = std::min(nstreams, nsys);
+  std::vector<thc_ctx*> workers;
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    auto& pool = g_pool[{device, precision}];
+    while ((int)pool.size() < nstreams) {
+      thc_ctx* h = nullptr;
+      int st = thc_ctx_create(device, precision, &h);
+      if (st) return st;
+      pool.push_back(h);
+    }
+    workers.assign(pool.begin(), pool.begin() + nstreams);
+  }
+  std::atomic<int> next(0);
+  auto work = [&](thc_ctx* h) {
+    cudaSetDevice(device);
+    for (int i = next++; i < nsys; i = next++) {
+      thc_system& s = sys[i];
+      memset(&s.kmeans_stats, 0, sizeof(s.kmeans_stats));
+      memset(&s.isdf_stats, 0, sizeof(s.isdf_stats));
+      s.status = thc::kmeans_run(&h->c, s.grid, s.rho, s.ng, s.nmu, s.init_idx, s.max_it,
+                                 s.threshold, s.out_idx, &s.kmeans_stats);
+      if (s.status != THC_OK) continue;
+      s.status = thc::isdf_run(&h->c, s.phi, s.ng, s.norb, s.out_idx, s.nmu, s.mesh, s.coulG,
+                               s.shift_rel, s.out_orbitals, s.out_M, s.out_L, &s.isdf_stats);
+    }
+    cudaStreamSynchronize(h->c.stream);
+  };
+  if (nstreams == 1) {
+    work(workers[0]);
+  } else {
+    std::vector<std::thread> th;
+    for (int w = 0; w < nstreams; w++) th.emplace_back(work, workers[w]);
+    for (auto& t : th) t.join();
+  }
+  for (int i = 0; i < nsys; i++)
+    if (sys[i].status != THC_OK && sys[i].status != THC_ERR_NOT_PD) return sys[i].status;
+  return THC_OK;
 }
 
 }  // extern "C"

@@ -931,6 +931,84 @@ __global__ void km_normdiff_exact(KmBufs b)
   st->diff_exact = 1;
 }
 
+// Bounding boxes of the 256-point tiles of the binned order (for the pruned map_to_grid).
+__global__ void km_tile_boxes(KmBufs b, double* box)
+{
+  __shared__ double red[6][8];
+  long long t = blockIdx.x * 256LL + threadIdx.x;
+  bool valid = t < b.ng;
+  long long i = valid ? b.perm[t] : 0;
+  double g[3] = {valid ? b.gx[i] : 0.0, valid ? b.gy[i] : 0.0, valid ? b.gz[i] : 0.0};
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int d = 0; d < 3; d++) {
+    double mn = valid ? g[d] : CUDART_INF, mx = valid ? g[d] : -CUDART_INF;
+    for (int off = 16; off; off >>= 1) {
+      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, off));
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    }
+    if (lane == 0) { red[d][wid] = mn; red[3 + d][wid] = mx; }
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    int d = threadIdx.x;
+    double v = red[d][0];
+    for (int w = 1; w < 8; w++) v = d < 3 ? fmin(v, red[d][w]) : fmax(v, red[d][w]);
+    box[(long long)blockIdx.x * 6 + d] = v;
+  }
+}
+
+// map_to_grid with exact pruning: one warp per centroid.  U = min over tiles of the largest
+// squared distance from the centroid to the tile box bounds the nearest squared distance;
+// only tiles whose smallest squared distance is <= U (1 + 1e-9) are scanned.  Tiles are not
+// in grid-index order, so candidates merge on (sqrt distance, grid index), which keeps the
+// reference's first-index rule (classify with the roles swapped, src/kmeans.cpp:146-150).
+__global__ void km_map_pruned(KmBufs b, const double* __restrict__ box, int ntiles, int* idx)
+{
+  const double* cen = b.cen + (size_t)b.st->final_buf * 3 * b.nmu;
+  int lane = threadIdx.x & 31;
+  long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (k >= b.nmu) return;
+  double c3[3] = {cen[k], cen[b.nmu + k], cen[2 * b.nmu + k]};
+  double u = CUDART_INF;
+  for (int t = lane; t < ntiles; t += 32) {
+    double ub = 0.0;
+    for (int d = 0; d < 3; d++) {
+      double a = c3[d] - box[t * 6 + d], e = c3[d] - box[t * 6 + 3 + d];
+      ub += fmax(a * a, e * e);
+    }
+    u = fmin(u, ub);
+  }
+  for (int off = 16; off; off >>= 1) u = fmin(u, __shfl_xor_sync(0xffffffffu, u, off));
+  double cut = u * (1.0 + 1e-9);
+  double bs = CUDART_INF, bm = CUDART_INF;
+  int bk = 0x7fffffff;
+  for (int t = lane; t < ntiles; t += 32) {
+    double lb = 0.0;
+    for (int d = 0; d < 3; d++) {
+      double v = fmax(0.0, fmax(box[t * 6 + d] - c3[d], c3[d] - box[t * 6 + 3 + d]));
+      lb += v * v;
+    }
+    if (lb > cut) continue;
+    long long p0 = (long long)t * 256, p1 = min((long long)b.ng, p0 + 256);
+    for (long long q = p0; q < p1; q++) {
+      int i = b.perm[q];
+      double d2 = d2_exact(b.gx[i], b.gy[i], b.gz[i], c3[0], c3[1], c3[2]);
+      // Any order: a candidate can win on a smaller sqrt or on an equal sqrt and a smaller
+      // index; equal sqrt values come from squared distances within a few ulps.
+      if (d2 <= bm * (1.0 + 0x1p-50)) {
+        double r = __dsqrt_rn(d2);
+        if (r < bs || (r == bs && i < bk)) { bs = r; bk = i; bm = fmin(bm, d2); }
+      }
+    }
+  }
+  for (int off = 16; off; off >>= 1) {
+    double s2 = __shfl_xor_sync(0xffffffffu, bs, off);
+    int k2 = __shfl_xor_sync(0xffffffffu, bk, off);
+    if (s2 < bs || (s2 == bs && k2 < bk)) { bs = s2; bk = k2; }
+  }
+  if (lane == 0) idx[k] = bk;
+}
+
 // map_to_grid, part 1: each thread owns one centroid and scans one chunk of grid points.
 __global__ void km_map_part(KmBufs b, double* part_s, int* part_i, int nch)
 {
@@ -1103,12 +1181,12 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   const bool mixed = c->precision == THC_PREC_MIXED;
   int nassign = (int)cdiv(ng, kAssignThreads);
   size_t hist_smem = sizeof(int) * nmu;
-  if (hist_smem > 48 * 1024) {
+  if (hist_smem > 16 * 1024) {  // dynamic + static above the 48 KB default needs the opt-in
     THC_CUDA(c, cudaFuncSetAttribute(km_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
     THC_CUDA(c, cudaFuncSetAttribute(km_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
   }
   size_t norm_smem = 3 * (size_t)nmu <= kNormSmem ? sizeof(double) * 3 * nmu : 0;
-  if (norm_smem > 48 * 1024)
+  if (norm_smem > 16 * 1024)  // dynamic + static above the 48 KB default needs the opt-in
     THC_CUDA(c, cudaFuncSetAttribute(km_normdiff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)norm_smem));
   int* hflag = (int*)c->pinned;
   const int kCheckEvery = 8;
@@ -1201,15 +1279,24 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   int* didx = is_device_ptr(out_idx) ? out_idx : (int*)((char*)hist);  // hist is free now
   int* dups = (int*)(part_i + (size_t)nmu * nch);
   THC_CUDA(c, cudaMemsetAsync(dups, 0, sizeof(int), s));
-  dim3 mg((unsigned)nch, (unsigned)cdiv(nmu, 256));
-  km_map_part<<<mg, 256, 0, s>>>(b, part_s, part_i, nch);
-  THC_LAUNCHED(c, "km_map_part");
-  km_map_reduce<<<(int)cdiv(nmu, 256), 256, 0, s>>>(nmu, nch, part_s, part_i, didx);
-  THC_LAUNCHED(c, "km_map_reduce");
+  if (prune) {
+    int ntiles = (int)cdiv(ng, 256);
+    double* box = part_s;   // 6 doubles per tile fit in the partials buffer
+    km_tile_boxes<<<ntiles, 256, 0, s>>>(b, box);
+    THC_LAUNCHED(c, "km_tile_boxes");
+    km_map_pruned<<<(int)cdiv((long long)nmu * 32, 256), 256, 0, s>>>(b, box, ntiles, didx);
+    THC_LAUNCHED(c, "km_map_pruned");
+  } else {
+    dim3 mg((unsigned)nch, (unsigned)cdiv(nmu, 256));
+    km_map_part<<<mg, 256, 0, s>>>(b, part_s, part_i, nch);
+    THC_LAUNCHED(c, "km_map_part");
+    km_map_reduce<<<(int)cdiv(nmu, 256), 256, 0, s>>>(nmu, nch, part_s, part_i, didx);
+    THC_LAUNCHED(c, "km_map_reduce");
+  }
   int np2 = 1;
   while (np2 < nmu) np2 <<= 1;
   size_t sort_smem = sizeof(int) * np2;
-  if (sort_smem > 48 * 1024)
+  if (sort_smem > 16 * 1024)  // dynamic + static above the 48 KB default needs the opt-in
     THC_CUDA(c, cudaFuncSetAttribute(km_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem));
   km_sort<<<1, 1024, sort_smem, s>>>(didx, nmu, np2, dups);
   THC_LAUNCHED(c, "km_sort");

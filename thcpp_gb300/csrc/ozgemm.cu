@@ -237,8 +237,36 @@ __global__ void oz_reduce_kernel(OzArgs g)
     ((double*)g.C)[m * g.ldc + n] = v;
 }
 
-// One warp per row: exponent from the row maximum, then the slices (FP64 input; every
-// step -- the power-of-two scaling, rint, the subtraction and the *128 -- is exact).
+// One warp per row: exponent from the row maximum, then the slices of an FP64 input in
+// integer arithmetic.  With e the row exponent (|x| < 2^e), X = round(x 2^{7 ns - e}) is an
+// integer below 2^{7 ns} built from the IEEE bits (round half to even at the cut), and the
+// slices are its signed base-128 digits S_i = round(R_i / 2^{7(ns-1-i)}), R_{i+1} = R_i -
+// S_i 2^{7(ns-1-i)}, so |S_0| <= 128 and |S_i| <= 64.  Rows scaled by `scale` (optional,
+// indexed c >> shift) are multiplied in FP64 first.
+__device__ __forceinline__ long long fixed_point(double x, int shift_total)
+{
+  // round(|x| * 2^shift_total) with the sign of x; |x| * 2^shift_total < 2^62 assumed.
+  unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  int E = (int)((bits >> 52) & 0x7ff);
+  if (E == 0) return 0;                              // zero or subnormal: below every slice
+  unsigned long long m = (bits & 0xfffffffffffffULL) | (1ULL << 52);
+  int s = E - 1075 + shift_total;
+  unsigned long long X;
+  if (s >= 0) {
+    X = m << s;
+  } else if (s <= -64) {
+    X = 0;
+  } else {
+    int r = -s;
+    unsigned long long q = m >> r;
+    unsigned long long rem = m & ((1ULL << r) - 1);
+    unsigned long long half = 1ULL << (r - 1);
+    if (rem > half || (rem == half && (q & 1))) q++;
+    X = q;
+  }
+  return (bits >> 63) ? -(long long)X : (long long)X;
+}
+
 __global__ void slice_rows_kernel(const double* __restrict__ X, long long rows, long long cols,
                                   long long ldx, long long sc, const double* __restrict__ scale,
                                   int shift, int ns, __nv_bfloat16* out, long long ldo,
@@ -252,19 +280,30 @@ __global__ void slice_rows_kernel(const double* __restrict__ X, long long rows, 
     if (scale) v *= scale[cidx >> shift];
     return v;
   };
-  double mx = 0.0;
+  // Row maximum of |x| through the bit patterns (monotone for non-negative doubles).
+  unsigned long long mx = 0;
   if (r < rows)
-    for (long long cc = lane; cc < cols; cc += 32) mx = fmax(mx, fabs(val(cc)));
-  for (int off = 16; off; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    for (long long cc = lane; cc < cols; cc += 32) {
+      unsigned long long a = (unsigned long long)__double_as_longlong(val(cc)) & 0x7fffffffffffffffULL;
+      mx = a > mx ? a : mx;
+    }
+  for (int off = 16; off; off >>= 1) {
+    unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
+    mx = o > mx ? o : mx;
+  }
+  // frexp exponent of the maximum: |x| < 2^e for every entry of the row.
   int e = 0;
-  if (mx > 0.0) frexp(mx, &e);
+  int Em = (int)(mx >> 52);
+  if (Em > 0) e = Em - 1022;
   if (lane == 0) exps[r] = e;
+  const int total = 7 * ns - e;
   for (long long cc = lane; cc < ldo; cc += 32) {
-    double x = (r < rows && cc < cols) ? ldexp(val(cc), 7 - e) : 0.0;
-    for (int s = 0; s < ns; s++) {
-      double q = rint(x);
-      out[s * sstride + r * ldo + cc] = __double2bfloat16(q);
-      x = (x - q) * 128.0;
+    long long R = (r < rows && cc < cols && Em > 0) ? fixed_point(val(cc), total) : 0;
+    for (int s2 = 0; s2 < ns; s2++) {
+      int sh = 7 * (ns - 1 - s2);
+      long long S = sh ? ((R + (1LL << (sh - 1))) >> sh) : R;
+      R -= S << sh;
+      out[s2 * sstride + r * ldo + cc] = __float2bfloat16_rn((float)S);
     }
   }
 }
