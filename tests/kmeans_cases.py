@@ -49,3 +49,20 @@ def exact_tie_grid(n=6):
     g = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
     rho = 1.0 + 0.01 * np.arange(g.shape[0]) % 7
     return g, rho
+
+
+def rounding_stress_grid(seed: int = 11):
+    """A lattice whose centroid sums round on nearly every step, with exact halves.
+
+    Coordinates are multiples of 2^-4 on both sides of zero and the weights are
+    1 + m 2^-40: products carry bits down to 2^-44 while sums of ~10^3 terms round at
+    2^-42, so a quarter of the additions are exact ties, and the coordinate sums change sign
+    and binade.  Pins the warp-parallel sequential summation against the plain loop.
+    """
+    rng = np.random.default_rng(seed)
+    n = 16
+    i, j, k = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    grid = np.stack([(i - 7.5) * 0.5, (j - 8) * 0.5625, (k - 6) * 0.4375], -1).reshape(-1, 3)
+    grid = grid + rng.integers(-3, 4, size=grid.shape) * 2.0 ** -4
+    rho = 1.0 + rng.integers(0, 2 ** 40, size=grid.shape[0]).astype(np.float64) * 2.0 ** -40
+    return np.ascontiguousarray(grid), rho

@@ -50,6 +50,17 @@ def test_kmeans_exact_ties(request, prec):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_kmeans_rounding_stress(request, prec):
+    g, rho = kmeans_cases.rounding_stress_grid()
+    init = oracle.initial_indices(g.shape[0], 32, 3)
+    ref = oracle.kmeans(g, rho, 32, init, 30, 1e-14)
+    idx, st, status = _ctx(request, prec).kmeans(g, rho, 32, init, 30, 1e-14)
+    assert status == 0 and ref.status == 0
+    assert np.array_equal(idx, ref.idx) and st.iterations == ref.iters
+    assert st.final_diff == ref.diff
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_kmeans_empty_cluster(request, prec):
     grid = np.array([[0.0, 0, 0], [1.0, 0, 0], [5.0, 0, 0]])
     rho = np.array([1.0, 1.0, 0.0])

@@ -28,7 +28,7 @@ enum Slot : int {
   WS_KM_HIST,       // nmu x nblocks ints
   WS_KM_TOTAL,      // nmu ints (counts) + nmu ints (starts)
   WS_KM_MEMBER,     // ng ints
-  WS_KM_TERMS,      // 3 x nmu doubles
+  WS_KM_TERMS,      // 4 x nmu doubles
   WS_KM_RECHECK,    // ng ints
   WS_KM_STATE,
   WS_KM_PART,       // map_to_grid partials
@@ -59,6 +59,7 @@ enum Slot : int {
   WS_DINV,          // inverted diagonal blocks + L^{-1} + scratch of the inverse
   WS_ROWMAX,        // per-row maxima for slicing
   WS_ZTMP,          // FP64 zeta of the rank-deficient fallback
+  WS_DPART,         // split-K partials chosen inside dgemm
   WS_NSLOTS
 };
 

@@ -2,11 +2,12 @@
 // solves.  These carry the all-FP64 path, which replaces the reference's ScaLAPACK
 // calls one for one:
 //   pzgemm 'C','N'  (P = Phi_mu^H Phi, src/interpolating_vectors.cpp:117)  -> dgemm + square
-//   pzgels 'N'      (least squares C X = Z, :416)                           -> potrf + trsm
+//   pzgels 'N'      (least squares C X = Z, :416)             -> potrf_inv + chol_inverse + dgemm
 //   pzherk 'L','C'  (M = zeta_hat^H zeta_hat, :278)                         -> dgemm lower
-//   pzpotrf 'L'     (Luv, :289)                                             -> potrf
-// GB300 runs FP64 at a small fraction of its FP32 rate, so these kernels are bound by
-// the FP64 pipe; a 64x64x16 register-blocked tile keeps that pipe fed.
+//   pzpotrf 'L'     (Luv, :289)                                             -> potrf_inv
+// GB300 runs FP64 at a small fraction of its FP32 rate (about two FMA lanes per clock per
+// SM), so these kernels are bound by the FP64 pipe, and a GEMM must spread over all SMs:
+// dgemm picks 64, 32 or 16 tiles and a split of K from the problem shape.
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
@@ -19,20 +20,23 @@ namespace thc {
 
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 16;
+constexpr int BK = 16;
 
 // C[m, n] = epilogue(sum_k A(m, k) * dk[k] * B(k, n)); AK / BK select which operand
-// index is unit-stride so that the shared-memory loads stay coalesced.
-template <bool AK, bool BK_>
+// index is unit-stride so that the shared-memory loads stay coalesced.  T x T tile per
+// CTA of 256 threads (16 x 16), (T/16)^2 outputs per thread.
+template <bool AK, bool BK_, int T>
 __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
 {
+  constexpr int R = T / 16;
+  constexpr int LOADS = BK * T / 256;
   if (g.skip_flag && *g.skip_flag) return;
-  long long m0 = (long long)blockIdx.y * BM, n0 = (long long)blockIdx.x * BN;
-  if (g.lower_only && n0 > m0 + BM - 1) return;
-  __shared__ double As[BK][BM + 1];
-  __shared__ double Bs[BK][BN + 1];
+  long long m0 = (long long)blockIdx.y * T, n0 = (long long)blockIdx.x * T;
+  if (g.lower_only && n0 > m0 + T - 1) return;
+  __shared__ double As[BK][T + 1];
+  __shared__ double Bs[BK][T + 1];
   int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  double acc[4][4] = {};
+  double acc[R][R] = {};
   int kbeg = 0, kend = g.K;
   if (g.ksplit > 1) {
     int kc = ((g.K + g.ksplit - 1) / g.ksplit + BK - 1) / BK * BK;
@@ -40,12 +44,11 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
     kend = min(g.K, kbeg + kc);
   }
   for (int k0 = kbeg; k0 < kend; k0 += BK) {
-    // 1024 elements of each tile, 4 per thread.
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
+    for (int r = 0; r < LOADS; r++) {
       int e = threadIdx.x + 256 * r;
       int mm, kk;
-      if (AK) { mm = e / BK; kk = e % BK; } else { kk = e / BM; mm = e % BM; }
+      if (AK) { mm = e / BK; kk = e % BK; } else { kk = e / T; mm = e % T; }
       long long m = m0 + mm;
       int k = k0 + kk;
       double av = 0.0;
@@ -55,7 +58,7 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
       }
       As[kk][mm] = av;
       int nn, kb;
-      if (BK_) { nn = e / BK; kb = e % BK; } else { kb = e / BN; nn = e % BN; }
+      if (BK_) { nn = e / BK; kb = e % BK; } else { kb = e / T; nn = e % T; }
       long long n = n0 + nn;
       int kq = k0 + kb;
       Bs[kb][nn] = (n < g.N && kq < kend) ? g.B[n * g.sbn + (long long)kq * g.sbk] : 0.0;
@@ -63,24 +66,24 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < BK; kk++) {
-      double a[4], b[4];
+      double a[R], b[R];
 #pragma unroll
-      for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 16 * i];
+      for (int i = 0; i < R; i++) a[i] = As[kk][ty + 16 * i];
 #pragma unroll
-      for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 16 * j];
+      for (int j = 0; j < R; j++) b[j] = Bs[kk][tx + 16 * j];
 #pragma unroll
-      for (int i = 0; i < 4; i++)
+      for (int i = 0; i < R; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] = __fma_rn(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < R; j++) acc[i][j] = __fma_rn(a[i], b[j], acc[i][j]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
+  for (int i = 0; i < R; i++) {
     long long m = m0 + ty + 16 * i;
     if (m >= g.M) continue;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < R; j++) {
       long long n = n0 + tx + 16 * j;
       if (n >= g.N) continue;
       if (g.lower_only && n > m) continue;
@@ -118,58 +121,28 @@ __global__ void dgemm_reduce(GemmArgs g)
 
 constexpr int NB = 64;
 
-// Factor the diagonal block at (k0, k0).  Pivots at or below `thr` stop the
-// factorisation: info = global 1-based index, flag set.
-__global__ void potrf_diag(double* A, long long ld, int n, int k0, const double* thr_p,
-                           CholStatus* cs)
+// 1/sqrt(d) for a positive normal d: FP32 seed, then two Newton-Raphson steps for the
+// reciprocal square root, y <- y (3 - d y^2) / 2, each of which doubles the correct bits
+// (24 -> 48 -> full FP64, within a few ulp).  A handful of dependent FP64 operations instead
+// of a square root followed by a division: the pivot is on the critical path of every
+// Cholesky step, and FP64 latency is long on this part.
+__device__ __forceinline__ double rsqrt_newton(double d)
 {
-  if (cs->flag) return;
-  double thr = thr_p ? *thr_p : 0.0;
-  __shared__ double a[NB][NB + 1];
-  __shared__ int bad;
-  int nb = min(NB, n - k0);
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    int r = e / nb, c = e % nb;
-    a[r][c] = A[(long long)(k0 + r) * ld + k0 + c];
-  }
-  if (threadIdx.x == 0) bad = 0;
-  __syncthreads();
-  for (int j = 0; j < nb; j++) {
-    if (threadIdx.x == 0) {
-      double d = a[j][j];
-      if (!(d > thr)) {
-        bad = 1;
-        cs->flag = 1;
-        cs->info = k0 + j + 1;
-      } else {
-        double r = sqrt(d);
-        a[j][j] = r;
-        double p = d;
-        if (p < cs->min_piv) cs->min_piv = p;
-        if (p > cs->max_piv) cs->max_piv = p;
-      }
-    }
-    __syncthreads();
-    if (bad) break;
-    double r = a[j][j];
-    for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) a[i][j] /= r;
-    __syncthreads();
-    for (int e = threadIdx.x; e < (nb - j - 1) * (nb - j - 1); e += blockDim.x) {
-      int i = j + 1 + e / (nb - j - 1), c = j + 1 + e % (nb - j - 1);
-      if (c <= i) a[i][c] = __fma_rn(-a[i][j], a[c][j], a[i][c]);
-    }
-    __syncthreads();
-  }
-  if (bad) return;
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    int r = e / nb, c = e % nb;
-    A[(long long)(k0 + r) * ld + k0 + c] = c <= r ? a[r][c] : 0.0;
-  }
+  if (!(d > 1e-30 && d < 1e30)) return 1.0 / sqrt(d);
+  double y = (double)rsqrtf((float)d);
+  double h = d * y;
+  y = y * (1.5 - 0.5 * h * y);
+  h = d * y;
+  y = y * (1.5 - 0.5 * h * y);
+  return y;
 }
 
 // Factor the diagonal block at (k0, k0) and invert its triangle: writes L_kk into A
 // (upper part zeroed) and L_kk^{-1} into dinv (nb x nb, row-major, zero above the diagonal).
 // Pivots at or below thr stop the factorisation (info = global 1-based index).
+// The inverse V is eliminated alongside the factor: at step j row j of V is scaled by
+// 1/L_jj and subtracted from the rows below (L V = I by forward substitution), so both
+// run on all threads with one pivot chain.
 __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, int n, int k0,
                                                       const double* thr_p, CholStatus* cs,
                                                       double* dinv)
@@ -186,9 +159,12 @@ __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, i
   for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
     int r = e / NB, c = e % NB;
     a[r][c] = (r < nb && c < nb) ? A[(long long)(k0 + r) * ld + k0 + c] : (r == c ? 1.0 : 0.0);
-    v[r][c] = 0.0;
+    v[r][c] = r == c ? 1.0 : 0.0;
   }
   if (threadIdx.x == 0) bad = 0;
+  // Pivot extremes stay in registers of thread 0 (no global traffic on the pivot chain).
+  double pmin = 0.0, pmax = 0.0;
+  if (threadIdx.x == 0) { pmin = cs->min_piv; pmax = cs->max_piv; }
   __syncthreads();
   for (int j = 0; j < nb; j++) {
     if (threadIdx.x == 0) {
@@ -197,111 +173,39 @@ __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, i
         bad = 1;
         cs->flag = 1;
         cs->info = k0 + j + 1;
+        cs->min_piv = pmin;
+        cs->max_piv = pmax;
       } else {
-        double r = sqrt(d);
-        a[j][j] = r;
-        rinv = 1.0 / r;
-        if (d < cs->min_piv) cs->min_piv = d;
-        if (d > cs->max_piv) cs->max_piv = d;
+        double y = rsqrt_newton(d);
+        a[j][j] = d * y;
+        rinv = y;
+        pmin = fmin(pmin, d);
+        pmax = fmax(pmax, d);
       }
     }
     __syncthreads();
     if (bad) return;
-    double ri = rinv;
+    const double ri = rinv;
     for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) a[i][j] *= ri;
+    for (int c = threadIdx.x; c <= j; c += blockDim.x) v[j][c] *= ri;
     __syncthreads();
-    // trailing lower update a[i][c] -= a[i][j] a[c][j], j < c <= i
-    for (int i = j + 1 + ty; i < nb; i += 16)
-      for (int c = j + 1 + tx; c <= i; c += 16) a[i][c] = __fma_rn(-a[i][j], a[c][j], a[i][c]);
-    __syncthreads();
-  }
-  // Triangular inverse by columns: for column c, v[c][c] = 1/a[c][c] and
-  // v[i][c] = -(sum_{k=c}^{i-1} a[i][k] v[k][c]) / a[i][i], i > c (one thread per column).
-  for (int c = threadIdx.x; c < nb; c += blockDim.x) {
-    v[c][c] = 1.0 / a[c][c];
-    for (int i = c + 1; i < nb; i++) {
-      double sacc = 0.0;
-      for (int k = c; k < i; k++) sacc = __fma_rn(a[i][k], v[k][c], sacc);
-      v[i][c] = -sacc / a[i][i];
+    // rows i > j: a[i][c] -= a[i][j] a[c][j] (j < c <= i) and v[i][c] -= a[i][j] v[j][c]
+    // (c <= j); together the columns 0..i of row i.
+    for (int i = j + 1 + ty; i < nb; i += 16) {
+      const double lij = a[i][j];
+      for (int c = tx; c <= i; c += 16) {
+        if (c <= j) v[i][c] = __fma_rn(-lij, v[j][c], v[i][c]);
+        else a[i][c] = __fma_rn(-lij, a[c][j], a[i][c]);
+      }
     }
+    __syncthreads();
   }
-  __syncthreads();
+  if (threadIdx.x == 0) { cs->min_piv = pmin; cs->max_piv = pmax; }
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     int r = e / nb, c = e % nb;
     A[(long long)(k0 + r) * ld + k0 + c] = c <= r ? a[r][c] : 0.0;
     dinv[(long long)r * nb + c] = c <= r ? v[r][c] : 0.0;
   }
-}
-
-// Rows below the diagonal block: x L_kk^T = a, one thread per row.
-__global__ void potrf_panel(double* A, long long ld, int n, int k0, CholStatus* cs)
-{
-  if (cs->flag) return;
-  __shared__ double l[NB][NB + 1];
-  int nb = min(NB, n - k0);
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    int r = e / nb, c = e % nb;
-    l[r][c] = A[(long long)(k0 + r) * ld + k0 + c];
-  }
-  __syncthreads();
-  long long row = (long long)k0 + nb + blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (row >= n) return;
-  double x[NB];
-  double* ar = A + row * ld + k0;
-#pragma unroll 1
-  for (int j = 0; j < nb; j++) {
-    double s = ar[j];
-    for (int t = 0; t < j; t++) s = __fma_rn(-x[t], l[j][t], s);
-    x[j] = s / l[j][j];
-  }
-  for (int j = 0; j < nb; j++) ar[j] = x[j];
-}
-
-// Forward substitution on a diagonal block: B[k0..k0+nb, :] = L_kk^{-1} B[...], one thread
-// per right-hand-side column.
-__global__ void trsm_diag_fwd(const double* L, long long ld, int n, int k0, double* B,
-                              long long ldb, long long nrhs, const CholStatus* cs)
-{
-  if (cs && cs->flag) return;
-  __shared__ double l[NB][NB + 1];
-  int nb = min(NB, n - k0);
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    int r = e / nb, c = e % nb;
-    l[r][c] = L[(long long)(k0 + r) * ld + k0 + c];
-  }
-  __syncthreads();
-  long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (col >= nrhs) return;
-  double y[NB];
-  for (int j = 0; j < nb; j++) {
-    double s = B[(long long)(k0 + j) * ldb + col];
-    for (int t = 0; t < j; t++) s = __fma_rn(-l[j][t], y[t], s);
-    y[j] = s / l[j][j];
-  }
-  for (int j = 0; j < nb; j++) B[(long long)(k0 + j) * ldb + col] = y[j];
-}
-
-// Backward substitution with L_kk^T on a diagonal block.
-__global__ void trsm_diag_bwd(const double* L, long long ld, int n, int k0, double* B,
-                              long long ldb, long long nrhs, const CholStatus* cs)
-{
-  if (cs && cs->flag) return;
-  __shared__ double l[NB][NB + 1];
-  int nb = min(NB, n - k0);
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    int r = e / nb, c = e % nb;
-    l[r][c] = L[(long long)(k0 + r) * ld + k0 + c];
-  }
-  __syncthreads();
-  long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (col >= nrhs) return;
-  double x[NB];
-  for (int j = nb - 1; j >= 0; j--) {
-    double s = B[(long long)(k0 + j) * ldb + col];
-    for (int t = j + 1; t < nb; t++) s = __fma_rn(-l[t][j], x[t], s);
-    x[j] = s / l[j][j];
-  }
-  for (int j = 0; j < nb; j++) B[(long long)(k0 + j) * ldb + col] = x[j];
 }
 
 __global__ void set_identity_k(double* A, long long ld, int n)
@@ -393,16 +297,43 @@ __global__ void zpotrf_small_k(double* A, int n, const double* thr_p, CholStatus
 
 }  // namespace
 
-int dgemm(Ctx* c, const GemmArgs& g)
+template <int T>
+static void launch_dgemm(const GemmArgs& g, cudaStream_t s)
 {
-  if (g.M <= 0 || g.N <= 0) return THC_OK;
-  dim3 grid((unsigned)cdiv(g.N, BN), (unsigned)cdiv(g.M, BM), (unsigned)std::max(1, g.ksplit));
+  dim3 grid((unsigned)cdiv(g.N, T), (unsigned)cdiv(g.M, T), (unsigned)std::max(1, g.ksplit));
   bool ak = g.sak == 1, bk = g.sbk == 1;
+  if (ak && bk) dgemm_kernel<true, true, T><<<grid, 256, 0, s>>>(g);
+  else if (ak && !bk) dgemm_kernel<true, false, T><<<grid, 256, 0, s>>>(g);
+  else if (!ak && bk) dgemm_kernel<false, true, T><<<grid, 256, 0, s>>>(g);
+  else dgemm_kernel<false, false, T><<<grid, 256, 0, s>>>(g);
+}
+
+int dgemm(Ctx* c, const GemmArgs& g_in)
+{
+  if (g_in.M <= 0 || g_in.N <= 0) return THC_OK;
+  GemmArgs g = g_in;
+  if (g.ksplit <= 1 && !g.part) {
+    // Tile and split-K so that the grid covers the SMs about twice.
+    const long long want = 2LL * 152;
+    auto tiles = [&](int t) {
+      long long mt = cdiv(g.M, t), nt = cdiv(g.N, t);
+      return g.lower_only ? (mt * nt + mt) / 2 : mt * nt;
+    };
+    g.tile = tiles(64) >= want / 2 ? 64 : (tiles(32) >= want / 2 ? 32 : 16);
+    long long split = std::min<long long>(cdiv(want, tiles(g.tile)), std::max(1, g.K / 32));
+    if (g.aliased) split = std::max<long long>(split, 2);
+    g.ksplit = (int)std::max<long long>(1, std::min<long long>(split, cdiv(g.K, BK)));
+    if (g.ksplit > 1) {
+      g.part = (double*)ws_get(c, WS_DPART, sizeof(double) * g.ksplit * g.M * g.N);
+      if (!g.part) return set_error(c, THC_ERR_NOMEM, "dgemm: split-K partials");
+    }
+  } else if (g.aliased && g.ksplit <= 1) {
+    return set_error(c, THC_ERR_ARG, "dgemm: aliased operands need split-K partials");
+  }
   ProfScope prof(c, "dgemm");
-  if (ak && bk) dgemm_kernel<true, true><<<grid, 256, 0, c->stream>>>(g);
-  else if (ak && !bk) dgemm_kernel<true, false><<<grid, 256, 0, c->stream>>>(g);
-  else if (!ak && bk) dgemm_kernel<false, true><<<grid, 256, 0, c->stream>>>(g);
-  else dgemm_kernel<false, false><<<grid, 256, 0, c->stream>>>(g);
+  if (g.tile == 16) launch_dgemm<16>(g, c->stream);
+  else if (g.tile == 32) launch_dgemm<32>(g, c->stream);
+  else launch_dgemm<64>(g, c->stream);
   THC_LAUNCHED(c, "dgemm");
   if (g.ksplit > 1) {
     dgemm_reduce<<<(unsigned)cdiv(g.M * g.N, 256), 256, 0, c->stream>>>(g);
@@ -434,6 +365,7 @@ int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholSta
       g.B = di; g.sbn = nb; g.sbk = 1;
       g.C = A + (long long)(k0 + nb) * ld + k0; g.ldc = ld;
       g.skip_flag = &cs->flag;
+      g.aliased = 1;
       int st = dgemm(c, g);
       if (st) return st;
     }
@@ -491,73 +423,6 @@ int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* din
   g.C = Cinv; g.ldc = n;
   g.skip_flag = cs ? &cs->flag : nullptr;
   return dgemm(c, g);
-}
-
-int potrf(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs)
-{
-  cudaStream_t s = c->stream;
-  for (int k0 = 0; k0 < n; k0 += NB) {
-    potrf_diag<<<1, 256, 0, s>>>(A, ld, n, k0, thr, cs);
-    THC_LAUNCHED(c, "potrf_diag");
-    int nb = std::min(NB, n - k0);
-    int rest = n - k0 - nb;
-    if (rest <= 0) break;
-    potrf_panel<<<(int)cdiv(rest, 128), 128, 0, s>>>(A, ld, n, k0, cs);
-    THC_LAUNCHED(c, "potrf_panel");
-    GemmArgs g{};
-    g.M = rest; g.N = rest; g.K = nb;
-    g.A = A + (long long)(k0 + nb) * ld + k0; g.sam = ld; g.sak = 1;
-    g.B = A + (long long)(k0 + nb) * ld + k0; g.sbn = ld; g.sbk = 1;
-    g.C = A + (long long)(k0 + nb) * ld + k0 + nb; g.ldc = ld;
-    g.alpha = -1.0; g.beta = 1.0; g.lower_only = 1; g.mode = GEMM_STORE;
-    g.skip_flag = &cs->flag;
-    int st = dgemm(c, g);
-    if (st) return st;
-  }
-  return THC_OK;
-}
-
-// B := L^{-T} L^{-1} B (solve (L L^T) X = B), B is n x nrhs row-major.
-int potrs(Ctx* c, const double* L, long long ld, int n, double* B, long long ldb,
-          long long nrhs, const CholStatus* cs)
-{
-  cudaStream_t s = c->stream;
-  int nthr = 128;
-  int nblk = (int)cdiv(nrhs, nthr);
-  for (int k0 = 0; k0 < n; k0 += NB) {
-    trsm_diag_fwd<<<nblk, nthr, 0, s>>>(L, ld, n, k0, B, ldb, nrhs, cs);
-    THC_LAUNCHED(c, "trsm_diag_fwd");
-    int nb = std::min(NB, n - k0);
-    int rest = n - k0 - nb;
-    if (rest <= 0) break;
-    GemmArgs g{};
-    g.M = rest; g.N = nrhs; g.K = nb;
-    g.A = L + (long long)(k0 + nb) * ld + k0; g.sam = ld; g.sak = 1;   // L rows below
-    g.B = B + (long long)k0 * ldb; g.sbn = 1; g.sbk = ldb;              // B(k,n) = B[k*ldb+n]
-    g.C = B + (long long)(k0 + nb) * ldb; g.ldc = ldb;
-    g.alpha = -1.0; g.beta = 1.0; g.mode = GEMM_STORE;
-    g.skip_flag = cs ? &cs->flag : nullptr;
-    int st = dgemm(c, g);
-    if (st) return st;
-  }
-  int nblocks = (int)cdiv(n, NB);
-  for (int kb = nblocks - 1; kb >= 0; kb--) {
-    int k0 = kb * NB;
-    trsm_diag_bwd<<<nblk, nthr, 0, s>>>(L, ld, n, k0, B, ldb, nrhs, cs);
-    THC_LAUNCHED(c, "trsm_diag_bwd");
-    if (k0 == 0) break;
-    int nb = std::min(NB, n - k0);
-    GemmArgs g{};
-    g.M = k0; g.N = nrhs; g.K = nb;
-    g.A = L + (long long)k0 * ld; g.sam = 1; g.sak = ld;               // A(m,k) = L[k0+k][m]
-    g.B = B + (long long)k0 * ldb; g.sbn = 1; g.sbk = ldb;
-    g.C = B; g.ldc = ldb;
-    g.alpha = -1.0; g.beta = 1.0; g.mode = GEMM_STORE;
-    g.skip_flag = cs ? &cs->flag : nullptr;
-    int st = dgemm(c, g);
-    if (st) return st;
-  }
-  return THC_OK;
 }
 
 int set_identity(Ctx* c, double* A, long long ld, int n)

@@ -27,6 +27,8 @@ struct GemmArgs {
   const int* skip_flag = nullptr;   // if non-null and set, the kernel does nothing
   int ksplit = 1;                    // > 1: K is split over blockIdx.z into FP64 partials
   double* part = nullptr;            // ksplit x M x N partial buffer (row-major, ld = N)
+  int aliased = 0;                   // C overlaps A or B: products go through partials
+  int tile = 64;                     // CTA tile edge (64, 32 or 16; chosen by dgemm)
 };
 
 struct CholStatus {
@@ -36,8 +38,10 @@ struct CholStatus {
   double max_piv;
 };
 
+// With ksplit <= 1 and no part buffer, dgemm picks the tile edge and a split of K itself so
+// that the grid covers the GPU (the FP64 pipe of one SM is narrow, so small GEMMs must spread
+// over many SMs); split partials are summed in split order (deterministic).
 int dgemm(Ctx* c, const GemmArgs& g);
-int potrf(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs);
 // Cholesky with GEMM panels; dinv receives the inverted 64 x 64 diagonal blocks
 // (ceil(n/64) x 64 x 64 doubles).
 int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs,
@@ -45,8 +49,6 @@ int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholSta
 // Cinv = (L L^T)^{-1} via X = L^{-1}; X (n x ld) and T (64 x n) are scratch.
 int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* dinv, double* X,
                  double* T, double* Cinv, const CholStatus* cs);
-int potrs(Ctx* c, const double* L, long long ld, int n, double* B, long long ldb,
-          long long nrhs, const CholStatus* cs);
 int set_identity(Ctx* c, double* A, long long ld, int n);
 int add_diag_shift(Ctx* c, double* A, long long ld, int n, double rel, double* shift_out);
 int diag_mean(Ctx* c, const double* A, long long ld, int n, double* out);

@@ -24,8 +24,11 @@
 //     first index among equal sqrt values exactly as std::min_element does;
 //   * per-cluster sums run in ascending grid order through a stable counting sort of
 //     the labels (block histograms -> per-cluster scans -> stable warp scatter), then
-//     one thread per cluster accumulates its members sequentially;
-//   * the normed difference is summed by one thread in index order.
+//     each cluster's members are accumulated in that order by warp_seqsum, which
+//     reproduces the sequential loop's rounding exactly (seqsum.cuh);
+//   * the normed difference that is reported is the sequential sum in index order (again
+//     warp_seqsum); the per-iteration convergence test uses a fixed-order approximation
+//     and falls back to the exact sum whenever the two could decide differently.
 // Mixed precision: an FP32 pass keeps the best and second-best squared distance and
 // accepts its argmin only when the gap exceeds a proven bound on the FP32 error;
 // every other point is queued and resolved by a warp-parallel FP64 scan with the exact
@@ -38,6 +41,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "seqsum.cuh"
 
 namespace thc {
 
@@ -47,7 +51,6 @@ constexpr int kAssignThreads = 256;
 constexpr int kTile = 1024;       // centroids staged per shared-memory tile
 constexpr int kBP = 512;          // points per histogram / scatter block
 constexpr int kMapChunk = 1024;   // grid points per map_to_grid block
-constexpr int kNormSmem = 6144;   // terms of the normed difference staged in shared memory
 
 struct KmState {
   int iter;
@@ -73,7 +76,9 @@ struct KmState {
   double blo[3], binv[3];                // bin origin and inverse bin width
   double slack32;                        // absolute slack of the FP32 candidate bound
   int diff_exact;                        // st->diff came from the sequential sum
-  int pad3;
+  int ticket;                            // blocks of km_sums finished this iteration
+  int scan_ticket;                       // blocks of km_colscan finished this iteration
+  int pad4;
 };
 
 struct KmBufs {
@@ -664,39 +669,15 @@ __global__ void km_hist(KmBufs b)
     if (sh[k]) b.hist[(size_t)k * b.nb + blockIdx.x] = sh[k];
 }
 
-// One warp per cluster: exclusive scan of its block counts (in place) and its total.
-__global__ void km_colscan(KmBufs b)
+// Exclusive scan of the cluster totals into cluster start offsets (one block).
+__device__ void kscan_block(KmBufs& b)
 {
-  if (b.st->done) return;
-  int lane = threadIdx.x & 31;
-  long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  if (k >= b.nmu) return;
-  int* h = b.hist + (size_t)k * b.nb;
-  int carry = 0;
-  for (int c = 0; c < b.nb; c += 32) {
-    int j = c + lane;
-    int v = j < b.nb ? h[j] : 0;
-    int x = v;
-    for (int off = 1; off < 32; off <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, x, off);
-      if (lane >= off) x += y;
-    }
-    if (j < b.nb) h[j] = carry + x - v;
-    carry += __shfl_sync(0xffffffffu, x, 31);
-  }
-  if (lane == 0) b.total[k] = carry;
-}
-
-// Single block: exclusive scan of the cluster totals into cluster start offsets.
-__global__ void km_kscan(KmBufs b)
-{
-  if (b.st->done) return;
   __shared__ int warp_sums[32];
   int n = b.nmu;
   int per = (n + blockDim.x - 1) / blockDim.x;
   int lo = threadIdx.x * per, hi = min(n, lo + per);
   int s = 0;
-  for (int k = lo; k < hi; k++) s += b.total[k];
+  for (int k = lo; k < hi; k++) s += __ldcg(b.total + k);
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int x = s;
   for (int off = 1; off < 32; off <<= 1) {
@@ -718,103 +699,86 @@ __global__ void km_kscan(KmBufs b)
   int run = warp_sums[wid] + x - s;
   for (int k = lo; k < hi; k++) {
     b.start[k] = run;
-    run += b.total[k];
+    run += __ldcg(b.total + k);
   }
 }
 
-// Stable scatter of point indices into per-cluster member lists.  Warp 0 walks the
-// block's points in ascending order, 32 at a time; lanes with equal labels take ranks
-// from __match_any_sync so each cluster keeps ascending grid order.
-__global__ void km_scatter(KmBufs b)
+// One warp per cluster: exclusive scan of its block counts (in place) and its total.  The
+// last block to finish (a ticket in the state) turns the totals into start offsets.
+__global__ void __launch_bounds__(256) km_colscan(KmBufs b)
+{
+  KmState* st = b.st;
+  if (st->done) return;
+  __shared__ int last;
+  int lane = threadIdx.x & 31;
+  long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (k < b.nmu) {
+    int* h = b.hist + (size_t)k * b.nb;
+    int carry = 0;
+    for (int c = 0; c < b.nb; c += 32) {
+      int j = c + lane;
+      int v = j < b.nb ? h[j] : 0;
+      int x = v;
+      for (int off = 1; off < 32; off <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+      }
+      if (j < b.nb) h[j] = carry + x - v;
+      carry += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (lane == 0) b.total[k] = carry;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&st->scan_ticket, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  kscan_block(b);
+  if (threadIdx.x == 0) st->scan_ticket = 0;
+}
+
+// Stable scatter of point indices into per-cluster member lists.  The block's labels and
+// every cluster's output offset are staged in shared memory by all threads; then warp 0
+// walks the points in ascending order, 32 at a time, and lanes with equal labels take
+// ranks from __match_any_sync, so each cluster keeps ascending grid order.
+__global__ void __launch_bounds__(256) km_scatter(KmBufs b)
 {
   if (b.st->done) return;
-  int it = b.st->iter;
-  extern __shared__ int base[];
-  for (int k = threadIdx.x; k < b.nmu; k += blockDim.x) base[k] = -1;
+  const int it = b.st->iter;
+  extern __shared__ int base[];          // nmu offsets
+  __shared__ int slab[kBP];
+  const int* lab = b.labels + (size_t)(it & 1) * b.ng;
+  const long long blk = (long long)blockIdx.x * kBP;
+  for (int k = threadIdx.x; k < b.nmu; k += blockDim.x)
+    base[k] = b.start[k] + b.hist[(size_t)k * b.nb + blockIdx.x];
+  for (int t = threadIdx.x; t < kBP; t += blockDim.x) {
+    long long i = blk + t;
+    int l = i < b.ng ? lab[i] : -1;
+    if (i < b.ng && (unsigned)l >= (unsigned)b.nmu) l = 0;  // flagged by km_hist
+    slab[t] = l;
+  }
   __syncthreads();
   if (threadIdx.x >= 32) return;
-  int lane = threadIdx.x;
-  const int* lab = b.labels + (size_t)(it & 1) * b.ng;
-  long long blk = (long long)blockIdx.x * kBP;
-  unsigned lt = (1u << lane) - 1u;
+  const int lane = threadIdx.x;
+  const unsigned lt = (1u << lane) - 1u;
   for (int c = 0; c < kBP; c += 32) {
-    long long i = blk + c + lane;
-    bool valid = i < b.ng;
-    unsigned active = __ballot_sync(0xffffffffu, valid);
+    const int l = slab[c + lane];
+    const bool valid = l >= 0;
+    const unsigned active = __ballot_sync(0xffffffffu, valid);
     if (!active) break;
     if (valid) {
-      int l = lab[i];
-      if ((unsigned)l >= (unsigned)b.nmu) l = 0;  // flagged by km_hist; keeps indexing in range
       unsigned peers = __match_any_sync(active, l);
       int leader = __ffs(peers) - 1;
-      if (lane == leader && base[l] < 0)
-        base[l] = b.start[l] + b.hist[(size_t)l * b.nb + blockIdx.x];
-      __syncwarp(active);
       int pos = base[l] + __popc(peers & lt);
-      b.member[pos] = (int)i;
+      b.member[pos] = (int)(blk + c + lane);
       __syncwarp(active);
       if (lane == leader) base[l] += __popc(peers);
     }
     __syncwarp();
   }
-}
-
-// One warp per cluster.  Lanes load 32 members at a time and form the products rho_i * g_i
-// (each rounded on its own, as the reference's `rho[i] * grid[i*ndim]`); four lanes then
-// add them into w, x, y, z strictly in ascending member order from shared memory, so the
-// sums round exactly as the reference's sequential loop (src/kmeans.cpp:121-126).
-constexpr int kSumWarps = 1;
-constexpr int kSumChunk = 512;
-__global__ void __launch_bounds__(32 * kSumWarps) km_sums(KmBufs b)
-{
-  KmState* st = b.st;
-  if (st->done) return;
-  // Products of up to kSumChunk members are formed by all lanes first (their loads are
-  // independent), then four lanes run the in-order FP64 chains from shared memory.
-  __shared__ double sv[4][kSumChunk];
-  int it = st->iter;
-  int lane = threadIdx.x & 31;
-  int k = blockIdx.x;
-  if (k >= b.nmu) return;
-  int s = b.start[k], n = b.total[k];
-  double acc = 0.0;  // lane q < 4 owns quantity q: 0 = w, 1 = x, 2 = y, 3 = z
-  for (int base = 0; base < n; base += kSumChunk) {
-    int cnt = min(kSumChunk, n - base);
-#pragma unroll 4
-    for (int m = lane; m < cnt; m += 32) {
-      int i = b.member[s + base + m];
-      double r = b.rho[i];
-      sv[0][m] = r;
-      sv[1][m] = __dmul_rn(r, b.gx[i]);
-      sv[2][m] = __dmul_rn(r, b.gy[i]);
-      sv[3][m] = __dmul_rn(r, b.gz[i]);
-    }
-    __syncwarp();
-    if (lane < 4) {
-      const double* v = sv[lane];
-      int j = 0;
-      for (; j + 4 <= cnt; j += 4) {
-        double t0 = v[j], t1 = v[j + 1], t2 = v[j + 2], t3 = v[j + 3];
-        acc = __dadd_rn(acc, t0);
-        acc = __dadd_rn(acc, t1);
-        acc = __dadd_rn(acc, t2);
-        acc = __dadd_rn(acc, t3);
-      }
-      for (; j < cnt; j++) acc = __dadd_rn(acc, v[j]);
-    }
-    __syncwarp();
-  }
-  double wsum = __shfl_sync(0xffffffffu, acc, 0);
-  double x = __shfl_sync(0xffffffffu, acc, 1);
-  double y = __shfl_sync(0xffffffffu, acc, 2);
-  double z = __shfl_sync(0xffffffffu, acc, 3);
-  if (lane != 0) return;
-  if (wsum < 1e-8) atomicExch(&st->empty, 1);
-  double* nc = b.cen + (size_t)((it + 1) & 1) * 3 * b.nmu;
-  float* nc32 = b.cen32 + (size_t)((it + 1) & 1) * 3 * b.nmu;
-  double cx = __ddiv_rn(x, wsum), cy = __ddiv_rn(y, wsum), cz = __ddiv_rn(z, wsum);
-  nc[k] = cx; nc[b.nmu + k] = cy; nc[2 * b.nmu + k] = cz;
-  nc32[k] = (float)cx; nc32[b.nmu + k] = (float)cy; nc32[2 * b.nmu + k] = (float)cz;
 }
 
 __device__ __forceinline__ double block_max(double v, double* red)
@@ -833,57 +797,131 @@ __device__ __forceinline__ double block_max(double v, double* red)
   return red[0];
 }
 
-// Single block: normed difference (new vs current), convergence and state update.
-__global__ void km_normdiff(KmBufs b)
+// Fixed-order block sum (deterministic; not the reference's rounding).
+__device__ __forceinline__ double block_sum(double v, double* red)
 {
-  KmState* st = b.st;
-  if (st->done) return;
-  __shared__ double red[32];
-  int it = st->iter;
-  int n3 = 3 * b.nmu;
-  if (st->empty || st->bad_label) {
-    if (threadIdx.x == 0) { st->done = 1; st->iter = it + 1; }
-    return;
+  for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+    red[0] = t;
   }
-  const double* a = b.cen + (size_t)((it + 1) & 1) * 3 * b.nmu;   // new
-  const double* c = b.cen + (size_t)(it & 1) * 3 * b.nmu;         // current
+  __syncthreads();
+  return red[0];
+}
+
+// The terms ((a_i - c_i) / scale)^2 of the reference's normed difference in its index order
+// i = 3k + d (centroid k, coordinate d), written to `terms`; returns scale.  Whole block.
+__device__ double normdiff_terms(const KmBufs& b, const double* a, const double* c,
+                                 double* terms, double* red)
+{
+  const int n3 = 3 * b.nmu;
   double ma = 0.0, mc = 0.0;
   for (int i = threadIdx.x; i < n3; i += blockDim.x) {
-    int k = i / 3, d = i - 3 * k;
-    ma = fmax(ma, fabs(a[d * b.nmu + k]));
-    mc = fmax(mc, fabs(c[d * b.nmu + k]));
+    ma = fmax(ma, fabs(__ldcg(a + i)));
+    mc = fmax(mc, fabs(__ldcg(c + i)));
   }
   ma = block_max(ma, red);
   mc = block_max(mc, red);
-  double scale = __dadd_rn(ma, mc);
-  extern __shared__ double sterm[];
-  const bool in_smem = n3 <= kNormSmem;
-  double* terms = in_smem ? sterm : b.terms;
+  const double scale = __dadd_rn(ma, mc);
   for (int i = threadIdx.x; i < n3; i += blockDim.x) {
     int k = i / 3, d = i - 3 * k;
-    double q = __ddiv_rn(__dsub_rn(a[d * b.nmu + k], c[d * b.nmu + k]), scale);
+    double q = __ddiv_rn(__dsub_rn(__ldcg(a + d * b.nmu + k), __ldcg(c + d * b.nmu + k)), scale);
     terms[i] = __dmul_rn(q, q);
   }
   __syncthreads();
-  // Fixed-order tree sum of the terms (deterministic); it differs from the reference's
-  // sequential sum by at most ~(n + log n) u relative, so it decides `diff < threshold`
-  // identically unless the two are within 1e-10 of each other -- then, and for the value
-  // finally reported, the sequential sum is evaluated exactly (km_normdiff_exact).
-  double part = 0.0;
-  for (int i = threadIdx.x; i < n3; i += blockDim.x) part += terms[i];
-  for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double tot = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
-    double diff = scale * sqrt(tot);
-    bool exact = fabs(diff - st->threshold) <= 1e-10 * st->threshold;
-    if (exact) {
-      double s = 0.0;
-      for (int i = 0; i < n3; i++) s = __dadd_rn(s, terms[i]);
-      diff = __dmul_rn(scale, __dsqrt_rn(s));
+  return scale;
+}
+
+// One block of four warps per cluster.  All threads form the products rho_i * g_i of up to
+// kSumChunk members (each rounded on its own, as the reference's `rho[i] * grid[i*ndim]`),
+// then warp q adds quantity q (0 = w, 1 = x, 2 = y, 3 = z) strictly in ascending member
+// order with warp_seqsum, which rounds exactly as the reference's sequential loop
+// (src/kmeans.cpp:121-126).  The last block to finish (a ticket in the state) also takes the
+// convergence decision of the iteration: the normed difference approximated by a
+// fixed-order sum of squared centroid moves (relative deviation from the reference's value
+// below (3 N_mu + 8) u), evaluated exactly when within 1e-10 of the threshold.
+constexpr int kSumChunk = 512;
+constexpr int kSumThreads = 128;
+__global__ void __launch_bounds__(kSumThreads) km_sums(KmBufs b)
+{
+  KmState* st = b.st;
+  if (st->done) return;
+  __shared__ double sv[4][kSumChunk];
+  __shared__ double res[4];
+  __shared__ double red[32];
+  __shared__ int last;
+  const int it = st->iter;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x;
+  const int nmu = b.nmu;
+  const int s = b.start[k], n = b.total[k];
+  double acc = 0.0;
+  for (int base = 0; base < n; base += kSumChunk) {
+    const int cnt = min(kSumChunk, n - base);
+    for (int m = threadIdx.x; m < cnt; m += kSumThreads) {
+      int i = b.member[s + base + m];
+      double r = b.rho[i];
+      sv[0][m] = r;
+      sv[1][m] = __dmul_rn(r, b.gx[i]);
+      sv[2][m] = __dmul_rn(r, b.gy[i]);
+      sv[3][m] = __dmul_rn(r, b.gz[i]);
     }
+    __syncthreads();
+    acc = warp_seqsum(acc, sv[warp], cnt);
+    __syncthreads();
+  }
+  if (lane == 0) res[warp] = acc;
+  __syncthreads();
+  double* part = b.terms + 3 * (size_t)nmu;   // per-cluster squared move
+  if (threadIdx.x == 0) {
+    const double wsum = res[0];
+    if (wsum < 1e-8) atomicExch(&st->empty, 1);
+    double* nc = b.cen + (size_t)((it + 1) & 1) * 3 * nmu;
+    float* nc32 = b.cen32 + (size_t)((it + 1) & 1) * 3 * nmu;
+    const double* oc = b.cen + (size_t)(it & 1) * 3 * nmu;
+    double sq = 0.0;
+    for (int d = 0; d < 3; d++) {
+      double v = __ddiv_rn(res[1 + d], wsum);
+      nc[d * nmu + k] = v;
+      nc32[d * nmu + k] = (float)v;
+      double dv = v - oc[d * nmu + k];
+      sq += dv * dv;
+    }
+    part[k] = sq;
+    __threadfence();
+    last = atomicAdd(&st->ticket, 1) == nmu - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // ---- last block: the convergence decision and the state update of this iteration ----
+  if (*(volatile int*)&st->empty || *(volatile int*)&st->bad_label) {
+    if (threadIdx.x == 0) { st->done = 1; st->iter = it + 1; st->ticket = 0; }
+    return;
+  }
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nmu; i += kSumThreads) v += __ldcg(part + i);
+  const double approx = sqrt(block_sum(v, red));
+  const double thr = st->threshold;
+  const bool exact = fabs(approx - thr) <= 1e-10 * thr;
+  double diff = approx;
+  if (exact) {
+    const double* a = b.cen + (size_t)((it + 1) & 1) * 3 * nmu;
+    const double* c = b.cen + (size_t)(it & 1) * 3 * nmu;
+    double scale = normdiff_terms(b, a, c, b.terms, red);
+    if (warp == 0) {
+      double ssum = warp_seqsum(0.0, b.terms, 3 * nmu);
+      if (lane == 0) res[0] = __dmul_rn(scale, __dsqrt_rn(ssum));
+    }
+    __syncthreads();
+    diff = res[0];
+  }
+  if (threadIdx.x == 0) {
     st->diff_exact = exact;
     st->diff = diff;
     st->pct = 100.0 * (double)st->changed / (double)b.ng;
@@ -893,42 +931,39 @@ __global__ void km_normdiff(KmBufs b)
     st->rechecked_total += st->recheck_n;
     st->recheck_n = 0;
     st->final_buf = (it + 1) & 1;
-    if (diff < st->threshold) {
+    if (diff < thr) {
       st->converged = 1;
       st->done = 1;
     } else if (it + 1 >= st->max_it) {
       st->done = 1;
-      st->zero_fill = !(diff > st->threshold);
+      st->zero_fill = !(diff > thr);
     }
+    st->ticket = 0;
     st->iter = it + 1;
   }
 }
 
-// The reference's sequential normed difference of the last iteration (one thread).
-__global__ void km_normdiff_exact(KmBufs b)
+// The reference's normed difference of the last iteration, exactly (one block).
+__global__ void __launch_bounds__(1024) km_normdiff_exact(KmBufs b)
 {
   KmState* st = b.st;
   if (st->diff_exact || st->empty || st->iter < 1) return;
-  int it = st->iter - 1;
-  int n3 = 3 * b.nmu;
+  __shared__ double red[32];
+  __shared__ double out;
+  const int it = st->iter - 1;
   const double* a = b.cen + (size_t)((it + 1) & 1) * 3 * b.nmu;
   const double* c = b.cen + (size_t)(it & 1) * 3 * b.nmu;
-  double ma = 0.0, mc = 0.0;
-  for (int i = 0; i < b.nmu * 3; i++) {
-    ma = fmax(ma, fabs(a[i]));
-    mc = fmax(mc, fabs(c[i]));
+  const double scale = normdiff_terms(b, a, c, b.terms, red);
+  if (threadIdx.x < 32) {
+    double ssum = warp_seqsum(0.0, b.terms, 3 * b.nmu);
+    if (threadIdx.x == 0) out = __dmul_rn(scale, __dsqrt_rn(ssum));
   }
-  double scale = __dadd_rn(ma, mc);
-  double s = 0.0;
-  for (int i = 0; i < n3; i++) {
-    int k = i / 3, d = i - 3 * k;
-    double q = __ddiv_rn(__dsub_rn(a[d * b.nmu + k], c[d * b.nmu + k]), scale);
-    s = __dadd_rn(s, __dmul_rn(q, q));
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    st->diff = out;
+    b.log[it] = out;
+    st->diff_exact = 1;
   }
-  double diff = __dmul_rn(scale, __dsqrt_rn(s));
-  st->diff = diff;
-  b.log[it] = diff;
-  st->diff_exact = 1;
 }
 
 // Bounding boxes of the 256-point tiles of the binned order (for the pruned map_to_grid).
@@ -982,22 +1017,33 @@ __global__ void km_map_pruned(KmBufs b, const double* __restrict__ box, int ntil
   double cut = u * (1.0 + 1e-9);
   double bs = CUDART_INF, bm = CUDART_INF;
   int bk = 0x7fffffff;
-  for (int t = lane; t < ntiles; t += 32) {
-    double lb = 0.0;
-    for (int d = 0; d < 3; d++) {
-      double v = fmax(0.0, fmax(box[t * 6 + d] - c3[d], c3[d] - box[t * 6 + 3 + d]));
-      lb += v * v;
+  // Candidate tiles are found 32 at a time; the whole warp then scans each one (coalesced
+  // reads of the binned order, 8 points per lane).
+  for (int t0 = 0; t0 < ntiles; t0 += 32) {
+    int t = t0 + lane;
+    bool cand = false;
+    if (t < ntiles) {
+      double lb = 0.0;
+      for (int d = 0; d < 3; d++) {
+        double v = fmax(0.0, fmax(box[t * 6 + d] - c3[d], c3[d] - box[t * 6 + 3 + d]));
+        lb += v * v;
+      }
+      cand = lb <= cut;
     }
-    if (lb > cut) continue;
-    long long p0 = (long long)t * 256, p1 = min((long long)b.ng, p0 + 256);
-    for (long long q = p0; q < p1; q++) {
-      int i = b.perm[q];
-      double d2 = d2_exact(b.gx[i], b.gy[i], b.gz[i], c3[0], c3[1], c3[2]);
-      // Any order: a candidate can win on a smaller sqrt or on an equal sqrt and a smaller
-      // index; equal sqrt values come from squared distances within a few ulps.
-      if (d2 <= bm * (1.0 + 0x1p-50)) {
-        double r = __dsqrt_rn(d2);
-        if (r < bs || (r == bs && i < bk)) { bs = r; bk = i; bm = fmin(bm, d2); }
+    unsigned m = __ballot_sync(0xffffffffu, cand);
+    while (m) {
+      int tt = t0 + __ffs(m) - 1;
+      m &= m - 1;
+      long long p0 = (long long)tt * 256, p1 = min((long long)b.ng, p0 + 256);
+      for (long long q = p0 + lane; q < p1; q += 32) {
+        int i = b.perm[q];
+        double d2 = d2_exact(b.gx[i], b.gy[i], b.gz[i], c3[0], c3[1], c3[2]);
+        // Any order: a candidate can win on a smaller sqrt or on an equal sqrt and a
+        // smaller index; equal sqrt values come from squared distances within a few ulps.
+        if (d2 <= bm * (1.0 + 0x1p-50)) {
+          double r = __dsqrt_rn(d2);
+          if (r < bs || (r == bs && i < bk)) { bs = r; bk = i; bm = fmin(bm, d2); }
+        }
       }
     }
   }
@@ -1125,7 +1171,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   int* hist = (int*)ws_get(c, WS_KM_HIST, sizeof(int) * (size_t)nmu * b.nb);
   int* tot = (int*)ws_get(c, WS_KM_TOTAL, sizeof(int) * 2 * nmu);
   int* member = (int*)ws_get(c, WS_KM_MEMBER, sizeof(int) * ng);
-  double* terms = (double*)ws_get(c, WS_KM_TERMS, sizeof(double) * 3 * nmu);
+  double* terms = (double*)ws_get(c, WS_KM_TERMS, sizeof(double) * 4 * nmu);
   int* recheck = (int*)ws_get(c, WS_KM_RECHECK, sizeof(int) * ng);
   KmState* st = (KmState*)ws_get(c, WS_KM_STATE, sizeof(KmState) + 64);
   double* logb = (double*)ws_get(c, WS_KM_LOG, sizeof(double) * 2 * max_it);
@@ -1185,9 +1231,6 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     THC_CUDA(c, cudaFuncSetAttribute(km_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
     THC_CUDA(c, cudaFuncSetAttribute(km_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
   }
-  size_t norm_smem = 3 * (size_t)nmu <= kNormSmem ? sizeof(double) * 3 * nmu : 0;
-  if (norm_smem > 16 * 1024)  // dynamic + static above the 48 KB default needs the opt-in
-    THC_CUDA(c, cudaFuncSetAttribute(km_normdiff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)norm_smem));
   int* hflag = (int*)c->pinned;
   const int kCheckEvery = 8;
   // One k-means iteration; every kernel reads the iteration index from device state and
@@ -1215,14 +1258,10 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     THC_LAUNCHED(c, "km_hist");
     km_colscan<<<(int)cdiv((long long)nmu * 32, 256), 256, 0, s>>>(b);
     THC_LAUNCHED(c, "km_colscan");
-    km_kscan<<<1, 1024, 0, s>>>(b);
-    THC_LAUNCHED(c, "km_kscan");
-    km_scatter<<<b.nb, 128, hist_smem, s>>>(b);
+    km_scatter<<<b.nb, 256, hist_smem, s>>>(b);
     THC_LAUNCHED(c, "km_scatter");
-    km_sums<<<nmu, 32 * kSumWarps, 0, s>>>(b);
+    km_sums<<<nmu, kSumThreads, 0, s>>>(b);
     THC_LAUNCHED(c, "km_sums");
-    km_normdiff<<<1, 1024, norm_smem, s>>>(b);
-    THC_LAUNCHED(c, "km_normdiff");
     return THC_OK;
   };
   // A CUDA graph of kCheckEvery iterations, cached on the context for these buffers.
@@ -1259,7 +1298,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     int nblock = std::min(kCheckEvery, max_it - it);
     if (gexec && nblock == kCheckEvery) {
       THC_CUDA(c, cudaGraphLaunch(gexec, s));
-      c->launches += (mixed ? 8LL : 7LL) * kCheckEvery;  // kernels per captured iteration
+      c->launches += (mixed ? 6LL : 5LL) * kCheckEvery;  // kernels per captured iteration
     } else {
       for (int k = 0; k < nblock; k++) {
         int rc = iteration(true);
@@ -1273,7 +1312,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
       if (*hflag) break;
     }
   }
-  km_normdiff_exact<<<1, 1, 0, s>>>(b);
+  km_normdiff_exact<<<1, 1024, 0, s>>>(b);
   THC_LAUNCHED(c, "km_normdiff_exact");
   // Map the final centroids to the grid, sort, count duplicates.
   int* didx = is_device_ptr(out_idx) ? out_idx : (int*)((char*)hist);  // hist is free now

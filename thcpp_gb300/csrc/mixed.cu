@@ -162,7 +162,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   double* phimu = (double*)ws_get(c, WS_PHIMU, sizeof(double) * nmu * no);
   double* C = (double*)ws_get(c, WS_C, sizeof(double) * 2 * nn);
   double* Cinv = (double*)ws_get(c, WS_CINV, sizeof(double) * nn);
-  double* zg = (double*)ws_get(c, WS_ZT, sizeof(double) * nmu * ng);   // Z: N_g x N_mu
+  float2* zg = (float2*)ws_get(c, WS_ZT, sizeof(float2) * nmu * ng);   // Z: N_g x N_mu, double-word
   float* zeta = (float*)ws_get(c, WS_ZETA, sizeof(float) * nmu * ng);
   float2* zhat = (float2*)ws_get(c, WS_ZHAT, sizeof(float2) * nmu * nc);
   double* dsym = (double*)ws_get(c, WS_DSYM, (sizeof(double) + sizeof(float)) * nc + 64);
@@ -232,6 +232,8 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   };
   // Z = (Phi Phi_mu^T)^2 (N_g x N_mu) via the sliced GEMM: A = Phi sliced by grid point,
   // B = Phi_mu sliced by interpolating point; Z's rows are then K-contiguous for the solve.
+  // Z is kept as double-word FP32 (~46 bits; the solve slices it to 42), so the epilogue
+  // squares in FP32 arithmetic instead of on the narrow FP64 pipe.
   if ((st = oz_slice_rows_f64(c, phi, ng, no, no, 1, nullptr, 0, sp, sa, no_kpad,
                               ng_pad * no_kpad, eb, ng_pad)))
     return st;
@@ -244,7 +246,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     g.a.s = sa; g.a.e = eb; g.a.ld = no_kpad; g.a.slice_stride = ng_pad * no_kpad;
     g.b.s = sb; g.b.e = ea; g.b.ld = no_kpad; g.b.slice_stride = mu_pad * no_kpad;
     g.b.k_contig = true;
-    g.levels = sp; g.epilogue = OZ_SQUARE_F64; g.C = zg; g.ldc = nmu;
+    g.levels = sp; g.epilogue = OZ_SQUARE_DW; g.C = zg; g.ldc = nmu;
     if ((st = gemm(g))) return st;
   }
   CholStatus hcs{};
@@ -269,12 +271,14 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   // A rank-deficient C (shifted) has an inverse whose null-space entries are ~1/shift, so
   // the product cancels by far more than any slice depth resolves: it runs in FP64 then.
   if (shifted) {
-    double* z64 = (double*)ws_get(c, WS_ZTMP, sizeof(double) * nmu * ng);
+    double* z64 = (double*)ws_get(c, WS_ZTMP, 2 * sizeof(double) * nmu * ng);
     if (!z64) return set_error(c, THC_ERR_NOMEM, "thc_isdf: FP64 zeta buffer");
+    double* zf = z64 + (long long)nmu * ng;
+    if ((st = dw_to_f64(c, zg, (long long)nmu * ng, zf))) return st;
     GemmArgs g;
     g.M = nmu; g.N = ng; g.K = nmu;
     g.A = Cinv; g.sam = nmu; g.sak = 1;
-    g.B = zg; g.sbn = nmu; g.sbk = 1;
+    g.B = zf; g.sbn = nmu; g.sbk = 1;
     g.C = z64; g.ldc = ng;
     if ((st = dgemm(c, g))) return st;
     to_f32<<<(unsigned)cdiv((long long)nmu * ng, 256), 256, 0, s>>>(z64, (long long)nmu * ng, zeta);
@@ -283,8 +287,8 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, sz, sa, mu_kpad,
                                 mu_pad * mu_kpad, ea, mu_pad)))
       return st;
-    if ((st = oz_slice_rows_f64(c, zg, ng, nmu, nmu, 1, nullptr, 0, sz, sb, mu_kpad,
-                                ng_pad * mu_kpad, eb, ng_pad)))
+    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, sz, sb, mu_kpad, ng_pad * mu_kpad, eb,
+                               ng_pad)))
       return st;
     OzArgs g;
     g.M = nmu; g.N = ng; g.K = nmu;

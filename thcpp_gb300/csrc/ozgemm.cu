@@ -17,6 +17,21 @@ namespace thc {
 
 namespace {
 
+// Final store of one FP64 product value under the epilogue (FP64 arithmetic: used by the
+// mma.sync kernel and the split-K reduction, not on the tcgen05 fast path).
+__device__ __forceinline__ void store_epilogue(const OzArgs& g, long long m, long long n, double v)
+{
+  if (g.epilogue == OZ_SQUARE_F64 || g.epilogue == OZ_SQUARE_DW) v = v * v;
+  if (g.epilogue == OZ_STORE_F32) {
+    ((float*)g.C)[m * g.ldc + n] = (float)v;
+  } else if (g.epilogue == OZ_SQUARE_DW) {
+    float hi = (float)v;
+    ((float2*)g.C)[m * g.ldc + n] = make_float2(hi, (float)(v - (double)hi));
+  } else {
+    ((double*)g.C)[m * g.ldc + n] = v;
+  }
+}
+
 constexpr int OBM = 64, OBN = 32, OBK = 32, OCHUNK = 256, OPAD = 8;
 constexpr int OLDA = OBK + OPAD;      // shared row length (bf16) of A and k-contiguous B
 constexpr int OLDBN = OBN + OPAD;     // shared row length of n-contiguous B
@@ -192,11 +207,7 @@ __global__ void __launch_bounds__(128, 2) ozgemm_kernel(OzArgs g)
         g.part[((long long)blockIdx.z * g.M + m) * g.N + n] = v;
         continue;
       }
-      if (g.epilogue == OZ_SQUARE_F64) v = v * v;
-      if (g.epilogue == OZ_STORE_F32)
-        ((float*)g.C)[m * g.ldc + n] = (float)v;
-      else
-        ((double*)g.C)[m * g.ldc + n] = v;
+      store_epilogue(g, m, n, v);
     }
   }
 }
@@ -230,11 +241,7 @@ __global__ void oz_reduce_kernel(OzArgs g)
   if (g.lower_only && n > m) return;
   double v = 0.0;
   for (int z = 0; z < g.ksplit; z++) v += g.part[((long long)z * g.M + m) * g.N + n];
-  if (g.epilogue == OZ_SQUARE_F64) v = v * v;
-  if (g.epilogue == OZ_STORE_F32)
-    ((float*)g.C)[m * g.ldc + n] = (float)v;
-  else
-    ((double*)g.C)[m * g.ldc + n] = v;
+  store_epilogue(g, m, n, v);
 }
 
 // One warp per row: exponent from the row maximum, then the slices of an FP64 input in
@@ -303,9 +310,78 @@ __global__ void slice_rows_kernel(const double* __restrict__ X, long long rows, 
       int sh = 7 * (ns - 1 - s2);
       long long S = sh ? ((R + (1LL << (sh - 1))) >> sh) : R;
       R -= S << sh;
-      out[s2 * sstride + r * ldo + cc] = __float2bfloat16_rn((float)S);
+      // |S| <= 128: convert through int32 (a 64-bit integer conversion runs on the slow
+      // FP64-class path on this part).
+      out[s2 * sstride + r * ldo + cc] = __float2bfloat16_rn((float)(int)S);
     }
   }
+}
+
+// round(|x| 2^shift_total) of an FP32 value as a signed 64-bit integer (round half even).
+__device__ __forceinline__ long long fixed_point_f32(float x, int shift_total)
+{
+  unsigned bits = __float_as_uint(x);
+  int E = (int)((bits >> 23) & 0xff);
+  if (E == 0) return 0;
+  unsigned long long m = (bits & 0x7fffffu) | 0x800000u;
+  int s = E - 150 + shift_total;
+  unsigned long long X;
+  if (s >= 0) {
+    X = s < 40 ? m << s : 0;   // beyond 2^63: cannot occur for |x| < 2^e rows
+  } else if (s <= -32) {
+    X = 0;
+  } else {
+    int r = -s;
+    unsigned long long q = m >> r;
+    unsigned long long rem = m & ((1ULL << r) - 1);
+    unsigned long long half = 1ULL << (r - 1);
+    if (rem > half || (rem == half && (q & 1))) q++;
+    X = q;
+  }
+  return (bits >> 31) ? -(long long)X : (long long)X;
+}
+
+// Slices of a double-word (hi, lo) matrix, one warp per row, as slice_rows_kernel: the row
+// exponent comes from max |hi| (|hi + lo| < 2^e whenever |hi| < 2^e), and the fixed-point
+// integer is the sum of the two parts' roundings (within one unit of the exact value).
+__global__ void slice_rows_dw_kernel(const float2* __restrict__ X, long long rows, long long cols,
+                                     long long ldx, int ns, __nv_bfloat16* out, long long ldo,
+                                     long long sstride, int* exps, long long rows_pad)
+{
+  long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (r >= rows_pad) return;
+  unsigned mx = 0;
+  if (r < rows)
+    for (long long cc = lane; cc < cols; cc += 32) {
+      unsigned a = __float_as_uint(X[r * ldx + cc].x) & 0x7fffffffu;
+      mx = a > mx ? a : mx;
+    }
+  for (int off = 16; off; off >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  int e = 0;
+  int Em = (int)(mx >> 23);
+  if (Em > 0) e = Em - 126;
+  if (lane == 0) exps[r] = e;
+  const int total = 7 * ns - e;
+  for (long long cc = lane; cc < ldo; cc += 32) {
+    long long R = 0;
+    if (r < rows && cc < cols && Em > 0) {
+      float2 v = X[r * ldx + cc];
+      R = fixed_point_f32(v.x, total) + fixed_point_f32(v.y, total);
+    }
+    for (int s2 = 0; s2 < ns; s2++) {
+      int sh = 7 * (ns - 1 - s2);
+      long long S = sh ? ((R + (1LL << (sh - 1))) >> sh) : R;
+      R -= S << sh;
+      out[s2 * sstride + r * ldo + cc] = __float2bfloat16_rn((float)(int)S);
+    }
+  }
+}
+
+__global__ void dw_to_f64_kernel(const float2* __restrict__ X, long long n, double* out)
+{
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)X[i].x + (double)X[i].y;
 }
 
 // FP32 input scaled by an FP32 copy of `scale` (rounded once to FP32, then sliced exactly
@@ -355,30 +431,6 @@ __global__ void slice_rows_f32_kernel(const float* __restrict__ X, long long row
   }
 }
 
-// One thread per column: exponent from the column maximum, then the slices.
-__global__ void slice_cols_kernel(const double* __restrict__ X, long long rows, long long cols,
-                                  long long ldx, int ns, __nv_bfloat16* out, long long ldo,
-                                  long long sstride, int* exps, long long rows_pad,
-                                  long long cols_pad)
-{
-  long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (n >= cols_pad) return;
-  double mx = 0.0;
-  if (n < cols)
-    for (long long k = 0; k < rows; k++) mx = fmax(mx, fabs(X[k * ldx + n]));
-  int e = 0;
-  if (mx > 0.0) frexp(mx, &e);
-  exps[n] = e;
-  for (long long k = 0; k < rows_pad; k++) {
-    double x = (n < cols && k < rows) ? ldexp(X[k * ldx + n], 7 - e) : 0.0;
-    for (int s = 0; s < ns; s++) {
-      double q = rint(x);
-      out[s * sstride + k * ldo + n] = __double2bfloat16(q);
-      x = (x - q) * 128.0;
-    }
-  }
-}
-
 }  // namespace
 
 int oz_choose_split(long long M, long long N, long long K, bool lower)
@@ -409,6 +461,24 @@ int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, l
   return THC_OK;
 }
 
+int oz_slice_rows_dw(Ctx* c, const float2* X, long long rows, long long cols, long long ldx,
+                     int nslices, __nv_bfloat16* out, long long ldo, long long slice_stride,
+                     int* exps, long long rows_pad)
+{
+  long long threads = rows_pad * 32;
+  slice_rows_dw_kernel<<<(unsigned)cdiv(threads, 256), 256, 0, c->stream>>>(
+      X, rows, cols, ldx, nslices, out, ldo, slice_stride, exps, rows_pad);
+  THC_LAUNCHED(c, "slice_rows_dw");
+  return THC_OK;
+}
+
+int dw_to_f64(Ctx* c, const float2* X, long long n, double* out)
+{
+  dw_to_f64_kernel<<<(unsigned)cdiv(n, 256), 256, 0, c->stream>>>(X, n, out);
+  THC_LAUNCHED(c, "dw_to_f64");
+  return THC_OK;
+}
+
 int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, long long ldx,
                       const float* scale, int scale_shift, int nslices, __nv_bfloat16* out,
                       long long ldo, long long slice_stride, int* exps, long long rows_pad)
@@ -424,16 +494,6 @@ int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, lo
   slice_rows_f32_kernel<<<g2, 256, 0, c->stream>>>(X, rows, cols, ldx, scale, scale_shift,
                                                    nslices, out, ldo, slice_stride, rowmax, exps);
   THC_LAUNCHED(c, "slice_rows_f32");
-  return THC_OK;
-}
-
-int oz_slice_cols_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
-                      int nslices, __nv_bfloat16* out, long long ldo, long long slice_stride,
-                      int* exps, long long rows_pad, long long cols_pad)
-{
-  slice_cols_kernel<<<(unsigned)cdiv(cols_pad, 256), 256, 0, c->stream>>>(
-      X, rows, cols, ldx, nslices, out, ldo, slice_stride, exps, rows_pad, cols_pad);
-  THC_LAUNCHED(c, "slice_cols_f64");
   return THC_OK;
 }
 

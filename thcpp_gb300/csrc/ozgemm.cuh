@@ -18,7 +18,9 @@
 
 namespace thc {
 
-enum OzEpilogue : int { OZ_STORE_F64 = 0, OZ_SQUARE_F64 = 1, OZ_STORE_F32 = 2 };
+// OZ_SQUARE_DW stores the squared product as a double-word FP32 pair (float2 {hi, lo},
+// hi + lo carrying ~46 bits), which needs no FP64 arithmetic in the epilogue.
+enum OzEpilogue : int { OZ_STORE_F64 = 0, OZ_SQUARE_F64 = 1, OZ_STORE_F32 = 2, OZ_SQUARE_DW = 3 };
 
 struct OzOperand {
   const __nv_bfloat16* s = nullptr;  // slices
@@ -57,15 +59,15 @@ int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, l
                       long long sc, const double* scale, int scale_shift, int nslices,
                       __nv_bfloat16* out, long long ldo, long long slice_stride, int* exps,
                       long long rows_pad);
+// Slices of a double-word matrix (float2 {hi, lo} entries, row-major, ld = ldx).
+int oz_slice_rows_dw(Ctx* c, const float2* X, long long rows, long long cols, long long ldx,
+                     int nslices, __nv_bfloat16* out, long long ldo, long long slice_stride,
+                     int* exps, long long rows_pad);
+// Double-word matrix to FP64 (hi + lo).
+int dw_to_f64(Ctx* c, const float2* X, long long n, double* out);
 int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, long long ldx,
                       const float* scale, int scale_shift, int nslices, __nv_bfloat16* out,
                       long long ldo, long long slice_stride, int* exps, long long rows_pad);
-// Slice columns of X (rows = k, cols = n, X[k*ldx + n]) into out[slice][k][n] with one
-// exponent per column n.
-int oz_slice_cols_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
-                      int nslices, __nv_bfloat16* out, long long ldo, long long slice_stride,
-                      int* exps, long long rows_pad, long long cols_pad);
-
 // Warp-level mma.sync implementation (reference for the tensor-core kernel below).
 int ozgemm(Ctx* c, const OzArgs& g);
 // tcgen05 / TMEM / TMA implementation; both operands K-contiguous.  err_flag (device int)

@@ -370,16 +370,32 @@ __global__ void __launch_bounds__(TTHREADS, 1)
             ((float*)g.C)[m * g.ldc + n] = __fadd_rn(ah[q], al[q]) * sc;
             continue;
           }
+          if (g.epilogue == OZ_SQUARE_DW && g.ksplit <= 1 && ex > -60 && ex < 60) {
+            // (h + l)^2 in double-word FP32: p + e = h^2 exactly (FMA), plus 2 h l.
+            float sc = pow2f(ex);
+            float h = ah[q] * sc, l = al[q] * sc;
+            float p = __fmul_rn(h, h);
+            float e = __fmaf_rn(h, h, -p);
+            e = __fmaf_rn(2.f * h, l, e);
+            float zh, zl;
+            fast_two_sum(p, e, zh, zl);
+            ((float2*)g.C)[m * g.ldc + n] = make_float2(zh, zl);
+            continue;
+          }
           double val = ((double)ah[q] + (double)al[q]) * pow2d(ex);
           if (g.ksplit > 1) {
             g.part[((long long)blockIdx.z * g.M + m) * g.N + n] = val;
             continue;
           }
-          if (g.epilogue == OZ_SQUARE_F64) val = val * val;
-          if (g.epilogue == OZ_STORE_F32)
+          if (g.epilogue == OZ_SQUARE_F64 || g.epilogue == OZ_SQUARE_DW) val = val * val;
+          if (g.epilogue == OZ_STORE_F32) {
             ((float*)g.C)[m * g.ldc + n] = (float)val;
-          else
+          } else if (g.epilogue == OZ_SQUARE_DW) {
+            float hi = (float)val;
+            ((float2*)g.C)[m * g.ldc + n] = make_float2(hi, (float)(val - (double)hi));
+          } else {
             ((double*)g.C)[m * g.ldc + n] = val;
+          }
         }
       }
     }
