@@ -124,6 +124,22 @@ int thc_kmeans(thc_ctx* ctx, const double* grid, const double* rho, long long ng
 int thc_kmeans_history(thc_ctx* ctx, double* diff, double* pct_changed, int n);
 
 /*
+ * thc_kmeans without any device allocation.  No counterpart in the reference: it exists
+ * for callers whose device memory is owned by their own pool allocator and who therefore
+ * cannot let a library call cudaMalloc/cudaFree.  Same arguments, results and status codes
+ * as thc_kmeans (bit-identical indices), for N_g <= 65,536, N_mu <= 1,024 and
+ * max_it <= 1,000 (THC_ERR_SHAPE beyond).  All device scratch comes from one file-scope
+ * 12 MiB device array shared by every call in the process; it keeps the last call's
+ * contents (the call clears what must start at zero), and calls that overlap on the GPU
+ * race on it, so serialise them.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress) and may load the module: make it before any stream capture.
+ * thc_kmeans_history reports no history for these calls.
+ */
+int thc_kmeans_noalloc(thc_ctx* ctx, const double* grid, const double* rho, long long ng,
+                       int nmu, const int* init_idx, int max_it, double threshold,
+                       int* out_idx, thc_kmeans_stats* stats);
+
+/*
  * ISDF interpolating vectors + FFT Coulomb matrix + its Cholesky factor.
  *   phi           ng x norb doubles, C order: the real part of `aoR` (real orbitals)
  *   idx           nmu grid indices (the k-means output)

@@ -33,7 +33,7 @@ EXPORTS = [
     "thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
     "thc_ctx_last_error", "thc_status_string", "thc_ctx_kernel_launches",
     "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
-    "thc_kmeans_history", "thc_factorize_batched",
+    "thc_kmeans_history", "thc_factorize_batched", "thc_kmeans_noalloc",
 ]
 
 
@@ -109,10 +109,11 @@ def load(build_if_missing: bool = False):
     lib.thc_kmeans_history.restype = ci
     lib.thc_kmeans_initial_indices.argtypes = [cll, ci, cu, vp]
     lib.thc_kmeans.argtypes = [vp, vp, vp, cll, ci, vp, ci, cd, vp, ctypes.POINTER(KMeansStats)]
+    lib.thc_kmeans_noalloc.argtypes = lib.thc_kmeans.argtypes
     lib.thc_isdf.argtypes = [vp, vp, cll, ci, vp, ci, vp, vp, cd, vp, vp, vp,
                              ctypes.POINTER(IsdfStats)]
     for f in ("thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
-              "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf"):
+              "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_kmeans_noalloc"):
         getattr(lib, f).restype = ci
     _lib = lib
     return lib
@@ -218,6 +219,19 @@ class Context:
                                  threshold, _ptr(out_idx), ctypes.byref(stats))
         if raise_on_error:
             self._check(st, "thc_kmeans")
+        return out_idx, stats, st
+
+    def kmeans_noalloc(self, grid, rho, nmu, init_idx, max_it, threshold, out_idx=None,
+                       raise_on_error=True):
+        """thc_kmeans_noalloc: thc_kmeans on a fixed device scratch (no allocation)."""
+        ng = int(grid.shape[0])
+        if out_idx is None:
+            out_idx = np.zeros(nmu, np.int32)
+        stats = KMeansStats()
+        st = self.lib.thc_kmeans_noalloc(self.h, _ptr(grid), _ptr(rho), ng, nmu, _ptr(init_idx),
+                                         max_it, threshold, _ptr(out_idx), ctypes.byref(stats))
+        if raise_on_error:
+            self._check(st, "thc_kmeans_noalloc")
         return out_idx, stats, st
 
     def kmeans_history(self, n):

@@ -17,10 +17,6 @@
 #include "common.cuh"
 #include "isdf.cuh"
 
-struct thc_ctx {
-  thc::Ctx c;
-};
-
 namespace thc {
 
 void* ws_get(Ctx* c, Slot s, size_t bytes)

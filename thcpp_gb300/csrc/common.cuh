@@ -120,6 +120,11 @@ const void* to_device(Ctx* c, const void* p, size_t bytes, Slot staging, int* st
 
 }  // namespace thc
 
+// The opaque handle of the C ABI.
+struct thc_ctx {
+  thc::Ctx c;
+};
+
 #define THC_CUDA(c, call)                                                          \
   do {                                                                             \
     cudaError_t e_ = (call);                                                       \

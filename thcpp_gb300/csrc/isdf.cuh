@@ -15,9 +15,28 @@ int isdf_run_mixed(Ctx* c, const double* phi, long long ng, int no, const int* i
                    const int* mesh, const double* coul, double shift_rel, double* out_orb,
                    double* out_M, double* out_L, thc_isdf_stats* stats);
 
+// Scratch source of one k-means call: the context's grow-only workspace (base == nullptr)
+// or a fixed, caller-provided device region that is carved up in order (256-byte aligned);
+// a request that does not fit returns nullptr.
+struct KmAlloc {
+  Ctx* c = nullptr;
+  char* base = nullptr;
+  size_t cap = 0, used = 0;
+  void* get(Slot s, size_t bytes)
+  {
+    if (!base) return ws_get(c, s, bytes);
+    size_t off = (used + 255) & ~(size_t)255;
+    if (off > cap || bytes > cap - off) return nullptr;
+    used = off + bytes;
+    return base + off;
+  }
+};
+
+// With `fixed` set, every device buffer comes from that region: no device memory is
+// allocated, no CUDA graph is built and no profiling events are recorded.
 int kmeans_run(Ctx* c, const double* grid, const double* rho, long long ng, int nmu,
                const int* init, int max_it, double threshold, int* out_idx,
-               thc_kmeans_stats* stats);
+               thc_kmeans_stats* stats, KmAlloc* fixed = nullptr);
 
 int kmeans_history(Ctx* c, double* diff, double* pct, int n);
 

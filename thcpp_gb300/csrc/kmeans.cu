@@ -41,6 +41,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "isdf.cuh"
 #include "seqsum.cuh"
 
 namespace thc {
@@ -1125,17 +1126,29 @@ __global__ void km_sort(int* idx, int n, int npow2, int* dups)
 
 int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng, int nmu,
                const int* init_in, int max_it, double threshold, int* out_idx,
-               thc_kmeans_stats* stats)
+               thc_kmeans_stats* stats, KmAlloc* fixed)
 {
+  KmAlloc ws_alloc;
+  ws_alloc.c = c;
+  KmAlloc& al = fixed ? *fixed : ws_alloc;
   if (!grid_in || !rho_in || !init_in || !out_idx || ng <= 0 || nmu <= 0 || nmu > ng ||
       max_it < 1 || ng > 0x7fffffffLL)
     return set_error(c, THC_ERR_ARG, "thc_kmeans: invalid arguments");
   if (nmu > 16384) return set_error(c, THC_ERR_SHAPE, "thc_kmeans: nmu > 16384 unsupported");
   cudaStream_t s = c->stream;
   int st_status = 0;
-  const double* grid = (const double*)to_device(c, grid_in, sizeof(double) * 3 * ng,
-                                                WS_KM_IO, &st_status);
-  if (st_status) return st_status;
+  const double* grid = nullptr;
+  if (!fixed) {
+    grid = (const double*)to_device(c, grid_in, sizeof(double) * 3 * ng, WS_KM_IO, &st_status);
+    if (st_status) return st_status;
+  } else if (is_device_ptr(grid_in)) {
+    grid = grid_in;
+  } else {
+    double* gs = (double*)al.get(WS_KM_IO, sizeof(double) * 3 * ng);
+    if (!gs) return set_error(c, THC_ERR_NOMEM, "thc_kmeans: grid staging exceeds the scratch");
+    THC_CUDA(c, cudaMemcpyAsync(gs, grid_in, sizeof(double) * 3 * ng, cudaMemcpyHostToDevice, s));
+    grid = gs;
+  }
   // rho and the initial indices share a second staging area after the grid copy.
   const double* rho = nullptr;
   const int* init = nullptr;
@@ -1144,7 +1157,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     bool rd = is_device_ptr(rho_in), id = is_device_ptr(init_in);
     char* stage = nullptr;
     if (!rd || !id) {
-      stage = (char*)ws_get(c, WS_KM_IDX, rb + ib + 256);
+      stage = (char*)al.get(WS_KM_IDX, rb + ib + 256);
       if (!stage) return set_error(c, THC_ERR_NOMEM, "thc_kmeans: staging");
     }
     if (rd) rho = rho_in;
@@ -1163,22 +1176,22 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   b.ng = ng;
   b.nmu = nmu;
   b.nb = (int)cdiv(ng, kBP);
-  double* g64 = (double*)ws_get(c, WS_KM_GRID, sizeof(double) * 4 * ng);
-  float* g32 = (float*)ws_get(c, WS_KM_GRID32, sizeof(float) * 3 * ng);
-  double* cen = (double*)ws_get(c, WS_KM_CENT, sizeof(double) * 6 * nmu);
-  float* cen32 = (float*)ws_get(c, WS_KM_CENT32, sizeof(float) * 6 * nmu);
-  int* labels = (int*)ws_get(c, WS_KM_LABELS, sizeof(int) * 2 * ng);
-  int* hist = (int*)ws_get(c, WS_KM_HIST, sizeof(int) * (size_t)nmu * b.nb);
-  int* tot = (int*)ws_get(c, WS_KM_TOTAL, sizeof(int) * 2 * nmu);
-  int* member = (int*)ws_get(c, WS_KM_MEMBER, sizeof(int) * ng);
-  double* terms = (double*)ws_get(c, WS_KM_TERMS, sizeof(double) * 4 * nmu);
-  int* recheck = (int*)ws_get(c, WS_KM_RECHECK, sizeof(int) * ng);
-  KmState* st = (KmState*)ws_get(c, WS_KM_STATE, sizeof(KmState) + 64);
-  double* logb = (double*)ws_get(c, WS_KM_LOG, sizeof(double) * 2 * max_it);
+  double* g64 = (double*)al.get(WS_KM_GRID, sizeof(double) * 4 * ng);
+  float* g32 = (float*)al.get(WS_KM_GRID32, sizeof(float) * 3 * ng);
+  double* cen = (double*)al.get(WS_KM_CENT, sizeof(double) * 6 * nmu);
+  float* cen32 = (float*)al.get(WS_KM_CENT32, sizeof(float) * 6 * nmu);
+  int* labels = (int*)al.get(WS_KM_LABELS, sizeof(int) * 2 * ng);
+  int* hist = (int*)al.get(WS_KM_HIST, sizeof(int) * (size_t)nmu * b.nb);
+  int* tot = (int*)al.get(WS_KM_TOTAL, sizeof(int) * 2 * nmu);
+  int* member = (int*)al.get(WS_KM_MEMBER, sizeof(int) * ng);
+  double* terms = (double*)al.get(WS_KM_TERMS, sizeof(double) * 4 * nmu);
+  int* recheck = (int*)al.get(WS_KM_RECHECK, sizeof(int) * ng);
+  KmState* st = (KmState*)al.get(WS_KM_STATE, sizeof(KmState) + 64);
+  double* logb = (double*)al.get(WS_KM_LOG, sizeof(double) * 2 * max_it);
   int nch = (int)cdiv(ng, kMapChunk);
-  double* part_s = (double*)ws_get(c, WS_KM_PART, (sizeof(double) + sizeof(int)) * (size_t)nmu * nch + 64);
+  double* part_s = (double*)al.get(WS_KM_PART, (sizeof(double) + sizeof(int)) * (size_t)nmu * nch + 64);
   const int nbins_max = (int)std::max<long long>(1024, ng / 32);
-  int* permw = (int*)ws_get(c, WS_KM_PERM, sizeof(int) * (2 * (size_t)ng + 2 * (size_t)nbins_max));
+  int* permw = (int*)al.get(WS_KM_PERM, sizeof(int) * (2 * (size_t)ng + 2 * (size_t)nbins_max));
   if (!g64 || !g32 || !cen || !cen32 || !labels || !hist || !tot || !member || !terms ||
       !recheck || !st || !logb || !part_s || !permw)
     return set_error(c, THC_ERR_NOMEM, "thc_kmeans: workspace allocation failed");
@@ -1265,7 +1278,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     return THC_OK;
   };
   // A CUDA graph of kCheckEvery iterations, cached on the context for these buffers.
-  const bool graphs = c->use_graphs && !c->profile;
+  const bool graphs = c->use_graphs && !c->profile && !fixed;
   cudaGraphExec_t gexec = nullptr;
   if (graphs) {
     std::vector<long long> key = {ng, nmu, mixed, prune, (long long)(uintptr_t)g64,
@@ -1301,7 +1314,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
       c->launches += (mixed ? 6LL : 5LL) * kCheckEvery;  // kernels per captured iteration
     } else {
       for (int k = 0; k < nblock; k++) {
-        int rc = iteration(true);
+        int rc = iteration(!fixed);
         if (rc) return rc;
       }
     }
@@ -1347,7 +1360,9 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   if (didx != out_idx)
     THC_CUDA(c, cudaMemcpyAsync(out_idx, didx, sizeof(int) * nmu, cudaMemcpyDeviceToHost, s));
   THC_CUDA(c, cudaStreamSynchronize(s));
-  c->km_last_iters = hs.iter;
+  // The history of a fixed-scratch call lives in the shared region, which later calls
+  // overwrite: thc_kmeans_history reports none for it.
+  c->km_last_iters = fixed ? 0 : hs.iter;
   c->km_last_max_it = max_it;
   if (hs.bad_label) return set_error(c, THC_ERR_CUDA, "thc_kmeans: internal label out of range");
   if (hs.empty) {
