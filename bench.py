@@ -36,8 +36,14 @@ WORKLOADS = {
            "n_mu": 256, "mesh": [48, 48, 48]},
     "c3": {"workload": "diamond-64atom-72^3-no256-nmu2048", "n_g": 373248, "n_orb": 256,
            "n_mu": 2048, "mesh": [72, 72, 72]},
+    "c4": {"workload": "batch-48-random-cubic-cells-32^3..64^3-no16..200-nmu6..10xno",
+           "systems": 48},
 }
 WORKLOAD = "c2"
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per sliced-GEMM launch, mean of
+# the three launches of one factorisation, from one ncu capture of the workload; None where
+# no capture was taken.
+OZ_TRAFFIC = {"c2": (249.9e6 + 446.5e6 + 251.2e6) / 3.0, "c3": None}
 CONFIG = dict(WORKLOADS[WORKLOAD], kmeans_max_it=100, kmeans_threshold=1e-6,
               l2="flushed (256 MB write) before every timed step", parallelism="replicas")
 METRIC = "ISDF s/system on 1 GB300 (mixed precision; FP64 path reported beside)"
@@ -155,6 +161,77 @@ def run_reference(args):
     return 0
 
 
+def run_c4(args):
+    """The batched workload: 48 seeded random cubic systems, thc_factorize_batched against
+    the same 48 factorisations one after another on one context (mixed precision).
+
+    The batch spans several CUDA streams, so each step is timed on the host clock around a
+    device-wide synchronisation.  Inputs are resident in HBM before timing starts.
+    """
+    import torch
+    from thcpp_gb300 import batch, build, capi, synth
+    build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    nsys = args.c4_systems
+    t0 = time.perf_counter()
+    systems = [synth.c4_system(i) for i in range(nsys)]
+    gen_s = time.perf_counter() - t0
+    prec = capi.THC_PREC_MIXED
+    seq_arr = [batch.system_arrays(s, dev) for s in systems]
+    bat_arr = [batch.system_arrays(s, dev) for s in systems]
+    ctx = capi.Context(0, prec)
+
+    def run_seq():
+        st = batch.run_sequential(ctx, systems, seq_arr)
+        if any(x not in (capi.THC_OK, capi.THC_ERR_NOT_PD) for x in st):
+            raise RuntimeError(f"sequential statuses {st}")
+
+    def run_bat():
+        st, per = batch.run_batched(systems, bat_arr, prec, nstreams=args.c4_streams)
+        if st != capi.THC_OK:
+            raise RuntimeError(f"batched status {st}: {per}")
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            tot += time.perf_counter() - a
+        return tot / args.steps
+
+    launches0 = ctx.kernel_launches
+    t_seq = timed(run_seq)
+    seq_launches = (ctx.kernel_launches - launches0) // (args.steps + args.warmup)
+    t_bat = timed(run_bat)
+    same_idx = all(torch.equal(a["out_idx"], b["out_idx"]) for a, b in zip(seq_arr, bat_arr))
+    dm = max(float(torch.linalg.norm(a["out_M"] - b["out_M"]) / torch.linalg.norm(a["out_M"]))
+             for a, b in zip(seq_arr, bat_arr))
+    ctx.close()
+    line = {
+        "metric": "batched ISDF s/system on 1 GB300 (48 systems, mixed precision)",
+        "value": t_bat / nsys, "unit": "s/system", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_bat * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16-sliced/fp32/fp64",
+        "data": "synthetic (seeded random cubic cells, Gaussian s/p orbitals)",
+        "config": dict(WORKLOADS["c4"], systems=nsys, streams=args.c4_streams,
+                       l2="inputs of the batch (several GB) exceed L2",
+                       timing="host clock around device-synchronised batches"),
+        "sequential_s_per_system": t_seq / nsys,
+        "speedup_batched_vs_sequential": t_seq / t_bat,
+        "idx_identical": same_idx, "max_rel_diff_M_batched_vs_sequential": dm,
+        "gpu_launches": seq_launches,
+        "host_generation_s": gen_s,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -166,8 +243,12 @@ def main():
     ap.add_argument("--paths", default="mixed,fp64,e2e",
                     help="comma list of measured paths (a profiling run may keep only 'mixed')")
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS),
-                    help="c2 is the benchmark workload; c3 is reported separately")
+                    help="c2 is the benchmark workload; c3 and c4 (batch) are reported separately")
+    ap.add_argument("--c4-systems", type=int, default=48)
+    ap.add_argument("--c4-streams", type=int, default=8)
     args = ap.parse_args()
+    if args.workload == "c4" and args.impl != "reference":
+        return run_c4(args)
     global WORKLOAD, CONFIG
     WORKLOAD = args.workload
     CONFIG = dict(WORKLOADS[WORKLOAD], kmeans_max_it=100, kmeans_threshold=1e-6,
@@ -333,7 +414,8 @@ def main():
         roof = {"kernel": "ozgemm (sliced-BF16 tensor GEMM, mean over its 3 launches/system)",
                 "bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                 "frac": (achieved / bf16_peak) if achieved else None,
-                "peak_source": peak_src, "traffic": None,
+                "peak_source": peak_src, "traffic": OZ_TRAFFIC.get(args.workload),
+                "traffic_unit": "bytes per launch",
                 "share_of_step": (oz_ms / args.steps) / t_step if oz_n else None}
         cpu = None
         if not args.no_cpu_baseline:
@@ -354,7 +436,7 @@ def main():
                      "rel_err_M_mixed_vs_fp64": rel_err, "idx_identical": idx_same,
                      "dgemm_ms_per_system": dg_ms / max(args.fp64_steps, 1)},
             "kmeans": {"iterations": kst.iterations, "rechecked_points": int(kst.rechecked),
-                       "assign_ms_per_system": km_ms / args.steps},
+                       "assign_us_per_iteration": (1e3 * km_ms / km_n) if km_n else None},
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
         }
         # Whole-job s/system: ws replicas each factorised one system per step in t_step.

@@ -142,65 +142,81 @@ __device__ __forceinline__ double rsqrt_newton(double d)
 // Pivots at or below thr stop the factorisation (info = global 1-based index).
 // The inverse V is eliminated alongside the factor: at step j row j of V is scaled by
 // 1/L_jj and subtracted from the rows below (L V = I by forward substitution), so both
-// run on all threads with one pivot chain.
+// run on all threads with one pivot chain.  The next pivot's reciprocal square root is
+// taken by the thread that finishes updating that diagonal entry, while the other threads
+// are still updating (look-ahead): two barriers per step, and the long FP64 latency of the
+// pivot overlaps the FP64-throughput-bound update.
 __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, int n, int k0,
                                                       const double* thr_p, CholStatus* cs,
                                                       double* dinv)
 {
   if (cs->flag) return;
-  double thr = thr_p ? *thr_p : 0.0;
+  const double thr = thr_p ? *thr_p : 0.0;
   extern __shared__ double dsm[];                       // 2 x NB x (NB + 1) doubles
   double (*a)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm);
   double (*v)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm + NB * (NB + 1));
-  __shared__ double rinv;
+  __shared__ double rinv, pmin, pmax;
   __shared__ int bad;
   const int nb = min(NB, n - k0);
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads
   for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
     int r = e / NB, c = e % NB;
     a[r][c] = (r < nb && c < nb) ? A[(long long)(k0 + r) * ld + k0 + c] : (r == c ? 1.0 : 0.0);
     v[r][c] = r == c ? 1.0 : 0.0;
   }
-  if (threadIdx.x == 0) bad = 0;
-  // Pivot extremes stay in registers of thread 0 (no global traffic on the pivot chain).
-  double pmin = 0.0, pmax = 0.0;
-  if (threadIdx.x == 0) { pmin = cs->min_piv; pmax = cs->max_piv; }
-  __syncthreads();
-  for (int j = 0; j < nb; j++) {
-    if (threadIdx.x == 0) {
-      double d = a[j][j];
-      if (!(d > thr)) {
-        bad = 1;
-        cs->flag = 1;
-        cs->info = k0 + j + 1;
-        cs->min_piv = pmin;
-        cs->max_piv = pmax;
-      } else {
-        double y = rsqrt_newton(d);
-        a[j][j] = d * y;
-        rinv = y;
-        pmin = fmin(pmin, d);
-        pmax = fmax(pmax, d);
-      }
+  // One thread: check pivot j and publish 1/sqrt of it (or the breakdown).
+  auto pivot = [&](int j) {
+    const double d = a[j][j];
+    if (!(d > thr)) {
+      bad = 1;
+      cs->flag = 1;
+      cs->info = k0 + j + 1;
+    } else {
+      rinv = rsqrt_newton(d);
+      pmin = fmin(pmin, d);
+      pmax = fmax(pmax, d);
     }
-    __syncthreads();
-    if (bad) return;
+  };
+  if (threadIdx.x == 0) {
+    bad = 0;
+    pmin = cs->min_piv;
+    pmax = cs->max_piv;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && nb > 0) pivot(0);
+  __syncthreads();
+  for (int j = 0; j < nb && !bad; j++) {
     const double ri = rinv;
+    if (threadIdx.x == 0) a[j][j] *= ri;                  // d / sqrt(d)
     for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) a[i][j] *= ri;
     for (int c = threadIdx.x; c <= j; c += blockDim.x) v[j][c] *= ri;
     __syncthreads();
     // rows i > j: a[i][c] -= a[i][j] a[c][j] (j < c <= i) and v[i][c] -= a[i][j] v[j][c]
-    // (c <= j); together the columns 0..i of row i.
-    for (int i = j + 1 + ty; i < nb; i += 16) {
-      const double lij = a[i][j];
-      for (int c = tx; c <= i; c += 16) {
-        if (c <= j) v[i][c] = __fma_rn(-lij, v[j][c], v[i][c]);
-        else a[i][c] = __fma_rn(-lij, a[c][j], a[i][c]);
+    // (c <= j); together the columns 0..i of row i.  The (i, c) pairs are enumerated flat
+    // so that every warp-wide FP64 FMA has all 32 lanes busy: GB300 issues an FP64
+    // instruction at two lanes per clock whatever its active mask.
+    {
+      const int off = (j + 1) * (j + 2) / 2;                 // pairs of rows <= j
+      const int total = nb * (nb + 1) / 2 - off;
+      for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int x = e + off;
+        int i = (int)((sqrtf(8.f * (float)x + 1.f) - 1.f) * 0.5f);
+        while (i * (i + 1) / 2 > x) i--;
+        while ((i + 1) * (i + 2) / 2 <= x) i++;
+        const int c = x - i * (i + 1) / 2;
+        const bool inv = c <= j;
+        double* dst = inv ? &v[i][c] : &a[i][c];
+        const double src = inv ? v[j][c] : a[c][j];
+        *dst = __fma_rn(-a[i][j], src, *dst);
+        if (c == i && i == j + 1) pivot(i);                  // look-ahead pivot
       }
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) { cs->min_piv = pmin; cs->max_piv = pmax; }
+  if (threadIdx.x == 0) {
+    cs->min_piv = pmin;
+    cs->max_piv = pmax;
+  }
+  if (bad) return;
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     int r = e / nb, c = e % nb;
     A[(long long)(k0 + r) * ld + k0 + c] = c <= r ? a[r][c] : 0.0;

@@ -43,6 +43,7 @@
 #include "common.cuh"
 #include "isdf.cuh"
 #include "seqsum.cuh"
+#include "segsum.cuh"
 
 namespace thc {
 
@@ -838,32 +839,38 @@ __device__ double normdiff_terms(const KmBufs& b, const double* a, const double*
   return scale;
 }
 
-// One block of four warps per cluster.  All threads form the products rho_i * g_i of up to
-// kSumChunk members (each rounded on its own, as the reference's `rho[i] * grid[i*ndim]`),
-// then warp q adds quantity q (0 = w, 1 = x, 2 = y, 3 = z) strictly in ascending member
-// order with warp_seqsum, which rounds exactly as the reference's sequential loop
-// (src/kmeans.cpp:121-126).  The last block to finish (a ticket in the state) also takes the
-// convergence decision of the iteration: the normed difference approximated by a
-// fixed-order sum of squared centroid moves (relative deviation from the reference's value
-// below (3 N_mu + 8) u), evaluated exactly when within 1e-10 of the threshold.
-constexpr int kSumChunk = 512;
-constexpr int kSumThreads = 128;
-__global__ void __launch_bounds__(kSumThreads) km_sums(KmBufs b)
+// One block of four 128-thread groups per cluster.  All threads form the products
+// rho_i * g_i of up to kSegChunk members (each rounded on its own, as the reference's
+// `rho[i] * grid[i*ndim]`), then group q adds quantity q (0 = w, 1 = x, 2 = y, 3 = z)
+// strictly in ascending member order with group_seqsum, which rounds exactly as the
+// reference's sequential loop (src/kmeans.cpp:121-126).  The last block to finish (a ticket
+// in the state) also takes the convergence decision of the iteration: the normed difference
+// approximated by a fixed-order sum of squared centroid moves (relative deviation from the
+// reference's value below (3 N_mu + 8) u), evaluated exactly when within 1e-10 of the
+// threshold.
+constexpr int kSumThreads = 4 * kSegGroup;
+__global__ void __launch_bounds__(kSumThreads, 2) km_sums(KmBufs b)
 {
   KmState* st = b.st;
   if (st->done) return;
-  __shared__ double sv[4][kSumChunk];
+  __shared__ double sv[4][kSegChunk];
+  __shared__ SegScratch sc[4];
   __shared__ double res[4];
   __shared__ double red[32];
   __shared__ int last;
   const int it = st->iter;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = threadIdx.x / kSegGroup, gt = threadIdx.x % kSegGroup;
   const int k = blockIdx.x;
   const int nmu = b.nmu;
   const int s = b.start[k], n = b.total[k];
-  double acc = 0.0;
-  for (int base = 0; base < n; base += kSumChunk) {
-    const int cnt = min(kSumChunk, n - base);
+  if (gt == 0) {
+    sc[q].acc = 0.0;
+    sc[q].fall = 0;
+  }
+  for (int base = 0; base < n; base += kSegChunk) {
+    const int cnt = min(kSegChunk, n - base);
+    __syncthreads();
     for (int m = threadIdx.x; m < cnt; m += kSumThreads) {
       int i = b.member[s + base + m];
       double r = b.rho[i];
@@ -873,10 +880,10 @@ __global__ void __launch_bounds__(kSumThreads) km_sums(KmBufs b)
       sv[3][m] = __dmul_rn(r, b.gz[i]);
     }
     __syncthreads();
-    acc = warp_seqsum(acc, sv[warp], cnt);
-    __syncthreads();
+    group_seqsum(sv[q], cnt, gt, sc[q]);
   }
-  if (lane == 0) res[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x < 4) res[threadIdx.x] = sc[threadIdx.x].acc;
   __syncthreads();
   double* part = b.terms + 3 * (size_t)nmu;   // per-cluster squared move
   if (threadIdx.x == 0) {
@@ -1016,44 +1023,64 @@ __global__ void km_map_pruned(KmBufs b, const double* __restrict__ box, int ntil
   }
   for (int off = 16; off; off >>= 1) u = fmin(u, __shfl_xor_sync(0xffffffffu, u, off));
   double cut = u * (1.0 + 1e-9);
-  double bs = CUDART_INF, bm = CUDART_INF;
-  int bk = 0x7fffffff;
-  // Candidate tiles are found 32 at a time; the whole warp then scans each one (coalesced
-  // reads of the binned order, 8 points per lane).
-  for (int t0 = 0; t0 < ntiles; t0 += 32) {
-    int t = t0 + lane;
-    bool cand = false;
-    if (t < ntiles) {
-      double lb = 0.0;
-      for (int d = 0; d < 3; d++) {
-        double v = fmax(0.0, fmax(box[t * 6 + d] - c3[d], c3[d] - box[t * 6 + 3 + d]));
-        lb += v * v;
+  // The candidate tiles' points are scanned twice: first in FP32 for the smallest squared
+  // distance m, then in FP64 only for points whose FP32 squared distance is within
+  // m (1 + 1e-4) + slack32 -- a margin far above the FP32 rounding of the distances (the
+  // same one the pruned assign uses) -- so the FP64 pipe, which GB300 runs at two lanes
+  // per clock, sees a handful of points per centroid.
+  const float* cf = b.cen32 + (size_t)b.st->final_buf * 3 * b.nmu;
+  const float f3[3] = {cf[k], cf[b.nmu + k], cf[2 * b.nmu + k]};
+  float m32 = INFINITY;
+  for (int pass = 0; pass < 2; pass++) {
+    const float thr32 = pass ? m32 * (1.0f + 1e-4f) + (float)b.st->slack32 : 0.f;
+    double bs = CUDART_INF, bm = CUDART_INF;
+    int bk = 0x7fffffff;
+    for (int t0 = 0; t0 < ntiles; t0 += 32) {
+      int t = t0 + lane;
+      bool cand = false;
+      if (t < ntiles) {
+        double lb = 0.0;
+        for (int d = 0; d < 3; d++) {
+          double v = fmax(0.0, fmax(box[t * 6 + d] - c3[d], c3[d] - box[t * 6 + 3 + d]));
+          lb += v * v;
+        }
+        cand = lb <= cut;
       }
-      cand = lb <= cut;
-    }
-    unsigned m = __ballot_sync(0xffffffffu, cand);
-    while (m) {
-      int tt = t0 + __ffs(m) - 1;
-      m &= m - 1;
-      long long p0 = (long long)tt * 256, p1 = min((long long)b.ng, p0 + 256);
-      for (long long q = p0 + lane; q < p1; q += 32) {
-        int i = b.perm[q];
-        double d2 = d2_exact(b.gx[i], b.gy[i], b.gz[i], c3[0], c3[1], c3[2]);
-        // Any order: a candidate can win on a smaller sqrt or on an equal sqrt and a
-        // smaller index; equal sqrt values come from squared distances within a few ulps.
-        if (d2 <= bm * (1.0 + 0x1p-50)) {
-          double r = __dsqrt_rn(d2);
-          if (r < bs || (r == bs && i < bk)) { bs = r; bk = i; bm = fmin(bm, d2); }
+      unsigned m = __ballot_sync(0xffffffffu, cand);
+      while (m) {
+        int tt = t0 + __ffs(m) - 1;
+        m &= m - 1;
+        long long p0 = (long long)tt * 256, p1 = min((long long)b.ng, p0 + 256);
+        for (long long q = p0 + lane; q < p1; q += 32) {
+          int i = b.perm[q];
+          float dx = b.fx[i] - f3[0], dy = b.fy[i] - f3[1], dz = b.fz[i] - f3[2];
+          float d32 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+          if (!pass) {
+            m32 = fminf(m32, d32);
+            continue;
+          }
+          if (d32 > thr32) continue;
+          double d2 = d2_exact(b.gx[i], b.gy[i], b.gz[i], c3[0], c3[1], c3[2]);
+          // Any order: a candidate can win on a smaller sqrt or on an equal sqrt and a
+          // smaller index; equal sqrt values come from squared distances within a few ulps.
+          if (d2 <= bm * (1.0 + 0x1p-50)) {
+            double r = __dsqrt_rn(d2);
+            if (r < bs || (r == bs && i < bk)) { bs = r; bk = i; bm = fmin(bm, d2); }
+          }
         }
       }
     }
+    if (!pass) {
+      for (int off = 16; off; off >>= 1) m32 = fminf(m32, __shfl_xor_sync(0xffffffffu, m32, off));
+      continue;
+    }
+    for (int off = 16; off; off >>= 1) {
+      double s2 = __shfl_xor_sync(0xffffffffu, bs, off);
+      int k2 = __shfl_xor_sync(0xffffffffu, bk, off);
+      if (s2 < bs || (s2 == bs && k2 < bk)) { bs = s2; bk = k2; }
+    }
+    if (lane == 0) idx[k] = bk;
   }
-  for (int off = 16; off; off >>= 1) {
-    double s2 = __shfl_xor_sync(0xffffffffu, bs, off);
-    int k2 = __shfl_xor_sync(0xffffffffu, bk, off);
-    if (s2 < bs || (s2 == bs && k2 < bk)) { bs = s2; bk = k2; }
-  }
-  if (lane == 0) idx[k] = bk;
 }
 
 // map_to_grid, part 1: each thread owns one centroid and scans one chunk of grid points.
@@ -1278,7 +1305,9 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     return THC_OK;
   };
   // A CUDA graph of kCheckEvery iterations, cached on the context for these buffers.
-  const bool graphs = c->use_graphs && !c->profile && !fixed;
+  // Profiling keeps the graph: only iterations launched outside it (the tail when max_it is
+  // not a multiple of the graph length) get per-kernel events.
+  const bool graphs = c->use_graphs && !fixed;
   cudaGraphExec_t gexec = nullptr;
   if (graphs) {
     std::vector<long long> key = {ng, nmu, mixed, prune, (long long)(uintptr_t)g64,

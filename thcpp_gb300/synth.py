@@ -230,6 +230,15 @@ _SMOOTH = sorted({2**a * 3**b * 5**c * 7**d for a in range(7) for b in range(4)
                   if 32 <= 2**a * 3**b * 5**c * 7**d <= 64})
 
 
+# The reference exits on an empty k-means cluster (centroid weight < 1e-8).  The batched
+# workload keeps only systems whose k-means completes: the CPU restatement of the reference
+# k-means was run on each system; systems 1 and 23 complete with k-means seed 23 instead of
+# 21, and system 47 (a cell one third vacuum with N_mu = 132) empties a cluster for every
+# seed tried (21..79), so it is redrawn with its second draw.
+_C4_KMEANS_SEED = {1: 23, 23: 23}
+_C4_REDRAW = {47: 1}
+
+
 def c4_system(s: int) -> System:
     """System ``s`` (0..47) of the batched workload.
 
@@ -240,7 +249,7 @@ def c4_system(s: int) -> System:
     ``default_rng(4000 + s)`` in the order L, N_o, mesh, factor, positions, then the
     exponents and mixing matrix of :func:`make_system` from ``default_rng(5000 + s)``.
     """
-    rng = np.random.default_rng(4000 + s)
+    rng = np.random.default_rng(4000 + s + 100000 * _C4_REDRAW.get(s, 0))
     while True:
         edge = float(rng.uniform(6.0, 14.0))
         norb = int(rng.integers(16, 201))
@@ -264,7 +273,8 @@ def c4_system(s: int) -> System:
         if len(pos) == natom:
             break
     lat = edge * np.eye(3)
-    return make_system(f"c4_{s}", lat, np.array(pos), (n, n, n), norb, cfac, 5000 + s, 17 + 4)
+    return make_system(f"c4_{s}", lat, np.array(pos), (n, n, n), norb, cfac,
+                       5000 + s + 100000 * _C4_REDRAW.get(s, 0), _C4_KMEANS_SEED.get(s, 17 + 4))
 
 
 def write_orbital_file(system: System, path: str, half_rotate: bool = False) -> None:
