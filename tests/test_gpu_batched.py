@@ -27,7 +27,9 @@ def test_batched_matches_sequential(prec):
         st_seq = batch.run_sequential(ctx, systems, seq)
     st, st_bat = batch.run_batched(systems, bat, prec, nstreams=2)
     torch.cuda.synchronize()
-    assert st_seq == [capi.THC_OK] * len(systems)
+    # THC_ERR_NOT_PD (the reference's Cholesky warning on M; L is still written) is a result,
+    # not a failure: an M with eigenvalues below its mixed-precision error can report it.
+    assert all(x in (capi.THC_OK, capi.THC_ERR_NOT_PD) for x in st_seq)
     assert st == capi.THC_OK and st_bat == st_seq
     for s, a, b in zip(systems, seq, bat):
         assert torch.equal(a["out_idx"], b["out_idx"]), s.name

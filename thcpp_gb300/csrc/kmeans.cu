@@ -839,51 +839,66 @@ __device__ double normdiff_terms(const KmBufs& b, const double* a, const double*
   return scale;
 }
 
-// One block of four 128-thread groups per cluster.  All threads form the products
-// rho_i * g_i of up to kSegChunk members (each rounded on its own, as the reference's
-// `rho[i] * grid[i*ndim]`), then group q adds quantity q (0 = w, 1 = x, 2 = y, 3 = z)
-// strictly in ascending member order with group_seqsum, which rounds exactly as the
+// One block of four warps per cluster.  All threads gather up to kSumCap members and form
+// the products rho_i * g_i (each rounded on its own, as the reference's
+// `rho[i] * grid[i*ndim]`), then warp q adds quantity q (0 = w, 1 = x, 2 = y, 3 = z)
+// strictly in ascending member order with warp_segsum, which rounds exactly as the
 // reference's sequential loop (src/kmeans.cpp:121-126).  The last block to finish (a ticket
 // in the state) also takes the convergence decision of the iteration: the normed difference
 // approximated by a fixed-order sum of squared centroid moves (relative deviation from the
 // reference's value below (3 N_mu + 8) u), evaluated exactly when within 1e-10 of the
 // threshold.
-constexpr int kSumThreads = 4 * kSegGroup;
-__global__ void __launch_bounds__(kSumThreads, 2) km_sums(KmBufs b)
+constexpr int kSumThreads = 128;
+constexpr int kSumCap = 1024;
+__global__ void __launch_bounds__(kSumThreads) km_sums(KmBufs b)
 {
   KmState* st = b.st;
   if (st->done) return;
-  __shared__ double sv[4][kSegChunk];
+  __shared__ double sv[4][kSumCap];
   __shared__ SegScratch sc[4];
   __shared__ double res[4];
   __shared__ double red[32];
   __shared__ int last;
   const int it = st->iter;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int q = threadIdx.x / kSegGroup, gt = threadIdx.x % kSegGroup;
   const int k = blockIdx.x;
   const int nmu = b.nmu;
   const int s = b.start[k], n = b.total[k];
-  if (gt == 0) {
-    sc[q].acc = 0.0;
-    sc[q].fall = 0;
-  }
-  for (int base = 0; base < n; base += kSegChunk) {
-    const int cnt = min(kSegChunk, n - base);
+  double acc = 0.0;
+  for (int base = 0; base < n; base += kSumCap) {
+    const int cnt = min(kSumCap, n - base);
     __syncthreads();
-    for (int m = threadIdx.x; m < cnt; m += kSumThreads) {
-      int i = b.member[s + base + m];
-      double r = b.rho[i];
-      sv[0][m] = r;
-      sv[1][m] = __dmul_rn(r, b.gx[i]);
-      sv[2][m] = __dmul_rn(r, b.gy[i]);
-      sv[3][m] = __dmul_rn(r, b.gz[i]);
+    // Gather four members per thread per round: indices first, then the dependent loads.
+    for (int m0 = 0; m0 < cnt; m0 += 4 * kSumThreads) {
+      int id[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const int m = m0 + r * kSumThreads + threadIdx.x;
+        id[r] = m < cnt ? b.member[s + base + m] : -1;
+      }
+      double rv[4], xv[4], yv[4], zv[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        if (id[r] < 0) continue;
+        rv[r] = b.rho[id[r]];
+        xv[r] = b.gx[id[r]];
+        yv[r] = b.gy[id[r]];
+        zv[r] = b.gz[id[r]];
+      }
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        if (id[r] < 0) continue;
+        const int m = m0 + r * kSumThreads + threadIdx.x;
+        sv[0][m] = rv[r];
+        sv[1][m] = __dmul_rn(rv[r], xv[r]);
+        sv[2][m] = __dmul_rn(rv[r], yv[r]);
+        sv[3][m] = __dmul_rn(rv[r], zv[r]);
+      }
     }
     __syncthreads();
-    group_seqsum(sv[q], cnt, gt, sc[q]);
+    acc = warp_segsum(acc, sv[warp], cnt, sc[warp]);
   }
-  __syncthreads();
-  if (threadIdx.x < 4) res[threadIdx.x] = sc[threadIdx.x].acc;
+  if (lane == 0) res[warp] = acc;
   __syncthreads();
   double* part = b.terms + 3 * (size_t)nmu;   // per-cluster squared move
   if (threadIdx.x == 0) {
@@ -962,8 +977,9 @@ __global__ void __launch_bounds__(1024) km_normdiff_exact(KmBufs b)
   const double* a = b.cen + (size_t)((it + 1) & 1) * 3 * b.nmu;
   const double* c = b.cen + (size_t)(it & 1) * 3 * b.nmu;
   const double scale = normdiff_terms(b, a, c, b.terms, red);
+  __shared__ SegScratch scx;
   if (threadIdx.x < 32) {
-    double ssum = warp_seqsum(0.0, b.terms, 3 * b.nmu);
+    double ssum = warp_segsum(0.0, b.terms, 3 * b.nmu, scx);
     if (threadIdx.x == 0) out = __dmul_rn(scale, __dsqrt_rn(ssum));
   }
   __syncthreads();
