@@ -193,22 +193,40 @@ __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, i
     // rows i > j: a[i][c] -= a[i][j] a[c][j] (j < c <= i) and v[i][c] -= a[i][j] v[j][c]
     // (c <= j); together the columns 0..i of row i.  The (i, c) pairs are enumerated flat
     // so that every warp-wide FP64 FMA has all 32 lanes busy: GB300 issues an FP64
-    // instruction at two lanes per clock whatever its active mask.
+    // instruction at two lanes per clock whatever its active mask.  At most kSlots pairs
+    // per thread per step.
     {
+      // No element read in this step is written in it (the update reads column j of a and
+      // row j of v only), so each thread loads all its operands first, then issues its
+      // FMAs back to back, then stores: the dependent smem round trips of one element no
+      // longer serialise the next.
+      constexpr int kSlots = (NB * (NB + 1) / 2 + 255) / 256;
       const int off = (j + 1) * (j + 2) / 2;                 // pairs of rows <= j
       const int total = nb * (nb + 1) / 2 - off;
-      for (int e = threadIdx.x; e < total; e += blockDim.x) {
+      double* dst[kSlots];
+      double lij[kSlots], src[kSlots], cur[kSlots];
+      bool own_pivot = false;
+#pragma unroll
+      for (int q = 0; q < kSlots; q++) {
+        const int e = threadIdx.x + 256 * q;
+        dst[q] = nullptr;
+        if (e >= total) continue;
         const int x = e + off;
         int i = (int)((sqrtf(8.f * (float)x + 1.f) - 1.f) * 0.5f);
         while (i * (i + 1) / 2 > x) i--;
         while ((i + 1) * (i + 2) / 2 <= x) i++;
         const int c = x - i * (i + 1) / 2;
         const bool inv = c <= j;
-        double* dst = inv ? &v[i][c] : &a[i][c];
-        const double src = inv ? v[j][c] : a[c][j];
-        *dst = __fma_rn(-a[i][j], src, *dst);
-        if (c == i && i == j + 1) pivot(i);                  // look-ahead pivot
+        dst[q] = inv ? &v[i][c] : &a[i][c];
+        src[q] = inv ? v[j][c] : a[c][j];
+        lij[q] = a[i][j];
+        cur[q] = *dst[q];
+        own_pivot |= c == i && i == j + 1;
       }
+#pragma unroll
+      for (int q = 0; q < kSlots; q++)
+        if (dst[q]) *dst[q] = __fma_rn(-lij[q], src[q], cur[q]);
+      if (own_pivot) pivot(j + 1);                           // look-ahead pivot
     }
     __syncthreads();
   }

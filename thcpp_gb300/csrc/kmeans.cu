@@ -839,46 +839,60 @@ __device__ double normdiff_terms(const KmBufs& b, const double* a, const double*
   return scale;
 }
 
-// One block of four warps per cluster.  All threads gather up to kSumCap members and form
-// the products rho_i * g_i (each rounded on its own, as the reference's
-// `rho[i] * grid[i*ndim]`), then warp q adds quantity q (0 = w, 1 = x, 2 = y, 3 = z)
-// strictly in ascending member order with warp_segsum, which rounds exactly as the
-// reference's sequential loop (src/kmeans.cpp:121-126).  The last block to finish (a ticket
-// in the state) also takes the convergence decision of the iteration: the normed difference
-// approximated by a fixed-order sum of squared centroid moves (relative deviation from the
-// reference's value below (3 N_mu + 8) u), evaluated exactly when within 1e-10 of the
-// threshold.
-constexpr int kSumThreads = 128;
-constexpr int kSumCap = 1024;
+// One block of sixteen warps per cluster.  All threads gather up to kSumCap members and
+// form the products rho_i * g_i (each rounded on its own, as the reference's
+// `rho[i] * grid[i*ndim]`).  Quantity q (0 = w, 1 = x, 2 = y, 3 = z) is summed strictly in
+// ascending member order, rounding exactly as the reference's sequential loop
+// (src/kmeans.cpp:121-126): every 256-term window of every quantity gets its own warp for
+// the parallel part (seg_build, steered by an FP32 estimate of the running sum at the
+// window's start), then one warp per quantity walks its windows in order (seg_walk) with
+// the exact running sum.  The last block to finish (a ticket in the state) also takes the
+// convergence decision of the iteration: the normed difference approximated by a
+// fixed-order sum of squared centroid moves (relative deviation from the reference's value
+// below (3 N_mu + 8) u), evaluated exactly when within 1e-10 of the threshold.
+constexpr int kSumWin = kSegWin;                  // terms per window
+constexpr int kSumWins = 4;                       // windows per quantity and chunk
+constexpr int kSumCap = kSumWin * kSumWins;       // members per chunk
+constexpr int kSumThreads = 32 * 4 * kSumWins;    // one warp per (quantity, window)
+struct SumSmem {
+  double sv[4][kSumCap];
+  SegScratch tab[4][kSumWins];
+  float wsum[4][kSumWins];
+  double acc[4];
+  double res[4];
+  double red[32];
+  int last;
+};
 __global__ void __launch_bounds__(kSumThreads) km_sums(KmBufs b)
 {
   KmState* st = b.st;
   if (st->done) return;
-  __shared__ double sv[4][kSumCap];
-  __shared__ SegScratch sc[4];
-  __shared__ double res[4];
-  __shared__ double red[32];
-  __shared__ int last;
+  extern __shared__ __align__(16) unsigned char sum_smem[];
+  SumSmem& sm = *reinterpret_cast<SumSmem*>(sum_smem);
+  double* res = sm.res;
+  double* red = sm.red;
+  int& last = sm.last;
   const int it = st->iter;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tq = warp / kSumWins, tw = warp % kSumWins;   // this warp's window task
   const int k = blockIdx.x;
   const int nmu = b.nmu;
   const int s = b.start[k], n = b.total[k];
-  double acc = 0.0;
+  if (threadIdx.x < 4) sm.acc[threadIdx.x] = 0.0;
   for (int base = 0; base < n; base += kSumCap) {
     const int cnt = min(kSumCap, n - base);
     __syncthreads();
-    // Gather four members per thread per round: indices first, then the dependent loads.
-    for (int m0 = 0; m0 < cnt; m0 += 4 * kSumThreads) {
-      int id[4];
+    // Gather two members per thread: indices first, then the dependent loads.
+    {
+      int id[2];
 #pragma unroll
-      for (int r = 0; r < 4; r++) {
-        const int m = m0 + r * kSumThreads + threadIdx.x;
+      for (int r = 0; r < 2; r++) {
+        const int m = r * kSumThreads + threadIdx.x;
         id[r] = m < cnt ? b.member[s + base + m] : -1;
       }
-      double rv[4], xv[4], yv[4], zv[4];
+      double rv[2], xv[2], yv[2], zv[2];
 #pragma unroll
-      for (int r = 0; r < 4; r++) {
+      for (int r = 0; r < 2; r++) {
         if (id[r] < 0) continue;
         rv[r] = b.rho[id[r]];
         xv[r] = b.gx[id[r]];
@@ -886,19 +900,41 @@ __global__ void __launch_bounds__(kSumThreads) km_sums(KmBufs b)
         zv[r] = b.gz[id[r]];
       }
 #pragma unroll
-      for (int r = 0; r < 4; r++) {
+      for (int r = 0; r < 2; r++) {
         if (id[r] < 0) continue;
-        const int m = m0 + r * kSumThreads + threadIdx.x;
-        sv[0][m] = rv[r];
-        sv[1][m] = __dmul_rn(rv[r], xv[r]);
-        sv[2][m] = __dmul_rn(rv[r], yv[r]);
-        sv[3][m] = __dmul_rn(rv[r], zv[r]);
+        const int m = r * kSumThreads + threadIdx.x;
+        sm.sv[0][m] = rv[r];
+        sm.sv[1][m] = __dmul_rn(rv[r], xv[r]);
+        sm.sv[2][m] = __dmul_rn(rv[r], yv[r]);
+        sm.sv[3][m] = __dmul_rn(rv[r], zv[r]);
       }
     }
     __syncthreads();
-    acc = warp_segsum(acc, sv[warp], cnt, sc[warp]);
+    const int w0 = tw * kSumWin;
+    const int wcnt = max(0, min(kSumWin, cnt - w0));
+    {   // FP32 estimate of the window's sum (it only steers the binade prediction)
+      float f = 0.f;
+      for (int i = lane; i < wcnt; i += 32) f += (float)sm.sv[tq][w0 + i];
+      for (int off = 16; off; off >>= 1) f += __shfl_xor_sync(0xffffffffu, f, off);
+      if (lane == 0) sm.wsum[tq][tw] = f;
+    }
+    __syncthreads();
+    if (wcnt > 0) {
+      double pred = sm.acc[tq];
+      for (int v = 0; v < tw; v++) pred += (double)sm.wsum[tq][v];
+      seg_build(pred, &sm.sv[tq][w0], wcnt, sm.tab[tq][tw]);
+    }
+    __syncthreads();
+    if (warp < 4) {
+      double acc = sm.acc[warp];
+      for (int v = 0; v < kSumWins && v * kSumWin < cnt; v++)
+        acc = seg_walk(acc, &sm.sv[warp][v * kSumWin], min(kSumWin, cnt - v * kSumWin),
+                       sm.tab[warp][v]);
+      if (lane == 0) sm.acc[warp] = acc;
+    }
   }
-  if (lane == 0) res[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x < 4) res[threadIdx.x] = sm.acc[threadIdx.x];
   __syncthreads();
   double* part = b.terms + 3 * (size_t)nmu;   // per-cluster squared move
   if (threadIdx.x == 0) {
@@ -1287,6 +1323,8 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     THC_CUDA(c, cudaFuncSetAttribute(km_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
     THC_CUDA(c, cudaFuncSetAttribute(km_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
   }
+  THC_CUDA(c, cudaFuncSetAttribute(km_sums, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sizeof(SumSmem)));
   int* hflag = (int*)c->pinned;
   const int kCheckEvery = 8;
   // One k-means iteration; every kernel reads the iteration index from device state and
@@ -1316,7 +1354,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     THC_LAUNCHED(c, "km_colscan");
     km_scatter<<<b.nb, 256, hist_smem, s>>>(b);
     THC_LAUNCHED(c, "km_scatter");
-    km_sums<<<nmu, kSumThreads, 0, s>>>(b);
+    km_sums<<<nmu, kSumThreads, sizeof(SumSmem), s>>>(b);
     THC_LAUNCHED(c, "km_sums");
     return THC_OK;
   };

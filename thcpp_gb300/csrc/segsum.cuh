@@ -35,6 +35,7 @@ constexpr int kSegMax = 64;                  // segments per window before falli
 
 // Per-warp shared scratch: the segment table of the current window.
 struct SegScratch {
+  int nseg;                    // segments of the window, -1: walk it term by term
   int seg_pos[kSegMax];
   int seg_e[kSegMax];
   long long seg_c0[kSegMax];   // -1: the segment holds an invalid step
@@ -51,184 +52,216 @@ __device__ __forceinline__ void seg_compose(long long x0, long long x1, long lon
   y1 = n1;
 }
 
-// The parity map of one non-start term t on the grid of biased exponent e.
+// The parity map of one non-start term t (finite, non-negative) on the grid of biased
+// exponent e, without branches so that the eight terms of a lane overlap.  A term of at
+// least 2^52 grid units (shift <= 0) cannot stay inside the binade: flagged invalid.
 __device__ __forceinline__ void seg_term(double t, int e, long long& c0, long long& c1, bool& bad)
 {
-  bool tie;
-  long long k = seqsum_units(t, e - 1075, tie);
-  bad = k >= (1LL << 53);
-  if (bad) k = 0;
-  c0 = tie ? k + (k & 1) : k;
-  c1 = tie ? k + ((k + 1) & 1) : k;
+  const unsigned long long tb = (unsigned long long)__double_as_longlong(t);
+  const int et = (int)((tb >> 52) & 0x7ff);
+  unsigned long long m = tb & ((1ULL << 52) - 1);
+  if (et) m |= 1ULL << 52;
+  const int sh = e - max(et, 1);                 // t = m 2^(-sh) grid units
+  bad = sh <= 0;
+  const int shc = min(max(sh, 1), 63);
+  const unsigned long long kf = m >> shc;
+  const unsigned long long rem = m & ((1ULL << shc) - 1);
+  const unsigned long long half = 1ULL << (shc - 1);
+  const bool tie = rem == half;
+  const long long k = (long long)(kf + (rem > half ? 1 : 0));
+  const long long f = (long long)kf;
+  c0 = tie ? f + (f & 1) : k;
+  c1 = tie ? f + ((f + 1) & 1) : k;
+}
+
+// Phases 1-3 for one window of cnt <= kSegWin terms: the segment table in sc (sc.nseg = -1
+// when the window must be walked term by term).  acc_pred only steers the binade
+// prediction; it need not be the exact running sum.  One full warp.
+__device__ __noinline__ void seg_build(double acc_pred, const double* tw, int cnt, SegScratch& sc)
+{
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int i0 = lane * kSegPer;
+  auto term = [&](int u) -> double { return i0 + u < cnt ? tw[i0 + u] : 0.0; };
+  // ---- 1. sanity and the binade prediction from an integer prefix sum: every term
+  //         truncated to units of 2^U, U chosen from the largest exponent so that the
+  //         window's sum stays below 2^62 units (no FP64 instruction).
+  bool odd = false;
+  int emax = (int)((__double_as_longlong(acc_pred) >> 52) & 0x7ff);
+#pragma unroll
+  for (int u = 0; u < kSegPer; u++) {
+    const long long bb = __double_as_longlong(term(u));
+    const int et = (int)((bb >> 52) & 0x7ff);
+    odd |= bb < 0 || et == 0x7ff;
+    emax = max(emax, et);
+  }
+  if (__any_sync(full, odd) || __double_as_longlong(acc_pred) < 0) {
+    if (lane == 0) sc.nseg = -1;
+    __syncwarp();
+    return;
+  }
+#pragma unroll
+  for (int off = 16; off; off >>= 1) emax = max(emax, __shfl_xor_sync(full, emax, off));
+  if (emax == 0) {             // zero or subnormal terms only: rare, plain walk
+    if (lane == 0) sc.nseg = -1;
+    __syncwarp();
+    return;
+  }
+  // Sum < 257 * 2^(emax - 1022) < 2^(emax - 1013); a unit is 2^(emax - 1075), so the sum has
+  // at most 62 integer bits and the truncation error of a prefix is below 2^8 units.
+  const int U = emax - 1075;
+  auto units = [&](double x) -> long long {
+    const long long xb = __double_as_longlong(x);
+    const int ex = (int)((xb >> 52) & 0x7ff);
+    long long m = xb & ((1LL << 52) - 1);
+    if (ex) m |= 1LL << 52;
+    const int sh = (ex ? ex : 1) - 1075 - U;   // x = m 2^sh units, sh <= 0
+    return sh <= -63 ? 0 : (m >> (-sh));
+  };
+  long long loc[kSegPer];
+  long long run = 0;
+#pragma unroll
+  for (int u = 0; u < kSegPer; u++) {
+    run += units(term(u));
+    loc[u] = run;
+  }
+  long long incl = run;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    long long y = __shfl_up_sync(full, incl, off);
+    if (lane >= off) incl += y;
+  }
+  const long long base = units(acc_pred) + incl - run;
+  int E[kSegPer];
+#pragma unroll
+  for (int u = 0; u < kSegPer; u++) {
+    const long long P = base + loc[u];
+    E[u] = P > 0 ? (63 - __clzll(P)) + U + 1023 : 0;
+  }
+  int prev_e = __shfl_up_sync(full, E[kSegPer - 1], 1);
+  if (lane == 0) prev_e = -1;
+  // ---- 2. segment starts, the lane's segmented composite, the warp's segmented scan
+  unsigned stm = 0;
+#pragma unroll
+  for (int u = 0; u < kSegPer; u++) {
+    const int pe = u ? E[u - 1] : prev_e;
+    if (i0 + u < cnt && (i0 + u == 0 || E[u] != pe)) stm |= 1u << u;
+  }
+  long long a0 = 0, a1 = 0;
+  int af = 0;                  // bit 0: a segment starts in the lane, bit 1: invalid step
+#pragma unroll
+  for (int u = 0; u < kSegPer; u++) {
+    if (i0 + u >= cnt) continue;
+    if (stm >> u & 1) {
+      a0 = a1 = 0;
+      af = 1;
+    } else {
+      long long c0, c1;
+      bool bad;
+      seg_term(term(u), E[u], c0, c1, bad);
+      seg_compose(a0, a1, c0, c1);
+      a0 = c0;
+      a1 = c1;
+      if (bad) af |= 2;
+    }
+  }
+  // (x then y) = y if y starts a segment, else their composite.
+  long long s0 = a0, s1 = a1;
+  int sf = af, sn = __popc(stm);
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    long long x0 = __shfl_up_sync(full, s0, off), x1 = __shfl_up_sync(full, s1, off);
+    int xf = __shfl_up_sync(full, sf, off), xn = __shfl_up_sync(full, sn, off);
+    if (lane >= off) {
+      if (!(sf & 1)) {
+        seg_compose(x0, x1, s0, s1);
+        sf = (xf & 1) | ((xf | sf) & 2);
+      }
+      sn += xn;
+    }
+  }
+  long long e0 = __shfl_up_sync(full, s0, 1), e1 = __shfl_up_sync(full, s1, 1);
+  int ef = __shfl_up_sync(full, sf, 1), en = __shfl_up_sync(full, sn, 1);
+  if (lane == 0) { e0 = e1 = 0; ef = 0; en = 0; }
+  const int total = __shfl_sync(full, sn, 31);
+  if (total > kSegMax) {
+    if (lane == 0) sc.nseg = -1;
+    __syncwarp();
+    return;
+  }
+  // ---- 3. segment table: start position and exponent, end composite
+  {
+    unsigned next_start = __shfl_down_sync(full, stm & 1, 1);
+    if (lane == 31) next_start = 0;
+    int sidx = en - 1;
+    long long c0 = e0, c1 = e1;
+    bool cbad = (ef & 2) != 0;
+#pragma unroll
+    for (int u = 0; u < kSegPer; u++) {
+      const int i = i0 + u;
+      if (i >= cnt) continue;
+      if (stm >> u & 1) {
+        sidx++;
+        sc.seg_pos[sidx] = i;
+        sc.seg_e[sidx] = E[u];
+        c0 = c1 = 0;
+        cbad = false;
+      } else {
+        long long d0, d1;
+        bool bad;
+        seg_term(term(u), E[u], d0, d1, bad);
+        seg_compose(c0, c1, d0, d1);
+        c0 = d0;
+        c1 = d1;
+        cbad |= bad;
+      }
+      const bool end = i == cnt - 1 || (u + 1 < kSegPer ? (stm >> (u + 1) & 1) : next_start);
+      if (end) {
+        sc.seg_c0[sidx] = cbad ? -1 : c0;
+        sc.seg_c1[sidx] = c1;
+      }
+    }
+  }
+  if (lane == 0) sc.nseg = total;
+  __syncwarp();
+}
+
+// Phase 4 for one window: the exact running sum acc advanced over the window's terms with
+// the segment table built by seg_build.  One full warp; all lanes get the result.
+__device__ __noinline__ double seg_walk(double acc, const double* tw, int cnt, const SegScratch& sc)
+{
+  const long long kLo = 1LL << 52, kHi = 1LL << 53;
+  const int total = sc.nseg;
+  if (total < 0) return warp_seqsum(acc, tw, cnt);
+  // ---- 4. walk the segments (all lanes alike)
+  for (int j = 0; j < total; j++) {
+    const int a = sc.seg_pos[j];
+    const int bnd = (j + 1 < total ? sc.seg_pos[j + 1] : cnt) - 1;
+    acc = __dadd_rn(acc, tw[a]);
+    if (bnd == a) continue;
+    const long long ab = __double_as_longlong(acc);
+    const int ea = (int)((ab >> 52) & 0x7ff);
+    const long long S = (ab & (kLo - 1)) + kLo;
+    const long long c0 = sc.seg_c0[j];
+    const long long R = S + ((S & 1) ? sc.seg_c1[j] : c0);
+    if (ab > 0 && ea >= 1 && ea < 0x7fe && ea == sc.seg_e[j] && c0 >= 0 && R < kHi) {
+      acc = __longlong_as_double(((long long)ea << 52) | (R - kLo));
+    } else {
+      acc = warp_seqsum(acc, tw + a + 1, cnt - a - 1);
+      break;
+    }
+  }
+  return acc;
 }
 
 // acc + t[0] + ... + t[n-1] evaluated left to right in FP64 round-to-nearest by one full
 // warp (all lanes get the result); t in shared or global memory, sc private to the warp.
 __device__ __noinline__ double warp_segsum(double acc, const double* t, int n, SegScratch& sc)
 {
-  const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const int i0 = lane * kSegPer;
-  const long long kLo = 1LL << 52, kHi = 1LL << 53;
   for (int w0 = 0; w0 < n; w0 += kSegWin) {
     const int cnt = min(kSegWin, n - w0);
-    const double* tw = t + w0;
-    auto term = [&](int u) -> double { return i0 + u < cnt ? tw[i0 + u] : 0.0; };
-    // ---- 1. sanity and the binade prediction from an integer prefix sum: every term
-    //         truncated to units of 2^U, U chosen from the largest exponent so that the
-    //         window's sum stays below 2^62 units (no FP64 instruction).
-    bool odd = false;
-    int emax = (int)((__double_as_longlong(acc) >> 52) & 0x7ff);
-#pragma unroll
-    for (int u = 0; u < kSegPer; u++) {
-      const long long bb = __double_as_longlong(term(u));
-      const int et = (int)((bb >> 52) & 0x7ff);
-      odd |= bb < 0 || et == 0x7ff;
-      emax = max(emax, et);
-    }
-    if (__any_sync(full, odd) || __double_as_longlong(acc) < 0) {
-      acc = warp_seqsum(acc, tw, cnt);
-      continue;
-    }
-#pragma unroll
-    for (int off = 16; off; off >>= 1) emax = max(emax, __shfl_xor_sync(full, emax, off));
-    if (emax == 0) {             // zero or subnormal terms only: rare, plain walk
-      acc = warp_seqsum(acc, tw, cnt);
-      continue;
-    }
-    // Sum < 257 * 2^(emax - 1022) < 2^(emax - 1013); a unit is 2^(emax - 1075), so the sum has
-    // at most 62 integer bits and the truncation error of a prefix is below 2^8 units.
-    const int U = emax - 1075;
-    auto units = [&](double x) -> long long {
-      const long long xb = __double_as_longlong(x);
-      const int ex = (int)((xb >> 52) & 0x7ff);
-      long long m = xb & ((1LL << 52) - 1);
-      if (ex) m |= 1LL << 52;
-      const int sh = (ex ? ex : 1) - 1075 - U;   // x = m 2^sh units, sh <= 0
-      return sh <= -63 ? 0 : (m >> (-sh));
-    };
-    long long loc[kSegPer];
-    long long run = 0;
-#pragma unroll
-    for (int u = 0; u < kSegPer; u++) {
-      run += units(term(u));
-      loc[u] = run;
-    }
-    long long incl = run;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      long long y = __shfl_up_sync(full, incl, off);
-      if (lane >= off) incl += y;
-    }
-    const long long base = units(acc) + incl - run;
-    int E[kSegPer];
-#pragma unroll
-    for (int u = 0; u < kSegPer; u++) {
-      const long long P = base + loc[u];
-      E[u] = P > 0 ? (63 - __clzll(P)) + U + 1023 : 0;
-    }
-    int prev_e = __shfl_up_sync(full, E[kSegPer - 1], 1);
-    if (lane == 0) prev_e = -1;
-    // ---- 2. segment starts, the lane's segmented composite, the warp's segmented scan
-    unsigned stm = 0;
-#pragma unroll
-    for (int u = 0; u < kSegPer; u++) {
-      const int pe = u ? E[u - 1] : prev_e;
-      if (i0 + u < cnt && (i0 + u == 0 || E[u] != pe)) stm |= 1u << u;
-    }
-    long long a0 = 0, a1 = 0;
-    int af = 0;                  // bit 0: a segment starts in the lane, bit 1: invalid step
-#pragma unroll
-    for (int u = 0; u < kSegPer; u++) {
-      if (i0 + u >= cnt) continue;
-      if (stm >> u & 1) {
-        a0 = a1 = 0;
-        af = 1;
-      } else {
-        long long c0, c1;
-        bool bad;
-        seg_term(term(u), E[u], c0, c1, bad);
-        seg_compose(a0, a1, c0, c1);
-        a0 = c0;
-        a1 = c1;
-        if (bad) af |= 2;
-      }
-    }
-    // (x then y) = y if y starts a segment, else their composite.
-    long long s0 = a0, s1 = a1;
-    int sf = af, sn = __popc(stm);
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      long long x0 = __shfl_up_sync(full, s0, off), x1 = __shfl_up_sync(full, s1, off);
-      int xf = __shfl_up_sync(full, sf, off), xn = __shfl_up_sync(full, sn, off);
-      if (lane >= off) {
-        if (!(sf & 1)) {
-          seg_compose(x0, x1, s0, s1);
-          sf = (xf & 1) | ((xf | sf) & 2);
-        }
-        sn += xn;
-      }
-    }
-    long long e0 = __shfl_up_sync(full, s0, 1), e1 = __shfl_up_sync(full, s1, 1);
-    int ef = __shfl_up_sync(full, sf, 1), en = __shfl_up_sync(full, sn, 1);
-    if (lane == 0) { e0 = e1 = 0; ef = 0; en = 0; }
-    const int total = __shfl_sync(full, sn, 31);
-    if (total > kSegMax) {
-      acc = warp_seqsum(acc, tw, cnt);
-      continue;
-    }
-    // ---- 3. segment table: start position and exponent, end composite
-    {
-      unsigned next_start = __shfl_down_sync(full, stm & 1, 1);
-      if (lane == 31) next_start = 0;
-      int sidx = en - 1;
-      long long c0 = e0, c1 = e1;
-      bool cbad = (ef & 2) != 0;
-#pragma unroll
-      for (int u = 0; u < kSegPer; u++) {
-        const int i = i0 + u;
-        if (i >= cnt) continue;
-        if (stm >> u & 1) {
-          sidx++;
-          sc.seg_pos[sidx] = i;
-          sc.seg_e[sidx] = E[u];
-          c0 = c1 = 0;
-          cbad = false;
-        } else {
-          long long d0, d1;
-          bool bad;
-          seg_term(term(u), E[u], d0, d1, bad);
-          seg_compose(c0, c1, d0, d1);
-          c0 = d0;
-          c1 = d1;
-          cbad |= bad;
-        }
-        const bool end = i == cnt - 1 || (u + 1 < kSegPer ? (stm >> (u + 1) & 1) : next_start);
-        if (end) {
-          sc.seg_c0[sidx] = cbad ? -1 : c0;
-          sc.seg_c1[sidx] = c1;
-        }
-      }
-    }
-    __syncwarp();
-    // ---- 4. walk the segments (all lanes alike)
-    for (int j = 0; j < total; j++) {
-      const int a = sc.seg_pos[j];
-      const int bnd = (j + 1 < total ? sc.seg_pos[j + 1] : cnt) - 1;
-      acc = __dadd_rn(acc, tw[a]);
-      if (bnd == a) continue;
-      const long long ab = __double_as_longlong(acc);
-      const int ea = (int)((ab >> 52) & 0x7ff);
-      const long long S = (ab & (kLo - 1)) + kLo;
-      const long long c0 = sc.seg_c0[j];
-      const long long R = S + ((S & 1) ? sc.seg_c1[j] : c0);
-      if (ab > 0 && ea >= 1 && ea < 0x7fe && ea == sc.seg_e[j] && c0 >= 0 && R < kHi) {
-        acc = __longlong_as_double(((long long)ea << 52) | (R - kLo));
-      } else {
-        acc = warp_seqsum(acc, tw + a + 1, cnt - a - 1);
-        break;
-      }
-    }
+    seg_build(acc, t + w0, cnt, sc);
+    acc = seg_walk(acc, t + w0, cnt, sc);
     __syncwarp();
   }
   return acc;
