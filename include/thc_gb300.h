@@ -183,6 +183,7 @@ typedef struct thc_system {
   int status;
   thc_kmeans_stats kmeans_stats;
   thc_isdf_stats isdf_stats;
+  char error[192];          /* the worker context's last error message when status != 0 */
 } thc_system;
 
 /*

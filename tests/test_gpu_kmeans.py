@@ -61,6 +61,41 @@ def test_kmeans_rounding_stress(request, prec):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_kmeans_context_reuse_across_sizes(request, prec):
+    """One context, systems of different sizes in turn: workspace slots grow and move, and
+    the cached iteration graph must follow them."""
+    ctx = _ctx(request, prec)
+    for name in ["tiny", "c1", "tiny", "c2", "c1", "tiny"]:
+        s = system(name)
+        ref = oracle.kmeans_system(s)
+        init = capi.initial_indices(s.ng, s.nmu, s.rng_seed)
+        idx, st, status = ctx.kmeans(s.grid, s.density, s.nmu, init, s.max_it, s.threshold)
+        assert status == 0 and np.array_equal(idx, ref.idx), name
+        assert st.final_diff == ref.diff, name
+
+
+_C4_4 = {}
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_kmeans_pruned_repeatable(request, prec):
+    """A large cell with few, big clusters (C4 system 4: 157,464 points, 216 centroids),
+    three runs in a row: identical to the oracle every time (the pruned assign's shared
+    candidate list must be complete before any thread scans it)."""
+    from thcpp_gb300 import synth
+    if "s" not in _C4_4:
+        _C4_4["s"] = synth.c4_system(4)
+        _C4_4["ref"] = oracle.kmeans_system(_C4_4["s"])
+    s, ref = _C4_4["s"], _C4_4["ref"]
+    ctx = _ctx(request, prec)
+    init = capi.initial_indices(s.ng, s.nmu, s.rng_seed)
+    for _ in range(3):
+        idx, st, status = ctx.kmeans(s.grid, s.density, s.nmu, init, s.max_it, s.threshold)
+        assert status == 0 and np.array_equal(idx, ref.idx)
+        assert st.iterations == ref.iters and st.final_diff == ref.diff
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_kmeans_empty_cluster(request, prec):
     grid = np.array([[0.0, 0, 0], [1.0, 0, 0], [5.0, 0, 0]])
     rho = np.array([1.0, 1.0, 0.0])

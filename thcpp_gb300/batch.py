@@ -44,16 +44,20 @@ def batch_entry(s, arrs, shift_rel=-1.0):
 
 def run_sequential(ctx, systems, arrays):
     """One system after the other on one context: the sequential per-system baseline."""
-    statuses = []
+    statuses, times = [], []
     for s, a in zip(systems, arrays):
-        _, _, st = ctx.kmeans(a["grid"], a["rho"], s.nmu, a["init_idx"], s.max_it, s.threshold,
-                              out_idx=a["out_idx"], raise_on_error=False)
+        _, kst, st = ctx.kmeans(a["grid"], a["rho"], s.nmu, a["init_idx"], s.max_it,
+                                s.threshold, out_idx=a["out_idx"], raise_on_error=False)
+        ims = 0.0
         if st == capi.THC_OK:
             r = ctx.isdf(a["phi"], a["out_idx"], s.mesh, a["coulG"], out_M=a["out_M"],
                          out_L=a["out_L"], out_orbitals=a["out_orbitals"],
                          raise_on_error=False)
             st = r["status"]
+            ims = r["stats"].device_ms
         statuses.append(st)
+        times.append((kst.device_ms, ims))
+    run_sequential.times = times
     return statuses
 
 
@@ -62,4 +66,5 @@ def run_batched(systems, arrays, precision, nstreams=4, device=0):
     entries = [batch_entry(s, a) for s, a in zip(systems, arrays)]
     st, arr = capi.factorize_batched(entries, device=device, precision=precision,
                                      nstreams=nstreams)
+    run_batched.errors = [arr[i].error.decode(errors="replace") for i in range(len(systems))]
     return st, [arr[i].status for i in range(len(systems))]

@@ -60,7 +60,8 @@ class System(ctypes.Structure):
                 ("shift_rel", ctypes.c_double), ("out_idx", ctypes.c_void_p),
                 ("out_orbitals", ctypes.c_void_p), ("out_M", ctypes.c_void_p),
                 ("out_L", ctypes.c_void_p), ("status", ctypes.c_int),
-                ("kmeans_stats", KMeansStats), ("isdf_stats", IsdfStats)]
+                ("kmeans_stats", KMeansStats), ("isdf_stats", IsdfStats),
+                ("error", ctypes.c_char * 192)]
 
 
 class ThcError(RuntimeError):

@@ -21,19 +21,20 @@ namespace thc {
 
 void* ws_get(Ctx* c, Slot s, size_t bytes)
 {
+  // Stream-ordered allocation: growing a slot neither synchronises the device nor stalls
+  // other contexts' streams (a plain cudaFree would wait for the whole GPU).
   if (bytes == 0) bytes = 16;
   if (c->ws_bytes[s] >= bytes) return c->ws[s];
   if (c->ws[s]) {
-    cudaStreamSynchronize(c->stream);
-    cudaFree(c->ws[s]);
+    cudaFreeAsync(c->ws[s], c->stream);
     c->ws[s] = nullptr;
     c->ws_bytes[s] = 0;
   }
   size_t want = bytes + bytes / 8;  // headroom so that slightly larger calls reuse it
   void* p = nullptr;
-  if (cudaMalloc(&p, want) != cudaSuccess) {
+  if (cudaMallocAsync(&p, want, c->stream) != cudaSuccess) {
     cudaGetLastError();
-    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    if (cudaMallocAsync(&p, bytes, c->stream) != cudaSuccess) {
       cudaGetLastError();
       return nullptr;
     }
@@ -171,6 +172,16 @@ int thc_ctx_create(int device, int precision, thc_ctx** out)
     return THC_ERR_CUDA;
   }
   c->stream = c->own_stream;
+  {
+    // Keep freed workspace in the device's default pool instead of returning it to the
+    // driver at every synchronisation (process-local setting of this process's pool).
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      unsigned long long keep = ~0ULL;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  }
   *out = h;
   return THC_OK;
 }
@@ -183,10 +194,11 @@ int thc_ctx_destroy(thc_ctx* h)
   cudaStreamSynchronize(c->stream);
   for (auto& kv : c->plans) cufftDestroy(kv.second);
   for (int s = 0; s < thc::WS_NSLOTS; s++)
-    if (c->ws[s]) cudaFree(c->ws[s]);
+    if (c->ws[s]) cudaFreeAsync(c->ws[s], c->stream);
+  cudaStreamSynchronize(c->stream);
   thc::clear_profile(c);
   for (auto e : c->event_pool) cudaEventDestroy(e);
-  if (c->km_graph) cudaGraphExecDestroy(c->km_graph);
+  for (auto& g : c->km_graphs) cudaGraphExecDestroy(g.second);
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -198,6 +210,8 @@ int thc_ctx_destroy(thc_ctx* h)
 int thc_ctx_set_stream(thc_ctx* h, void* stream)
 {
   if (!h) return THC_ERR_ARG;
+  // Workspace is allocated in the order of the current stream: finish it before switching.
+  cudaStreamSynchronize(h->c.stream);
   h->c.stream = stream ? (cudaStream_t)stream : h->c.own_stream;
   for (auto& kv : h->c.plans) cufftSetStream(kv.second, h->c.stream);
   return THC_OK;
@@ -332,18 +346,31 @@ int thc_factorize_batched(int device, int precision, thc_system* sys, int nsys, 
     }
     workers.assign(pool.begin(), pool.begin() + nstreams);
   }
+  // Largest systems first (N_g N_mu estimates the work), taken dynamically by the workers.
+  std::vector<int> order(nsys);
+  for (int i = 0; i < nsys; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return (double)sys[x].ng * sys[x].nmu > (double)sys[y].ng * sys[y].nmu;
+  });
   std::atomic<int> next(0);
   auto work = [&](thc_ctx* h) {
     cudaSetDevice(device);
-    for (int i = next++; i < nsys; i = next++) {
-      thc_system& s = sys[i];
+    for (int n_ = next++; n_ < nsys; n_ = next++) {
+      thc_system& s = sys[order[n_]];
       memset(&s.kmeans_stats, 0, sizeof(s.kmeans_stats));
       memset(&s.isdf_stats, 0, sizeof(s.isdf_stats));
+      s.error[0] = 0;
+      h->c.last_error.clear();
       s.status = thc::kmeans_run(&h->c, s.grid, s.rho, s.ng, s.nmu, s.init_idx, s.max_it,
                                  s.threshold, s.out_idx, &s.kmeans_stats);
-      if (s.status != THC_OK) continue;
-      s.status = thc::isdf_run(&h->c, s.phi, s.ng, s.norb, s.out_idx, s.nmu, s.mesh, s.coulG,
-                               s.shift_rel, s.out_orbitals, s.out_M, s.out_L, &s.isdf_stats);
+      if (s.status == THC_OK)
+        s.status = thc::isdf_run(&h->c, s.phi, s.ng, s.norb, s.out_idx, s.nmu, s.mesh,
+                                 s.coulG, s.shift_rel, s.out_orbitals, s.out_M, s.out_L,
+                                 &s.isdf_stats);
+      if (s.status != THC_OK) {
+        snprintf(s.error, sizeof(s.error), "%s", h->c.last_error.c_str());
+        cudaGetLastError();
+      }
     }
     cudaStreamSynchronize(h->c.stream);
   };

@@ -10,6 +10,7 @@
 #include <map>
 #include <string>
 #include <tuple>
+#include <utility>
 #include <vector>
 
 #include "../../include/thc_gb300.h"
@@ -60,6 +61,7 @@ enum Slot : int {
   WS_ROWMAX,        // per-row maxima for slicing
   WS_ZTMP,          // FP64 zeta of the rank-deficient fallback
   WS_DPART,         // split-K partials chosen inside dgemm
+  WS_FFTWORK,       // cuFFT work area of the context's plans
   WS_NSLOTS
 };
 
@@ -71,6 +73,7 @@ struct Ctx {
   void* ws[WS_NSLOTS] = {};
   size_t ws_bytes[WS_NSLOTS] = {};
   std::map<std::tuple<int, int, int, int, int>, cufftHandle> plans;  // (n0,n1,n2,batch,type)
+  std::map<std::tuple<int, int, int, int, int>, size_t> plan_work;   // their work-area bytes
   void* pinned = nullptr;          // 4 KB pinned host scratch
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   long long launches = 0;
@@ -80,8 +83,9 @@ struct Ctx {
   int gemm_tc = 1;      // 1: tcgen05 sliced GEMM, 0: mma.sync sliced GEMM
   int km_prune = 1;     // 1: spatially pruned k-means assign, 0: exhaustive
   int use_graphs = 1;   // capture the k-means iteration block in a CUDA graph
-  cudaGraphExec_t km_graph = nullptr;
-  std::vector<long long> km_graph_key;
+  // Instantiated k-means iteration graphs, most recently used last, keyed by every kernel
+  // argument they bake in.
+  std::vector<std::pair<std::vector<long long>, cudaGraphExec_t>> km_graphs;
   std::string last_error;
   // History of the last k-means run (device buffer WS_KM_LOG: diff[max_it], pct[max_it]).
   int km_last_iters = 0;

@@ -121,31 +121,33 @@ __global__ void dgemm_reduce(GemmArgs g)
 
 constexpr int NB = 64;
 
-// 1/sqrt(d) for a positive normal d: FP32 seed, then two Newton-Raphson steps for the
-// reciprocal square root, y <- y (3 - d y^2) / 2, each of which doubles the correct bits
-// (24 -> 48 -> full FP64, within a few ulp).  A handful of dependent FP64 operations instead
-// of a square root followed by a division: the pivot is on the critical path of every
-// Cholesky step, and FP64 latency is long on this part.
-__device__ __forceinline__ double rsqrt_newton(double d)
+// 1/sqrt(d) for a positive normal d: an FP32 seed y0 (relative error e0 < 2^-22), then one
+// third-order step of the binomial series for (1 - e)^(-1/2), e = 1 - d y0^2:
+// y = y0 (1 + e/2 + 3e^2/8), which leaves O(e0^3) -- below FP64 rounding.  Five dependent
+// FP64 operations instead of a square root and a division: the pivot is on the critical
+// path of every Cholesky step, and FP64 latency is long on this part.
+__device__ __forceinline__ double rsqrt_fast(double d)
 {
-  if (!(d > 1e-30 && d < 1e30)) return 1.0 / sqrt(d);
-  double y = (double)rsqrtf((float)d);
-  double h = d * y;
-  y = y * (1.5 - 0.5 * h * y);
-  h = d * y;
-  y = y * (1.5 - 0.5 * h * y);
-  return y;
+  const long long db = __double_as_longlong(d);
+  const int ed = (int)((db >> 52) & 0x7ff);
+  if (ed < 1023 - 100 || ed > 1023 + 100) return 1.0 / sqrt(d);   // outside FP32's range
+  const double y = (double)rsqrtf((float)d);
+  const double e = __fma_rn(-d * y, y, 1.0);
+  return __fma_rn(y * e, __fma_rn(0.375, e, 0.5), y);
 }
+
+constexpr int kPanel = 4;   // columns factored per barrier round in potrf_diag_inv
 
 // Factor the diagonal block at (k0, k0) and invert its triangle: writes L_kk into A
 // (upper part zeroed) and L_kk^{-1} into dinv (nb x nb, row-major, zero above the diagonal).
 // Pivots at or below thr stop the factorisation (info = global 1-based index).
-// The inverse V is eliminated alongside the factor: at step j row j of V is scaled by
-// 1/L_jj and subtracted from the rows below (L V = I by forward substitution), so both
-// run on all threads with one pivot chain.  The next pivot's reciprocal square root is
-// taken by the thread that finishes updating that diagonal entry, while the other threads
-// are still updating (look-ahead): two barriers per step, and the long FP64 latency of the
-// pivot overlaps the FP64-throughput-bound update.
+// Blocked by panels of kPanel columns, with three barriers per panel:
+//   (a) one thread factors the panel's kPanel x kPanel diagonal block and inverts it
+//       (registers; the pivots' reciprocal square roots are its only long chain);
+//   (b) the panel rows below, L_ip = A_ip D^{-T}, and the panel's rows of V = L^{-1}
+//       (forward substitution L V = I: V_panel = D^{-1} (rows updated by earlier panels));
+//   (c) the rank-kPanel update of the trailing lower triangle of A and of the rows of V
+//       below the panel.
 __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, int n, int k0,
                                                       const double* thr_p, CholStatus* cs,
                                                       double* dinv)
@@ -155,7 +157,7 @@ __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, i
   extern __shared__ double dsm[];                       // 2 x NB x (NB + 1) doubles
   double (*a)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm);
   double (*v)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm + NB * (NB + 1));
-  __shared__ double rinv, pmin, pmax;
+  __shared__ double dinv_p[kPanel][kPanel];
   __shared__ int bad;
   const int nb = min(NB, n - k0);
   for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
@@ -163,70 +165,134 @@ __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, i
     a[r][c] = (r < nb && c < nb) ? A[(long long)(k0 + r) * ld + k0 + c] : (r == c ? 1.0 : 0.0);
     v[r][c] = r == c ? 1.0 : 0.0;
   }
-  // One thread: check pivot j and publish 1/sqrt of it (or the breakdown).
-  auto pivot = [&](int j) {
-    const double d = a[j][j];
-    if (!(d > thr)) {
-      bad = 1;
-      cs->flag = 1;
-      cs->info = k0 + j + 1;
-    } else {
-      rinv = rsqrt_newton(d);
-      pmin = fmin(pmin, d);
-      pmax = fmax(pmax, d);
-    }
-  };
+  double pmin = 0.0, pmax = 0.0;
   if (threadIdx.x == 0) {
     bad = 0;
     pmin = cs->min_piv;
     pmax = cs->max_piv;
   }
   __syncthreads();
-  if (threadIdx.x == 0 && nb > 0) pivot(0);
-  __syncthreads();
-  for (int j = 0; j < nb && !bad; j++) {
-    const double ri = rinv;
-    if (threadIdx.x == 0) a[j][j] *= ri;                  // d / sqrt(d)
-    for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) a[i][j] *= ri;
-    for (int c = threadIdx.x; c <= j; c += blockDim.x) v[j][c] *= ri;
-    __syncthreads();
-    // rows i > j: a[i][c] -= a[i][j] a[c][j] (j < c <= i) and v[i][c] -= a[i][j] v[j][c]
-    // (c <= j); together the columns 0..i of row i.  The (i, c) pairs are enumerated flat
-    // so that every warp-wide FP64 FMA has all 32 lanes busy: GB300 issues an FP64
-    // instruction at two lanes per clock whatever its active mask.  At most kSlots pairs
-    // per thread per step.
-    {
-      // No element read in this step is written in it (the update reads column j of a and
-      // row j of v only), so each thread loads all its operands first, then issues its
-      // FMAs back to back, then stores: the dependent smem round trips of one element no
-      // longer serialise the next.
-      constexpr int kSlots = (NB * (NB + 1) / 2 + 255) / 256;
-      const int off = (j + 1) * (j + 2) / 2;                 // pairs of rows <= j
-      const int total = nb * (nb + 1) / 2 - off;
-      double* dst[kSlots];
-      double lij[kSlots], src[kSlots], cur[kSlots];
-      bool own_pivot = false;
+  for (int j0 = 0; j0 < nb; j0 += kPanel) {
+    const int w = min(kPanel, nb - j0);
+    // ---- (a) the panel's diagonal block and its inverse, by one thread
+    if (threadIdx.x == 0) {
+      // Fully unrolled over kPanel (registers only); rows/columns >= w are an identity pad.
+      double L[kPanel][kPanel], D[kPanel][kPanel], r[kPanel];
 #pragma unroll
-      for (int q = 0; q < kSlots; q++) {
-        const int e = threadIdx.x + 256 * q;
-        dst[q] = nullptr;
-        if (e >= total) continue;
-        const int x = e + off;
-        int i = (int)((sqrtf(8.f * (float)x + 1.f) - 1.f) * 0.5f);
-        while (i * (i + 1) / 2 > x) i--;
-        while ((i + 1) * (i + 2) / 2 <= x) i++;
-        const int c = x - i * (i + 1) / 2;
-        const bool inv = c <= j;
-        dst[q] = inv ? &v[i][c] : &a[i][c];
-        src[q] = inv ? v[j][c] : a[c][j];
-        lij[q] = a[i][j];
-        cur[q] = *dst[q];
-        own_pivot |= c == i && i == j + 1;
+      for (int i = 0; i < kPanel; i++)
+#pragma unroll
+        for (int c = 0; c < kPanel; c++)
+          L[i][c] = (i < w && c <= i) ? a[j0 + i][j0 + c] : (i == c ? 1.0 : 0.0);
+      bool ok = true;
+#pragma unroll
+      for (int q = 0; q < kPanel; q++) {
+        const double d = L[q][q];
+        if (ok && q < w && !(d > thr)) {
+          ok = false;
+          bad = 1;
+          cs->flag = 1;
+          cs->info = k0 + j0 + q + 1;
+        }
+        if (q < w) {
+          pmin = fmin(pmin, d);
+          pmax = fmax(pmax, d);
+        }
+        r[q] = ok ? rsqrt_fast(d) : 1.0;
+        L[q][q] = d * r[q];
+#pragma unroll
+        for (int i = q + 1; i < kPanel; i++) L[i][q] *= r[q];
+#pragma unroll
+        for (int i = q + 1; i < kPanel; i++)
+#pragma unroll
+          for (int c = q + 1; c <= i; c++) L[i][c] = __fma_rn(-L[i][q], L[c][q], L[i][c]);
       }
+      if (ok) {
+        // D = L^{-1}: D_qq = 1 / L_qq = r_q, D_iq = -r_i sum_{p=q}^{i-1} L_ip D_pq.
 #pragma unroll
-      for (int q = 0; q < kSlots; q++)
-        if (dst[q]) *dst[q] = __fma_rn(-lij[q], src[q], cur[q]);
-      if (own_pivot) pivot(j + 1);                           // look-ahead pivot
+        for (int q = 0; q < kPanel; q++) {
+#pragma unroll
+          for (int i = 0; i < kPanel; i++) D[i][q] = 0.0;
+          D[q][q] = r[q];
+#pragma unroll
+          for (int i = q + 1; i < kPanel; i++) {
+            double t = 0.0;
+#pragma unroll
+            for (int p = q; p < i; p++) t = __fma_rn(L[i][p], D[p][q], t);
+            D[i][q] = -t * r[i];
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < kPanel; i++)
+#pragma unroll
+          for (int c = 0; c < kPanel; c++) {
+            if (i < w && c <= i) a[j0 + i][j0 + c] = L[i][c];
+            dinv_p[i][c] = (i < w && c <= i) ? D[i][c] : 0.0;
+          }
+      }
+    }
+    __syncthreads();
+    if (bad) break;
+    // ---- (b) panel rows below (thread per row) and the panel rows of V (thread per column)
+    for (int t = threadIdx.x; t < (nb - j0 - w) + (j0 + w); t += blockDim.x) {
+      if (t < nb - j0 - w) {
+        const int i = j0 + w + t;
+        double x[kPanel], y[kPanel];
+#pragma unroll
+        for (int p = 0; p < kPanel; p++) x[p] = p < w ? a[i][j0 + p] : 0.0;
+#pragma unroll
+        for (int q = 0; q < kPanel; q++) {
+          double s2 = 0.0;
+#pragma unroll
+          for (int p = 0; p <= q; p++) s2 = __fma_rn(x[p], dinv_p[q][p], s2);
+          y[q] = s2;
+        }
+#pragma unroll
+        for (int q = 0; q < kPanel; q++)
+          if (q < w) a[i][j0 + q] = y[q];
+      } else {
+        const int c = t - (nb - j0 - w);                    // column of V, c < j0 + w
+        double x[kPanel], y[kPanel];
+#pragma unroll
+        for (int p = 0; p < kPanel; p++) x[p] = p < w ? v[j0 + p][c] : 0.0;
+#pragma unroll
+        for (int q = 0; q < kPanel; q++) {
+          double s2 = 0.0;
+#pragma unroll
+          for (int p = 0; p <= q; p++) s2 = __fma_rn(dinv_p[q][p], x[p], s2);
+          y[q] = s2;
+        }
+#pragma unroll
+        for (int q = 0; q < kPanel; q++)
+          if (q < w) v[j0 + q][c] = y[q];
+      }
+    }
+    __syncthreads();
+    // ---- (c) rank-w update of rows i >= j0 + w: a[i][c] for j0 + w <= c <= i and
+    //          v[i][c] for c < j0 + w, i.e. columns 0..i of each row.
+    {
+      const int r0 = j0 + w;
+      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+      for (int i = r0 + ty; i < nb; i += 16) {
+        double l[kPanel];
+#pragma unroll
+        for (int p = 0; p < kPanel; p++) l[p] = p < w ? a[i][j0 + p] : 0.0;
+        for (int c = tx; c <= i; c += 16) {
+          double acc;
+          if (c < r0) {
+            acc = v[i][c];
+#pragma unroll
+            for (int p = 0; p < kPanel; p++)
+              if (p < w) acc = __fma_rn(-l[p], v[j0 + p][c], acc);
+            v[i][c] = acc;
+          } else {
+            acc = a[i][c];
+#pragma unroll
+            for (int p = 0; p < kPanel; p++)
+              if (p < w) acc = __fma_rn(-l[p], a[c][j0 + p], acc);
+            a[i][c] = acc;
+          }
+        }
+      }
     }
     __syncthreads();
   }

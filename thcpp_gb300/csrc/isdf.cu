@@ -137,26 +137,32 @@ __global__ void init_chol_status(CholStatus* cs)
 
 int get_plan(Ctx* c, int n0, int n1, int n2, int batch, cufftType type, cufftHandle* out)
 {
+  // Plans are cached per context; their work area is the context's own stream-ordered
+  // FFT slot (cuFFT's automatic allocation would cudaMalloc, which synchronises the GPU).
   auto key = std::make_tuple(n0, n1, n2, batch, (int)type);
   auto it = c->plans.find(key);
-  if (it != c->plans.end()) {
-    cufftSetStream(it->second, c->stream);
-    *out = it->second;
-    return THC_OK;
-  }
   cufftHandle p;
-  if (cufftCreate(&p) != CUFFT_SUCCESS) return set_error(c, THC_ERR_CUFFT, "cufftCreate failed");
-  long long n[3] = {n0, n1, n2};
-  long long ng = (long long)n0 * n1 * n2;
-  long long nc = (long long)n0 * n1 * (n2 / 2 + 1);
-  size_t work = 0;
-  cufftResult r = cufftMakePlanMany64(p, 3, n, nullptr, 1, ng, nullptr, 1, nc, type, batch, &work);
-  if (r != CUFFT_SUCCESS) {
-    cufftDestroy(p);
-    return set_error(c, THC_ERR_CUFFT, "cufftMakePlanMany64 failed (%d)", (int)r);
+  if (it != c->plans.end()) {
+    p = it->second;
+  } else {
+    if (cufftCreate(&p) != CUFFT_SUCCESS) return set_error(c, THC_ERR_CUFFT, "cufftCreate failed");
+    cufftSetAutoAllocation(p, 0);
+    long long n[3] = {n0, n1, n2};
+    long long ng = (long long)n0 * n1 * n2;
+    long long nc = (long long)n0 * n1 * (n2 / 2 + 1);
+    size_t work = 0;
+    cufftResult r = cufftMakePlanMany64(p, 3, n, nullptr, 1, ng, nullptr, 1, nc, type, batch, &work);
+    if (r != CUFFT_SUCCESS) {
+      cufftDestroy(p);
+      return set_error(c, THC_ERR_CUFFT, "cufftMakePlanMany64 failed (%d)", (int)r);
+    }
+    c->plans[key] = p;
+    c->plan_work[key] = work;
   }
-  cufftSetStream(p, c->stream);
-  c->plans[key] = p;
+  void* wa = ws_get(c, WS_FFTWORK, c->plan_work[key]);
+  if (!wa) return set_error(c, THC_ERR_NOMEM, "cuFFT work area");
+  if (cufftSetWorkArea(p, wa) != CUFFT_SUCCESS || cufftSetStream(p, c->stream) != CUFFT_SUCCESS)
+    return set_error(c, THC_ERR_CUFFT, "cuFFT work area / stream");
   *out = p;
   return THC_OK;
 }

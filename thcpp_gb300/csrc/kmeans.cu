@@ -407,6 +407,7 @@ __global__ void __launch_bounds__(kAssignThreads) km_assign64p(KmBufs b)
       cand[slot] = k; ccx[slot] = c3[0]; ccy[slot] = c3[1]; ccz[slot] = c3[2];
     }
   }
+  __syncthreads();   // every thread reads every candidate written above
   int nc = ncand;
   ArgMin am;
   am.init();
@@ -497,6 +498,7 @@ __global__ void __launch_bounds__(kAssignThreads) km_assign32p(KmBufs b)
       cand[slot] = k; ccx[slot] = c3[0]; ccy[slot] = c3[1]; ccz[slot] = c3[2];
     }
   }
+  __syncthreads();   // every thread reads every candidate written above
   int nc = ncand;
   if (!valid) return;
   float m1 = INFINITY, m2 = INFINITY;
@@ -1251,7 +1253,8 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
       init = (const int*)p;
     }
   }
-  KmBufs b{};
+  KmBufs b;
+  memset(&b, 0, sizeof b);   // padding included: the bytes key the cached graph
   b.ng = ng;
   b.nmu = nmu;
   b.nb = (int)cdiv(ng, kBP);
@@ -1364,17 +1367,26 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   const bool graphs = c->use_graphs && !fixed;
   cudaGraphExec_t gexec = nullptr;
   if (graphs) {
-    std::vector<long long> key = {ng, nmu, mixed, prune, (long long)(uintptr_t)g64,
-                                  (long long)(uintptr_t)cen, (long long)(uintptr_t)hist,
-                                  (long long)(uintptr_t)st, (long long)(uintptr_t)permw,
-                                  (long long)(uintptr_t)member, (long long)(uintptr_t)logb,
-                                  (long long)(uintptr_t)s};
-    if (c->km_graph && c->km_graph_key == key) {
-      gexec = c->km_graph;
+    // The graph bakes in every kernel argument: key it on all of them (the whole KmBufs,
+    // whose pointers can move when a workspace slot grows) and on the launch shapes.
+    std::vector<long long> key = {ng, nmu, mixed, prune, (long long)(uintptr_t)s,
+                                  (long long)hist_smem, (long long)nassign};
+    {
+      const size_t words = (sizeof(KmBufs) + sizeof(long long) - 1) / sizeof(long long);
+      std::vector<long long> raw(words, 0);
+      memcpy(raw.data(), &b, sizeof(KmBufs));
+      key.insert(key.end(), raw.begin(), raw.end());
+    }
+    auto hit = std::find_if(c->km_graphs.begin(), c->km_graphs.end(),
+                            [&](const auto& e) { return e.first == key; });
+    if (hit != c->km_graphs.end()) {
+      gexec = hit->second;
+      std::rotate(hit, hit + 1, c->km_graphs.end());      // most recently used last
     } else {
-      if (c->km_graph) {
-        cudaGraphExecDestroy(c->km_graph);
-        c->km_graph = nullptr;
+      constexpr size_t kGraphCache = 32;
+      if (c->km_graphs.size() >= kGraphCache) {             // previous runs have finished
+        cudaGraphExecDestroy(c->km_graphs.front().second);
+        c->km_graphs.erase(c->km_graphs.begin());
       }
       cudaGraph_t graph;
       THC_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -1386,8 +1398,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
       ce = cudaGraphInstantiate(&gexec, graph, 0);
       cudaGraphDestroy(graph);
       if (ce != cudaSuccess) return set_error(c, THC_ERR_CUDA, "k-means graph instantiate: %s", cudaGetErrorString(ce));
-      c->km_graph = gexec;
-      c->km_graph_key = key;
+      c->km_graphs.emplace_back(key, gexec);
     }
   }
   for (int it = 0; it < max_it;) {
