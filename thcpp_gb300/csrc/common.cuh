@@ -59,7 +59,6 @@ enum Slot : int {
   WS_PART,          // split-K partial sums
   WS_DINV,          // inverted diagonal blocks + L^{-1} + scratch of the inverse
   WS_ROWMAX,        // per-row maxima for slicing
-  WS_ZTMP,          // FP64 zeta of the rank-deficient fallback
   WS_DPART,         // split-K partials chosen inside dgemm
   WS_FFTWORK,       // cuFFT work area of the context's plans
   WS_NSLOTS

@@ -516,6 +516,7 @@ int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* din
     st = dgemm(c, h);
     if (st) return st;
   }
+  if (!Cinv) return THC_OK;
   GemmArgs g{};
   g.M = n; g.N = n; g.K = n;                            // Cinv = X^T X
   g.A = X; g.sam = 1; g.sak = ld;

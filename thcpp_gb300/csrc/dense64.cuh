@@ -47,6 +47,7 @@ int dgemm(Ctx* c, const GemmArgs& g);
 int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs,
               double* dinv);
 // Cinv = (L L^T)^{-1} via X = L^{-1}; X (n x ld) and T (64 x n) are scratch.
+// With Cinv == nullptr only X = L^{-1} is formed.
 int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* dinv, double* X,
                  double* T, double* Cinv, const CholStatus* cs);
 int set_identity(Ctx* c, double* A, long long ld, int n);

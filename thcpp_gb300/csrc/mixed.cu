@@ -123,12 +123,6 @@ __global__ void mixed_scalars(double* dmean, double* thr, double* shift, double*
   *zero = 0.0;
 }
 
-__global__ void to_f32(const double* __restrict__ x, long long n, float* y)
-{
-  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (e < n) y[e] = (float)x[e];
-}
-
 __global__ void init_cs(CholStatus* cs)
 {
   cs->flag = 0;
@@ -266,23 +260,67 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     if (hcs.flag)
       return set_error(c, THC_ERR_NOT_PD, "thc_isdf: Cholesky of C failed at pivot %d", hcs.info);
   }
-  if ((st = chol_inverse(c, Lc, nmu, nmu, dinv, Xinv, Tinv, Cinv, cs))) return st;
+  // X = L^{-1}; C^{-1} = X^T X is needed by the full-rank solve only.  From N_mu = 512 on,
+  // that product runs as a sliced tensor GEMM (A = B = the slices of X^T): on C2 its M
+  // error is 4e-9, while the FP64 product would cost 2 N_mu^3 on the narrow FP64 pipe.
+  const bool cinv_tc = !shifted && nmu >= 512;
+  if ((st = chol_inverse(c, Lc, nmu, nmu, dinv, Xinv, Tinv, (shifted || cinv_tc) ? nullptr : Cinv,
+                         cs)))
+    return st;
+  if (cinv_tc) {
+    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, 1, nmu, nullptr, 0, sz, sa, mu_kpad,
+                                mu_pad * mu_kpad, ea, mu_pad)))   // rows of X^T
+      return st;
+    OzArgs g;
+    g.M = nmu; g.N = nmu; g.K = nmu;
+    g.a.s = sa; g.a.e = ea; g.a.ld = mu_kpad; g.a.slice_stride = mu_pad * mu_kpad;
+    g.b = g.a;
+    g.b.k_contig = true;
+    g.levels = sz; g.epilogue = OZ_STORE_F64; g.C = Cinv; g.ldc = nmu;
+    g.ksplit = oz_choose_split(nmu, nmu, nmu, false);
+    if (g.ksplit > 1) {
+      g.part = (double*)ws_get(c, WS_PART, sizeof(double) * g.ksplit * nn);
+      if (!g.part) return set_error(c, THC_ERR_NOMEM, "thc_isdf: split-K partials");
+    }
+    if ((st = gemm(g))) return st;
+  }
   // zeta^T = C^{-1} Z^T: A = C^{-1} sliced by rows, B = Z sliced by rows (grid points).
   // A rank-deficient C (shifted) has an inverse whose null-space entries are ~1/shift, so
   // the product cancels by far more than any slice depth resolves: it runs in FP64 then.
   if (shifted) {
-    double* z64 = (double*)ws_get(c, WS_ZTMP, 2 * sizeof(double) * nmu * ng);
-    if (!z64) return set_error(c, THC_ERR_NOMEM, "thc_isdf: FP64 zeta buffer");
-    double* zf = z64 + (long long)nmu * ng;
-    if ((st = dw_to_f64(c, zg, (long long)nmu * ng, zf))) return st;
-    GemmArgs g;
+    // Regularised (rank-deficient) C: never form C^{-1} = X^T X (X = L^{-1}), whose
+    // null-space entries are ~1/shift and would swamp the slices.  Two sliced products with
+    // X instead, each amplifying by ~1/sqrt(shift) only: Y^T = Z X^T, then
+    // zeta^T = X^T Y.  (Emulated on the C1 cell this is also more accurate than the FP64
+    // C^{-1} product: pair-Coulomb invariant 1.7e-8 against 2.2e-6.)
+    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, sz, sb, mu_kpad, ng_pad * mu_kpad, eb,
+                               ng_pad)))
+      return st;
+    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, nmu, 1, nullptr, 0, sz, sa, mu_kpad,
+                                mu_pad * mu_kpad, ea, mu_pad)))
+      return st;
+    {
+      OzArgs g;                                  // Y^T (N_g x N_mu) = Z X^T, into zg
+      g.M = ng; g.N = nmu; g.K = nmu;
+      g.a.s = sb; g.a.e = eb; g.a.ld = mu_kpad; g.a.slice_stride = ng_pad * mu_kpad;
+      g.b.s = sa; g.b.e = ea; g.b.ld = mu_kpad; g.b.slice_stride = mu_pad * mu_kpad;
+      g.b.k_contig = true;
+      g.levels = sz; g.epilogue = OZ_STORE_DW; g.C = zg; g.ldc = nmu;
+      if ((st = gemm(g))) return st;
+    }
+    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, 1, nmu, nullptr, 0, sz, sa, mu_kpad,
+                                mu_pad * mu_kpad, ea, mu_pad)))   // rows of X^T
+      return st;
+    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, sz, sb, mu_kpad, ng_pad * mu_kpad, eb,
+                               ng_pad)))
+      return st;
+    OzArgs g;                                    // zeta^T = X^T Y
     g.M = nmu; g.N = ng; g.K = nmu;
-    g.A = Cinv; g.sam = nmu; g.sak = 1;
-    g.B = zf; g.sbn = nmu; g.sbk = 1;
-    g.C = z64; g.ldc = ng;
-    if ((st = dgemm(c, g))) return st;
-    to_f32<<<(unsigned)cdiv((long long)nmu * ng, 256), 256, 0, s>>>(z64, (long long)nmu * ng, zeta);
-    THC_LAUNCHED(c, "to_f32");
+    g.a.s = sa; g.a.e = ea; g.a.ld = mu_kpad; g.a.slice_stride = mu_pad * mu_kpad;
+    g.b.s = sb; g.b.e = eb; g.b.ld = mu_kpad; g.b.slice_stride = ng_pad * mu_kpad;
+    g.b.k_contig = true;
+    g.levels = sz; g.epilogue = OZ_STORE_F32; g.C = zeta; g.ldc = ng;
+    if ((st = gemm(g))) return st;
   } else {
     if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, sz, sa, mu_kpad,
                                 mu_pad * mu_kpad, ea, mu_pad)))

@@ -24,7 +24,7 @@ __device__ __forceinline__ void store_epilogue(const OzArgs& g, long long m, lon
   if (g.epilogue == OZ_SQUARE_F64 || g.epilogue == OZ_SQUARE_DW) v = v * v;
   if (g.epilogue == OZ_STORE_F32) {
     ((float*)g.C)[m * g.ldc + n] = (float)v;
-  } else if (g.epilogue == OZ_SQUARE_DW) {
+  } else if (g.epilogue == OZ_SQUARE_DW || g.epilogue == OZ_STORE_DW) {
     float hi = (float)v;
     ((float2*)g.C)[m * g.ldc + n] = make_float2(hi, (float)(v - (double)hi));
   } else {
@@ -378,12 +378,6 @@ __global__ void slice_rows_dw_kernel(const float2* __restrict__ X, long long row
   }
 }
 
-__global__ void dw_to_f64_kernel(const float2* __restrict__ X, long long n, double* out)
-{
-  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < n) out[i] = (double)X[i].x + (double)X[i].y;
-}
-
 // FP32 input scaled by an FP32 copy of `scale` (rounded once to FP32, then sliced exactly
 // in FP32 arithmetic).  Two passes so that long rows use the whole GPU: per-row maxima by
 // column chunks (atomicMax on the bit pattern, valid for non-negative floats), then the
@@ -469,13 +463,6 @@ int oz_slice_rows_dw(Ctx* c, const float2* X, long long rows, long long cols, lo
   slice_rows_dw_kernel<<<(unsigned)cdiv(threads, 256), 256, 0, c->stream>>>(
       X, rows, cols, ldx, nslices, out, ldo, slice_stride, exps, rows_pad);
   THC_LAUNCHED(c, "slice_rows_dw");
-  return THC_OK;
-}
-
-int dw_to_f64(Ctx* c, const float2* X, long long n, double* out)
-{
-  dw_to_f64_kernel<<<(unsigned)cdiv(n, 256), 256, 0, c->stream>>>(X, n, out);
-  THC_LAUNCHED(c, "dw_to_f64");
   return THC_OK;
 }
 

@@ -20,7 +20,10 @@ namespace thc {
 
 // OZ_SQUARE_DW stores the squared product as a double-word FP32 pair (float2 {hi, lo},
 // hi + lo carrying ~46 bits), which needs no FP64 arithmetic in the epilogue.
-enum OzEpilogue : int { OZ_STORE_F64 = 0, OZ_SQUARE_F64 = 1, OZ_STORE_F32 = 2, OZ_SQUARE_DW = 3 };
+// OZ_STORE_DW stores the product itself as such a pair.
+enum OzEpilogue : int {
+  OZ_STORE_F64 = 0, OZ_SQUARE_F64 = 1, OZ_STORE_F32 = 2, OZ_SQUARE_DW = 3, OZ_STORE_DW = 4
+};
 
 struct OzOperand {
   const __nv_bfloat16* s = nullptr;  // slices
@@ -63,8 +66,6 @@ int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, l
 int oz_slice_rows_dw(Ctx* c, const float2* X, long long rows, long long cols, long long ldx,
                      int nslices, __nv_bfloat16* out, long long ldo, long long slice_stride,
                      int* exps, long long rows_pad);
-// Double-word matrix to FP64 (hi + lo).
-int dw_to_f64(Ctx* c, const float2* X, long long n, double* out);
 int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, long long ldx,
                       const float* scale, int scale_shift, int nslices, __nv_bfloat16* out,
                       long long ldo, long long slice_stride, int* exps, long long rows_pad);

@@ -370,6 +370,13 @@ __global__ void __launch_bounds__(TTHREADS, 1)
             ((float*)g.C)[m * g.ldc + n] = __fadd_rn(ah[q], al[q]) * sc;
             continue;
           }
+          if (g.epilogue == OZ_STORE_DW && g.ksplit <= 1 && ex > -100 && ex < 100) {
+            float sc = pow2f(ex);
+            float zh, zl;
+            fast_two_sum(ah[q] * sc, al[q] * sc, zh, zl);
+            ((float2*)g.C)[m * g.ldc + n] = make_float2(zh, zl);
+            continue;
+          }
           if (g.epilogue == OZ_SQUARE_DW && g.ksplit <= 1 && ex > -60 && ex < 60) {
             // (h + l)^2 in double-word FP32: p + e = h^2 exactly (FMA), plus 2 h l.
             float sc = pow2f(ex);
@@ -390,7 +397,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
           if (g.epilogue == OZ_SQUARE_F64 || g.epilogue == OZ_SQUARE_DW) val = val * val;
           if (g.epilogue == OZ_STORE_F32) {
             ((float*)g.C)[m * g.ldc + n] = (float)val;
-          } else if (g.epilogue == OZ_SQUARE_DW) {
+          } else if (g.epilogue == OZ_SQUARE_DW || g.epilogue == OZ_STORE_DW) {
             float hi = (float)val;
             ((float2*)g.C)[m * g.ldc + n] = make_float2(hi, (float)(val - (double)hi));
           } else {
