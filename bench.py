@@ -38,6 +38,8 @@ WORKLOADS = {
            "n_mu": 2048, "mesh": [72, 72, 72]},
     "c4": {"workload": "batch-48-random-cubic-cells-32^3..64^3-no16..200-nmu6..10xno",
            "systems": 48},
+    "c5": {"workload": "diamond-216atom-108^3-no864-nmu5184", "n_g": 1259712, "n_orb": 864,
+           "n_mu": 5184, "mesh": [108, 108, 108]},
 }
 WORKLOAD = "c2"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per sliced-GEMM launch, mean of
@@ -270,15 +272,22 @@ def main():
 
     from thcpp_gb300 import build, capi, synth
     build.build()
-    s = synth.config(WORKLOAD)
+    on_device = WORKLOAD == "c5"
+    if on_device:
+        # 1.26e6 points x 864 Gaussians: generated on the GPU (the host build takes hours).
+        with capi.Context(local, capi.THC_PREC_FP64) as gctx:
+            s = synth.config_gpu(WORKLOAD, gctx, dev)
+    else:
+        s = synth.config(WORKLOAD)
     nmu, ng, no = s.nmu, s.ng, s.norb
     init = capi.initial_indices(ng, nmu, s.rng_seed)
 
     # Device-resident inputs.
-    d_grid = torch.from_numpy(s.grid).to(dev)
-    d_rho = torch.from_numpy(s.density).to(dev)
-    d_phi = torch.from_numpy(s.phi).to(dev)
-    d_coul = torch.from_numpy(s.coulG).to(dev)
+    as_dev = (lambda a: a) if on_device else (lambda a: torch.from_numpy(a).to(dev))
+    d_grid = as_dev(s.grid)
+    d_rho = as_dev(s.density)
+    d_phi = as_dev(s.phi)
+    d_coul = as_dev(s.coulG)
     d_init = torch.from_numpy(init).to(dev)
     d_idx = torch.zeros(nmu, dtype=torch.int32, device=dev)
     d_M = torch.zeros((nmu, nmu, 2), dtype=torch.float64, device=dev)
@@ -343,16 +352,22 @@ def main():
     dg_ms = 0.0
     idx_same = None
     if "fp64" in paths:
+        idx_mx = d_idx.cpu().numpy().copy()
+        if on_device:
+            # Both paths' workspaces do not fit at once at this size: free the mixed one.
+            ctx.close()
         ctx64 = capi.Context(local, capi.THC_PREC_FP64)
         torch.cuda.nvtx.range_push("fp64")
-        ms_fp64, launches64, kst64, r64 = timed(ctx64, args.fp64_steps, 1)
+        ms_fp64, launches64, kst64, r64 = timed(ctx64, args.fp64_steps,
+                                                0 if on_device else 1)
         torch.cuda.nvtx.range_pop()
         dg_ms, dg_n = ctx64.kernel_time("dgemm")
         ctx64.set_option("profile", 0)
         idx64 = d_idx.cpu().numpy().copy()
         M_fp64 = d_M.cpu().numpy().copy()
-        device_step(ctx)  # idx from the mixed path for the comparison below
-        idx_mx = d_idx.cpu().numpy().copy()
+        if on_device:
+            ctx64.close()
+            ctx = capi.Context(local, capi.THC_PREC_MIXED)
         Mc = M_mixed[..., 0] + 1j * M_mixed[..., 1]
         M6 = M_fp64[..., 0] + 1j * M_fp64[..., 1]
         rel_err = float(np.linalg.norm(Mc - M6) / np.linalg.norm(M6))
@@ -362,8 +377,9 @@ def main():
     def pinned(a):
         t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
         return t.numpy()
-    h_grid, h_rho, h_phi, h_coul = (pinned(s.grid), pinned(s.density), pinned(s.phi),
-                                    pinned(s.coulG))
+    host = (lambda a: a.cpu().numpy()) if on_device else (lambda a: a)
+    h_grid, h_rho, h_phi, h_coul = (pinned(host(s.grid)), pinned(host(s.density)),
+                                    pinned(host(s.phi)), pinned(host(s.coulG)))
     h_init = pinned(init)
     h_idx = pinned(np.zeros(nmu, np.int32))
     h_M = pinned(np.zeros((nmu, nmu, 2)))
@@ -406,7 +422,7 @@ def main():
         peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
         # Dominant tensor kernel: the sliced GEMMs.  Algorithmic tensor-pipe work per
         # factorisation = sum over the three GEMMs of (slice pairs) x 2 M N K.
-        sp, sz, sm = 6, 6, 4
+        sp, sz, sm = 6, 6, 5
         pairs = lambda L: L * (L + 1) // 2
         n0, n1, n2 = s.mesh
         nc2 = 2 * n0 * n1 * (n2 // 2 + 1)
@@ -423,7 +439,7 @@ def main():
                 "traffic_unit": "bytes per launch",
                 "share_of_step": (oz_ms / args.steps) / t_step if oz_n else None}
         cpu = None
-        if not args.no_cpu_baseline:
+        if not args.no_cpu_baseline and not on_device:
             t_cpu = cpu_reference_step(s, os.cpu_count() or 1)
             cpu = {"value": t_cpu, "unit": "s/system", "cores": os.cpu_count(), "kind": "port",
                    "sample": "1 full factorisation of the workload (C++ k-means restatement "

@@ -85,7 +85,8 @@ int thc_ctx_set_stream(thc_ctx* ctx, void* cuda_stream);
  * P, zeta and Coulomb products, 2..6); "gemm_tc" (1 = tcgen05 tensor-core kernel, the
  * default; 0 = warp-level mma.sync kernel); "km_prune" (1 = spatially pruned k-means
  * assignment, the default; 0 = exhaustive scan -- both exact); "graphs" (1 = replay the
- * k-means iteration block as a CUDA graph, the default);
+ * k-means iteration block as a CUDA graph, the default); "fft64" (mixed path: 1 = zeta
+ * in FP64 through a D2Z FFT, 0 = FP32 and R2C, the default);
  * "profile" (1 = record a CUDA event pair around every launch of the named kernels,
  * 0 = stop and clear). */
 int thc_ctx_set_option(thc_ctx* ctx, const char* key, double value);
@@ -122,6 +123,22 @@ int thc_kmeans(thc_ctx* ctx, const double* grid, const double* rho, long long ng
  * src/kmeans.cpp:238).  n must not exceed the last call's iteration count.
  */
 int thc_kmeans_history(thc_ctx* ctx, double* diff, double* pct_changed, int n);
+
+/*
+ * Synthetic inputs: periodised Gaussian s/p basis functions on the mesh, as the reference's
+ * input generator evaluates them with pyscf (tools/thcpy/thcpy/transform_basis.py:51-148)
+ * for the seeded synthetic systems.  out[p * nfunc + f] (device, N_g x nfunc, overwritten)
+ * = sum over the image centres c of atom a = f / 4 within rcut of point p of
+ * exp(-alphas[f] |d|^2), times d_x, d_y or d_z for f % 4 = 1, 2, 3 (d = r_p - centre).
+ *   grid         N_g x 3 doubles (host or device), C order over mesh (n2 fastest)
+ *   mesh         3 ints (host)
+ *   centres      ncentres x 3 doubles, the atom positions plus lattice translations that
+ *                can reach the cell, grouped by atom (centre_atom non-decreasing)
+ * Values agree with an FP64 evaluation to ~1e-6 relative (FP32 distances and expf).
+ */
+int thc_synth_gaussian_basis(thc_ctx* ctx, const double* grid, const int* mesh,
+                             const double* centres, const int* centre_atom, int ncentres,
+                             const double* alphas, int nfunc, double rcut, double* out);
 
 /*
  * thc_kmeans without any device allocation.  No counterpart in the reference: it exists

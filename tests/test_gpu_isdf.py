@@ -104,6 +104,25 @@ def test_isdf_rank_deficient_c1(request, prec):
     assert inv < 1e-4
 
 
+def test_isdf_mixed_fft64_option(lib):
+    """zeta in FP64 through a D2Z FFT (the fft64 option) against the oracle on C2, and the
+    slice-depth knob of the Coulomb product: fewer slices must not be more accurate."""
+    s = system("c2")
+    idx = kmeans_idx("c2")
+    ref = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG)["M"]
+    err = {}
+    for fft64, sm in ((0, 5), (1, 5), (0, 3)):
+        with capi.Context(0, capi.THC_PREC_MIXED) as ctx:
+            ctx.set_option("fft64", fft64)
+            ctx.set_option("slices_m", sm)
+            r = ctx.isdf(s.phi, idx, s.mesh, s.coulG)
+            assert r["status"] == 0
+            err[(fft64, sm)] = _rel(_cplx(r["M"]), ref)
+    print("mixed ||dM||/||M|| (fft64, slices_m):", err)
+    assert err[(1, 5)] < 1e-6 and err[(0, 5)] < 1e-6
+    assert err[(0, 3)] > err[(0, 5)]
+
+
 def test_sliced_gemm_tc_matches_mma_sync(lib):
     """The tcgen05 sliced GEMM against the warp-level mma.sync one (same slicing).
 

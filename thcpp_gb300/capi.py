@@ -34,6 +34,7 @@ EXPORTS = [
     "thc_ctx_last_error", "thc_status_string", "thc_ctx_kernel_launches",
     "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
     "thc_kmeans_history", "thc_factorize_batched", "thc_kmeans_noalloc",
+    "thc_synth_gaussian_basis",
 ]
 
 
@@ -111,6 +112,8 @@ def load(build_if_missing: bool = False):
     lib.thc_kmeans_initial_indices.argtypes = [cll, ci, cu, vp]
     lib.thc_kmeans.argtypes = [vp, vp, vp, cll, ci, vp, ci, cd, vp, ctypes.POINTER(KMeansStats)]
     lib.thc_kmeans_noalloc.argtypes = lib.thc_kmeans.argtypes
+    lib.thc_synth_gaussian_basis.argtypes = [vp, vp, vp, vp, vp, ci, vp, ci, cd, vp]
+    lib.thc_synth_gaussian_basis.restype = ci
     lib.thc_isdf.argtypes = [vp, vp, cll, ci, vp, ci, vp, vp, cd, vp, vp, vp,
                              ctypes.POINTER(IsdfStats)]
     for f in ("thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
@@ -234,6 +237,15 @@ class Context:
         if raise_on_error:
             self._check(st, "thc_kmeans_noalloc")
         return out_idx, stats, st
+
+    def gaussian_basis(self, grid, mesh, centres, centre_atom, alphas, nfunc, rcut, out):
+        """thc_synth_gaussian_basis: periodised Gaussian s/p functions into ``out`` (device)."""
+        mesh_a = np.ascontiguousarray(np.asarray(mesh, dtype=np.int32).reshape(3))
+        st = self.lib.thc_synth_gaussian_basis(self.h, _ptr(grid), _ptr(mesh_a), _ptr(centres),
+                                               _ptr(centre_atom), int(centre_atom.shape[0]),
+                                               _ptr(alphas), int(nfunc), float(rcut), _ptr(out))
+        self._check(st, "thc_synth_gaussian_basis")
+        return out
 
     def kmeans_history(self, n):
         diff = np.zeros(n)

@@ -30,13 +30,23 @@ void* ws_get(Ctx* c, Slot s, size_t bytes)
     c->ws[s] = nullptr;
     c->ws_bytes[s] = 0;
   }
-  size_t want = bytes + bytes / 8;  // headroom so that slightly larger calls reuse it
+  // Headroom so that slightly larger calls reuse the slot (at most 256 MiB of it).
+  size_t want = bytes + std::min(bytes / 8, (size_t)256 << 20);
   void* p = nullptr;
   if (cudaMallocAsync(&p, want, c->stream) != cudaSuccess) {
     cudaGetLastError();
     if (cudaMallocAsync(&p, bytes, c->stream) != cudaSuccess) {
       cudaGetLastError();
-      return nullptr;
+      // The pool keeps freed memory reserved (release threshold = max), possibly in pieces
+      // too small for this request: return what no allocation uses and try once more.
+      cudaMemPool_t pool;
+      if (cudaStreamSynchronize(c->stream) != cudaSuccess ||
+          cudaDeviceGetDefaultMemPool(&pool, c->device) != cudaSuccess ||
+          cudaMemPoolTrimTo(pool, 0) != cudaSuccess ||
+          cudaMallocAsync(&p, bytes, c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+      }
     }
     want = bytes;
   }
@@ -245,6 +255,10 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
   if (!strcmp(key, "profile")) {
     thc::clear_profile(&h->c);
     h->c.profile = value != 0.0;
+    return THC_OK;
+  }
+  if (!strcmp(key, "fft64")) {
+    h->c.fft64 = value != 0.0;
     return THC_OK;
   }
   if (!strcmp(key, "slices_z")) {

@@ -78,10 +78,14 @@ struct Ctx {
   long long launches = 0;
   int slices_p = 6;
   int slices_z = 6;
-  int slices_m = 4;
+  // The Coulomb product's rows span many binades (sqrt(v) ~ 1/|G| on top of the decay of
+  // zeta_hat): 4 slices leave 1.3e-6 on M at N_g 1.26e6 (a bias from the dropped level-4
+  // pairs on the diagonal), 5 slices 2.7e-7.
+  int slices_m = 5;
   int gemm_tc = 1;      // 1: tcgen05 sliced GEMM, 0: mma.sync sliced GEMM
   int km_prune = 1;     // 1: spatially pruned k-means assign, 0: exhaustive
   int use_graphs = 1;   // capture the k-means iteration block in a CUDA graph
+  int fft64 = 0;        // mixed path: zeta in FP64 and a D2Z FFT (else FP32 and R2C)
   // Instantiated k-means iteration graphs, most recently used last, keyed by every kernel
   // argument they bake in.
   std::vector<std::pair<std::vector<long long>, cudaGraphExec_t>> km_graphs;

@@ -167,6 +167,29 @@ int get_plan(Ctx* c, int n0, int n1, int n2, int batch, cufftType type, cufftHan
   return THC_OK;
 }
 
+int fft_forward(Ctx* c, int n0, int n1, int n2, int count, cufftType type, void* in, void* out)
+{
+  const long long ng = (long long)n0 * n1 * n2;
+  const long long nc = (long long)n0 * n1 * (n2 / 2 + 1);
+  const size_t esz = type == CUFFT_D2Z ? sizeof(double) : sizeof(float);
+  for (int f0 = 0; f0 < count; f0 += kFftChunk) {
+    const int nb = std::min(kFftChunk, count - f0);
+    cufftHandle plan;
+    int st = get_plan(c, n0, n1, n2, nb, type, &plan);
+    if (st) return st;
+    char* src = (char*)in + esz * ng * f0;
+    char* dst = (char*)out + 2 * esz * nc * f0;
+    cufftResult r = type == CUFFT_D2Z
+        ? cufftExecD2Z(plan, (double*)src, (cufftDoubleComplex*)dst)
+        : cufftExecR2C(plan, (float*)src, (cufftComplex*)dst);
+    if (r != CUFFT_SUCCESS)
+      return set_error(c, THC_ERR_CUFFT, "cufftExec%s failed (%d)",
+                       type == CUFFT_D2Z ? "D2Z" : "R2C", (int)r);
+    c->launches++;
+  }
+  return THC_OK;
+}
+
 int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_in, int nmu,
              const int* mesh_in, const double* coul_in, double shift_rel, double* out_orb,
              double* out_M, double* out_L, thc_isdf_stats* stats)
@@ -299,11 +322,7 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
     if ((st = dgemm(c, g))) return st;
   }
   // FFT of every interpolating vector.
-  cufftHandle plan;
-  if ((st = get_plan(c, n0, n1, n2, nmu, CUFFT_D2Z, &plan))) return st;
-  if (cufftExecD2Z(plan, zeta, (cufftDoubleComplex*)zhat) != CUFFT_SUCCESS)
-    return set_error(c, THC_ERR_CUFFT, "cufftExecD2Z failed");
-  c->launches++;
+  if ((st = fft_forward(c, n0, n1, n2, nmu, CUFFT_D2Z, zeta, zhat))) return st;
   coulomb_weights<<<(int)cdiv(nc, 256), 256, 0, s>>>(coul, n0, n1, n2, dsym, danti, n_anti);
   THC_LAUNCHED(c, "coulomb_weights");
   int h_anti = 0;

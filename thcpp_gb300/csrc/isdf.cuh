@@ -6,6 +6,13 @@ namespace thc {
 
 int get_plan(Ctx* c, int n0, int n1, int n2, int batch, cufftType type, cufftHandle* out);
 
+// Forward real-to-complex FFTs of `count` real n0 x n1 x n2 fields stored back to back (`in`)
+// into their half spectra (`out`, n0 n1 (n2/2+1) complex each); `type` is CUFFT_D2Z or
+// CUFFT_R2C.  Runs in chunks of at most kFftChunk fields so that cuFFT's work area stays a
+// few GB at the largest meshes.
+constexpr int kFftChunk = 1024;
+int fft_forward(Ctx* c, int n0, int n1, int n2, int count, cufftType type, void* in, void* out);
+
 int isdf_run(Ctx* c, const double* phi, long long ng, int no, const int* idx, int nmu,
              const int* mesh, const double* coul, double shift_rel, double* out_orb,
              double* out_M, double* out_L, thc_isdf_stats* stats);

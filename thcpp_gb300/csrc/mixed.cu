@@ -1,7 +1,8 @@
 // Mixed-precision ISDF: the same quantities as isdf.cu with the three large products on
 // the BF16 tensor cores through error-free slicing (ozgemm):
 //   Z      = (Phi Phi_mu^T)^2      sliced GEMM, FP64 result, squared in the epilogue
-//   zeta^T = C^{-1} Z^T            sliced GEMM, FP32 result (input of the FP32 FFT)
+//   zeta^T = C^{-1} Z^T            sliced GEMM, FP32 result (input of the FP32 FFT; FP64
+//                                  and a D2Z FFT with the fft64 option)
 //   Re M   = A A^T, A = zeta_hat * sqrt(w v_sym)  sliced GEMM over the half spectrum
 // C, its Cholesky factor and C^{-1} stay FP64 (C is ill-conditioned: cond ~1e6-1e9), and
 // so does the Cholesky factorisation of M.  The slice depths fix the accuracy: each
@@ -43,7 +44,8 @@ __global__ void gather_rows_m(const double* __restrict__ phi, long long ng, int 
 }
 
 __global__ void coulomb_weights_m(const double* __restrict__ v, int n0, int n1, int n2,
-                                  double* dsym, double* danti, float* sq, int* n_anti)
+                                  double* dsym, double* danti, float* sq, double* sqd,
+                                  int* n_anti)
 {
   int nc = n2 / 2 + 1;
   long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -58,14 +60,18 @@ __global__ void coulomb_weights_m(const double* __restrict__ v, int n0, int n1, 
   double w = (k2 == 0 || (n2 % 2 == 0 && k2 == n2 / 2)) ? 1.0 : 2.0;
   double ds = w * 0.5 * (vp + vn);
   dsym[e] = ds;
-  sq[e] = (float)sqrt(fmax(ds, 0.0));
+  const double rt = sqrt(fmax(ds, 0.0));
+  sq[e] = (float)rt;
+  if (sqd) sqd[e] = rt;
   double a = w * 0.5 * (vp - vn);
   danti[e] = a;
   if (a != 0.0) atomicAdd(n_anti, 1);
 }
 
-// X[mu, nu] = sum_c danti[c] Re zh[mu, c] Im zh[nu, c] over the points with danti != 0.
-__global__ void imag_part_c64(const float2* __restrict__ zh, long long nc, int nmu,
+// X[mu, nu] = sum_c danti[c] Re zh[mu, c] Im zh[nu, c] over the points with danti != 0
+// (zh: float2 or double2 half spectra).
+template <typename Cplx>
+__global__ void imag_part_c64(const Cplx* __restrict__ zh, long long nc, int nmu,
                               const double* __restrict__ danti, double* X)
 {
   long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -156,10 +162,21 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   double* phimu = (double*)ws_get(c, WS_PHIMU, sizeof(double) * nmu * no);
   double* C = (double*)ws_get(c, WS_C, sizeof(double) * 2 * nn);
   double* Cinv = (double*)ws_get(c, WS_CINV, sizeof(double) * nn);
-  float2* zg = (float2*)ws_get(c, WS_ZT, sizeof(float2) * nmu * ng);   // Z: N_g x N_mu, double-word
-  float* zeta = (float*)ws_get(c, WS_ZETA, sizeof(float) * nmu * ng);
-  float2* zhat = (float2*)ws_get(c, WS_ZHAT, sizeof(float2) * nmu * nc);
-  double* dsym = (double*)ws_get(c, WS_DSYM, (sizeof(double) + sizeof(float)) * nc + 64);
+  // One region holds Z (N_g x N_mu double-word) and, once Z has been sliced, zeta followed
+  // by zeta_hat: the three never live at the same time, which keeps the largest cells
+  // (N_g 1.26e6, N_mu 5184) inside HBM.  zeta and zeta_hat are FP32 (R2C FFT) or, with the
+  // context's fft64 option, FP64 (D2Z FFT).
+  const bool f64fft = c->fft64 != 0;
+  const size_t real_sz = f64fft ? sizeof(double) : sizeof(float);
+  const size_t zeta_bytes = ((real_sz * (size_t)nmu * ng + 255) / 256) * 256;
+  const size_t zreg_bytes = std::max(sizeof(float2) * (size_t)nmu * ng,
+                                     zeta_bytes + 2 * real_sz * (size_t)nmu * nc);
+  char* zreg = (char*)ws_get(c, WS_ZT, zreg_bytes);
+  float2* zg = (float2*)zreg;                      // Z: N_g x N_mu, double-word
+  void* zeta = zreg;                               // zeta^T: N_mu x N_g (after Z is sliced)
+  void* zhat = zreg + zeta_bytes;                  // N_mu x N_c complex
+  // dsym (FP64), sqrt(dsym) in FP64, then sqrt(dsym) in FP32.
+  double* dsym = (double*)ws_get(c, WS_DSYM, (2 * sizeof(double) + sizeof(float)) * nc + 64);
   double* danti = (double*)ws_get(c, WS_DANTI, sizeof(double) * nc);
   double* Mw = (double*)ws_get(c, WS_M, sizeof(double) * 4 * nn);
   double* Lw = (double*)ws_get(c, WS_L, sizeof(double) * 2 * nn);
@@ -168,16 +185,19 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   double* dinv = (double*)ws_get(c, WS_DINV, sizeof(double) * (nblk64 * 64 * 64 + nn + 64 * (long long)nmu));
   double* Xinv = dinv + nblk64 * 64 * 64;
   double* Tinv = Xinv + nn;
-  size_t a_elems = std::max({(size_t)sp * ng_pad * no_kpad, (size_t)sz * mu_pad * mu_kpad,
+  // Slices: A holds Phi's, then C^{-1}'s / X's; B holds Phi_mu's, Z's (or Y's), then,
+  // once the solve is done, zeta_hat's for the Coulomb contraction.
+  size_t a_elems = std::max((size_t)sp * ng_pad * no_kpad, (size_t)sz * mu_pad * mu_kpad);
+  size_t b_elems = std::max({(size_t)sp * mu_pad * no_kpad, (size_t)sz * ng_pad * mu_kpad,
                              (size_t)sm * mu_pad * k2_pad});
-  size_t b_elems = std::max((size_t)sp * mu_pad * no_kpad, (size_t)sz * ng_pad * mu_kpad);
   __nv_bfloat16* sa = (__nv_bfloat16*)ws_get(c, WS_SLICE_A, sizeof(__nv_bfloat16) * a_elems);
   __nv_bfloat16* sb = (__nv_bfloat16*)ws_get(c, WS_SLICE_B, sizeof(__nv_bfloat16) * b_elems);
   int* ex = (int*)ws_get(c, WS_SLICE_E, sizeof(int) * (mu_pad + ng_pad + 64));
   if (!phimu || !C || !Cinv || !zg || !zeta || !zhat || !dsym || !danti || !Mw || !Lw || !scr || !dinv ||
       !sa || !sb || !ex)
     return set_error(c, THC_ERR_NOMEM, "thc_isdf (mixed): workspace allocation failed");
-  float* sq = (float*)(dsym + nc);
+  double* sqd = dsym + nc;
+  float* sq = (float*)(dsym + 2 * nc);
   int* ea = ex;
   int* eb = ex + mu_pad;
   CholStatus* cs = (CholStatus*)scr;
@@ -319,7 +339,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     g.a.s = sa; g.a.e = ea; g.a.ld = mu_kpad; g.a.slice_stride = mu_pad * mu_kpad;
     g.b.s = sb; g.b.e = eb; g.b.ld = mu_kpad; g.b.slice_stride = ng_pad * mu_kpad;
     g.b.k_contig = true;
-    g.levels = sz; g.epilogue = OZ_STORE_F32; g.C = zeta; g.ldc = ng;
+    g.levels = sz; g.epilogue = f64fft ? OZ_STORE_F64 : OZ_STORE_F32; g.C = zeta; g.ldc = ng;
     if ((st = gemm(g))) return st;
   } else {
     if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, sz, sa, mu_kpad,
@@ -333,30 +353,32 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     g.a.s = sa; g.a.e = ea; g.a.ld = mu_kpad; g.a.slice_stride = mu_pad * mu_kpad;
     g.b.s = sb; g.b.e = eb; g.b.ld = mu_kpad; g.b.slice_stride = ng_pad * mu_kpad;
     g.b.k_contig = true;
-    g.levels = sz; g.epilogue = OZ_STORE_F32; g.C = zeta; g.ldc = ng;
+    g.levels = sz; g.epilogue = f64fft ? OZ_STORE_F64 : OZ_STORE_F32; g.C = zeta; g.ldc = ng;
     if ((st = gemm(g))) return st;
   }
-  // FP32 R2C FFT of every interpolating vector.
-  cufftHandle plan;
-  if ((st = get_plan(c, n0, n1, n2, nmu, CUFFT_R2C, &plan))) return st;
-  if (cufftExecR2C(plan, zeta, (cufftComplex*)zhat) != CUFFT_SUCCESS)
-    return set_error(c, THC_ERR_CUFFT, "cufftExecR2C failed");
-  c->launches++;
-  coulomb_weights_m<<<(int)cdiv(nc, 256), 256, 0, s>>>(coul, n0, n1, n2, dsym, danti, sq, n_anti);
+  // R2C (FP32) or D2Z (FP64) FFT of every interpolating vector.
+  if ((st = fft_forward(c, n0, n1, n2, nmu, f64fft ? CUFFT_D2Z : CUFFT_R2C, zeta, zhat)))
+    return st;
+  coulomb_weights_m<<<(int)cdiv(nc, 256), 256, 0, s>>>(coul, n0, n1, n2, dsym, danti, sq,
+                                                       f64fft ? sqd : nullptr, n_anti);
   THC_LAUNCHED(c, "coulomb_weights");
   int h_anti = 0;
   THC_CUDA(c, cudaMemcpyAsync(&h_anti, n_anti, sizeof(int), cudaMemcpyDeviceToHost, s));
   // Re M (lower) = A A^T with A = zeta_hat (interleaved re, im) scaled by sqrt(w v_sym).
-  if ((st = oz_slice_rows_f32(c, (const float*)zhat, nmu, 2 * nc, 2 * nc, sq, 1, sm, sa, k2_pad,
-                              mu_pad * k2_pad, ea, mu_pad)))
-    return st;
+  if (f64fft)
+    st = oz_slice_rows_f64(c, (const double*)zhat, nmu, 2 * nc, 2 * nc, 1, sqd, 1, sm, sb,
+                           k2_pad, mu_pad * k2_pad, ea, mu_pad);
+  else
+    st = oz_slice_rows_f32(c, (const float*)zhat, nmu, 2 * nc, 2 * nc, sq, 1, sm, sb, k2_pad,
+                           mu_pad * k2_pad, ea, mu_pad);
+  if (st) return st;
   double* mre = Mw;
   double* xim = Mw + nn;
   double* mcx = Mw + 2 * nn;
   {
     OzArgs g;
     g.M = nmu; g.N = nmu; g.K = 2 * nc;
-    g.a.s = sa; g.a.e = ea; g.a.ld = k2_pad; g.a.slice_stride = mu_pad * k2_pad;
+    g.a.s = sb; g.a.e = ea; g.a.ld = k2_pad; g.a.slice_stride = mu_pad * k2_pad;
     g.b = g.a;
     g.b.k_contig = true;
     g.levels = sm; g.epilogue = OZ_STORE_F64; g.C = mre; g.ldc = nmu; g.lower_only = 1;
@@ -371,7 +393,10 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   THC_CUDA(c, cudaStreamSynchronize(s));
   int nb2 = (int)cdiv(nn, 256);
   if (h_anti > 0) {
-    imag_part_c64<<<nb2, 256, 0, s>>>(zhat, nc, nmu, danti, xim);
+    if (f64fft)
+      imag_part_c64<<<nb2, 256, 0, s>>>((const double2*)zhat, nc, nmu, danti, xim);
+    else
+      imag_part_c64<<<nb2, 256, 0, s>>>((const float2*)zhat, nc, nmu, danti, xim);
     THC_LAUNCHED(c, "imag_part_c64");
   }
   assemble_m_m<<<nb2, 256, 0, s>>>(mre, h_anti > 0 ? xim : nullptr, nmu, mcx);

@@ -175,12 +175,38 @@ def loewdin(phi: np.ndarray, volume: float) -> np.ndarray:
     return phi @ (u * (1.0 / np.sqrt(w))) @ u.T
 
 
+def draw_parameters(atoms, norb, seed):
+    """The seeded exponents (one per function, atom-major s, px, py, pz) and mixing matrix."""
+    rng = np.random.default_rng(seed)
+    alphas = rng.uniform(0.3, 1.5, size=4 * atoms.shape[0])
+    mix = rng.standard_normal((norb, norb))
+    return alphas, mix
+
+
+def image_centres(lattice, atoms, alphas, nfunc):
+    """The atom + lattice-translation centres that gaussian_sp_basis sums over, grouped by
+    atom (same filter), with their atom indices and the cutoff radius."""
+    amin = float(np.min(alphas[:nfunc]))
+    rcut = math.sqrt(40.0 / amin)
+    trans = _images(lattice, rcut)
+    centre = 0.5 * lattice.sum(axis=0)
+    corners = np.array([[i, j, k] for i in (0, 1) for j in (0, 1) for k in (0, 1)]) @ lattice
+    cell_r = float(np.max(np.linalg.norm(corners - centre, axis=1)))
+    cen, cat = [], []
+    for a in range((nfunc + 3) // 4):
+        for t in trans:
+            pos = atoms[a] + t
+            if np.linalg.norm(pos - centre) > cell_r + rcut:
+                continue
+            cen.append(pos)
+            cat.append(a)
+    return (np.ascontiguousarray(np.array(cen, np.float64).reshape(-1, 3)),
+            np.array(cat, np.int32), rcut)
+
+
 def make_system(name, lattice, atoms, mesh, norb, cfac, seed, kmeans_seed,
                 max_it=100, threshold=1e-6) -> System:
-    rng = np.random.default_rng(seed)
-    nfunc_all = 4 * atoms.shape[0]
-    alphas = rng.uniform(0.3, 1.5, size=nfunc_all)
-    mix = rng.standard_normal((norb, norb))
+    alphas, mix = draw_parameters(atoms, norb, seed)
     grid = uniform_grid(lattice, mesh)
     raw = gaussian_sp_basis(grid, lattice, atoms, alphas, norb)
     vol = abs(np.linalg.det(lattice))
@@ -200,29 +226,34 @@ def diamond_supercell(rep: int):
     return lat, atoms
 
 
-def config(name: str) -> System:
-    """The named workload: 'c1', 'c2', 'c3', 'c5' (and 'tiny' for unit tests)."""
+def config_args(name: str):
+    """make_system arguments of the named workload ('c1', 'c2', 'c3', 'c5', 'tiny', 'c4_<s>')."""
     if name == "c1":
         a = A_DIAMOND
         lat = 0.5 * a * np.array([[0.0, 1.0, 1.0], [1.0, 0.0, 1.0], [1.0, 1.0, 0.0]])
         atoms = np.array([[0.0, 0.0, 0.0], [0.25 * a, 0.25 * a, 0.25 * a]])
-        return make_system("c1", lat, atoms, (24, 24, 24), 8, 8, 1001, 18)
+        return ("c1", lat, atoms, (24, 24, 24), 8, 8, 1001, 18)
     if name == "c2":
         lat, atoms = diamond_supercell(1)
-        return make_system("c2", lat, atoms, (48, 48, 48), 32, 8, 1002, 19)
+        return ("c2", lat, atoms, (48, 48, 48), 32, 8, 1002, 19)
     if name == "c3":
         lat, atoms = diamond_supercell(2)
-        return make_system("c3", lat, atoms, (72, 72, 72), 256, 8, 1003, 20)
+        return ("c3", lat, atoms, (72, 72, 72), 256, 8, 1003, 20)
     if name == "c5":
         lat, atoms = diamond_supercell(3)
-        return make_system("c5", lat, atoms, (108, 108, 108), 864, 6, 1005, 22)
+        return ("c5", lat, atoms, (108, 108, 108), 864, 6, 1005, 22)
     if name == "tiny":
         # A small cubic cell used by unit tests: 8 atoms, 16^3 mesh, N_o = 12, N_mu = 48.
         lat, atoms = diamond_supercell(1)
-        return make_system("tiny", lat, atoms, (16, 16, 16), 12, 4, 1099, 99)
+        return ("tiny", lat, atoms, (16, 16, 16), 12, 4, 1099, 99)
     if name.startswith("c4_"):
-        return c4_system(int(name[3:]))
+        return c4_args(int(name[3:]))
     raise KeyError(name)
+
+
+def config(name: str) -> System:
+    """The named workload: 'c1', 'c2', 'c3', 'c5' (and 'tiny' for unit tests)."""
+    return make_system(*config_args(name))
 
 
 _SMOOTH = sorted({2**a * 3**b * 5**c * 7**d for a in range(7) for b in range(4)
@@ -239,8 +270,8 @@ _C4_KMEANS_SEED = {1: 23, 23: 23}
 _C4_REDRAW = {47: 1}
 
 
-def c4_system(s: int) -> System:
-    """System ``s`` (0..47) of the batched workload.
+def c4_args(s: int):
+    """make_system arguments of system ``s`` (0..47) of the batched workload.
 
     Cubic cell with edge L ~ U[6, 14] bohr; N_o ~ U{16..200}; ceil(N_o/4) atoms placed
     uniformly at random with minimum-image separation >= 2.5 bohr (L is redrawn when the
@@ -273,8 +304,13 @@ def c4_system(s: int) -> System:
         if len(pos) == natom:
             break
     lat = edge * np.eye(3)
-    return make_system(f"c4_{s}", lat, np.array(pos), (n, n, n), norb, cfac,
-                       5000 + s + 100000 * _C4_REDRAW.get(s, 0), _C4_KMEANS_SEED.get(s, 17 + 4))
+    return (f"c4_{s}", lat, np.array(pos), (n, n, n), norb, cfac,
+            5000 + s + 100000 * _C4_REDRAW.get(s, 0), _C4_KMEANS_SEED.get(s, 17 + 4))
+
+
+def c4_system(s: int) -> System:
+    """System ``s`` (0..47) of the batched workload (see :func:`c4_args`)."""
+    return make_system(*c4_args(s))
 
 
 def write_orbital_file(system: System, path: str, half_rotate: bool = False) -> None:
@@ -314,3 +350,69 @@ def input_json(system: System, orbital_file: str, output_file: str, **gpu) -> di
     if gpu:
         d["gpu"] = gpu
     return d
+
+
+@dataclasses.dataclass
+class DeviceSystem:
+    """A synthetic system generated on the GPU: grid, phi, density and coulG are device
+    tensors (FP64); the other fields match :class:`System`."""
+    name: str
+    lattice: np.ndarray
+    atoms: np.ndarray
+    mesh: tuple
+    grid: object
+    phi: object
+    density: object
+    coulG: object
+    thc_cfac: int
+    max_it: int = 100
+    threshold: float = 1e-6
+    rng_seed: int = 17
+
+    @property
+    def ng(self) -> int:
+        return int(self.grid.shape[0])
+
+    @property
+    def norb(self) -> int:
+        return int(self.phi.shape[1])
+
+    @property
+    def nmu(self) -> int:
+        return self.thc_cfac * self.norb
+
+
+def make_system_gpu(name, lattice, atoms, mesh, norb, cfac, seed, kmeans_seed, ctx, device,
+                    max_it=100, threshold=1e-6) -> DeviceSystem:
+    """make_system with the basis evaluated on the GPU (thc_synth_gaussian_basis) and the
+    mixing, Loewdin orthonormalisation and density formed there (FP64).  Same draws as
+    make_system; orbitals agree with it to ~1e-6 relative (FP32 Gaussians)."""
+    import torch
+    alphas, mix = draw_parameters(atoms, norb, seed)
+    grid = uniform_grid(lattice, mesh)
+    ng = grid.shape[0]
+    cen, cat, rcut = image_centres(lattice, atoms, alphas, norb)
+    d_grid = torch.from_numpy(grid).to(device)
+    torch.cuda.synchronize(device)
+    raw = torch.empty((ng, norb), dtype=torch.float64, device=device)
+    ctx.gaussian_basis(d_grid, mesh, cen, cat, np.ascontiguousarray(alphas), norb, rcut, raw)
+    phi0 = raw @ torch.from_numpy(mix).to(device)
+    del raw
+    vol = abs(np.linalg.det(lattice))
+    s_mat = ((vol / ng) * (phi0.T @ phi0)).cpu().numpy()
+    w, u = np.linalg.eigh(s_mat)
+    phi = phi0 @ torch.from_numpy((u * (1.0 / np.sqrt(w))) @ u.T).to(device)
+    del phi0
+    nocc = norb // 2
+    dens = (phi[:, :nocc] * phi[:, :nocc]).sum(dim=1)
+    coul = torch.from_numpy(coulomb_g(lattice, mesh)).to(device)
+    torch.cuda.synchronize(device)
+    return DeviceSystem(name=name, lattice=lattice, atoms=atoms,
+                        mesh=tuple(int(m) for m in mesh), grid=d_grid, phi=phi.contiguous(),
+                        density=dens.contiguous(), coulG=coul, thc_cfac=cfac, max_it=max_it,
+                        threshold=threshold, rng_seed=kmeans_seed)
+
+
+def config_gpu(name: str, ctx, device) -> DeviceSystem:
+    """The named workload generated on the GPU (see :func:`make_system_gpu`)."""
+    return make_system_gpu(*config_args(name), ctx=ctx, device=device)
