@@ -447,6 +447,7 @@ int dgemm(Ctx* c, const GemmArgs& g_in)
 int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs,
               double* dinv)
 {
+  ProfScope prof(c, "potrf_inv");
   cudaStream_t s = c->stream;
   for (int k0 = 0; k0 < n; k0 += NB) {
     int nb = std::min(NB, n - k0);
@@ -488,6 +489,7 @@ int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholSta
 int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* dinv, double* X,
                  double* T, double* Cinv, const CholStatus* cs)
 {
+  ProfScope prof(c, "chol_inverse");
   cudaStream_t s = c->stream;
   THC_CUDA(c, cudaMemsetAsync(X, 0, sizeof(double) * (size_t)n * ld, s));
   int nblk = (n + NB - 1) / NB;

@@ -172,6 +172,7 @@ int fft_forward(Ctx* c, int n0, int n1, int n2, int count, cufftType type, void*
   const long long ng = (long long)n0 * n1 * n2;
   const long long nc = (long long)n0 * n1 * (n2 / 2 + 1);
   const size_t esz = type == CUFFT_D2Z ? sizeof(double) : sizeof(float);
+  ProfScope prof(c, "fft");
   for (int f0 = 0; f0 < count; f0 += kFftChunk) {
     const int nb = std::min(kFftChunk, count - f0);
     cufftHandle plan;

@@ -1212,6 +1212,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   KmAlloc ws_alloc;
   ws_alloc.c = c;
   KmAlloc& al = fixed ? *fixed : ws_alloc;
+  ProfScope prof_all(fixed ? nullptr : c, "kmeans");
   if (!grid_in || !rho_in || !init_in || !out_idx || ng <= 0 || nmu <= 0 || nmu > ng ||
       max_it < 1 || ng > 0x7fffffffLL)
     return set_error(c, THC_ERR_ARG, "thc_kmeans: invalid arguments");

@@ -213,6 +213,12 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   if (out_orb) orb_dev = is_device_ptr(out_orb) ? out_orb : Lw;
   THC_CUDA(c, cudaMemsetAsync(scr + 512, 0, 64, s));
   auto gemm = [&](const OzArgs& g) { return c->gemm_tc ? ozgemm_tc(c, g, gemm_err) : ozgemm(c, g); };
+  // Slice buffers are k-tiled (both GEMM kernels read either layout).
+  auto slices = [&](__nv_bfloat16* buf, int* e, long long rows_pad, long long kpad, int ns) {
+    SliceBuf b;
+    b.s = buf; b.e = e; b.rows_pad = rows_pad; b.kpad = kpad; b.ns = ns; b.tiled = true;
+    return b;
+  };
   THC_CUDA(c, cudaEventRecord(c->ev0, s));
 
   gather_rows_m<<<(int)cdiv((long long)nmu * no, 256), 256, 0, s>>>(phi, ng, no, idx, nmu, phimu,
@@ -248,19 +254,16 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   // B = Phi_mu sliced by interpolating point; Z's rows are then K-contiguous for the solve.
   // Z is kept as double-word FP32 (~46 bits; the solve slices it to 42), so the epilogue
   // squares in FP32 arithmetic instead of on the narrow FP64 pipe.
-  if ((st = oz_slice_rows_f64(c, phi, ng, no, no, 1, nullptr, 0, sp, sa, no_kpad,
-                              ng_pad * no_kpad, eb, ng_pad)))
-    return st;
-  if ((st = oz_slice_rows_f64(c, phimu, nmu, no, no, 1, nullptr, 0, sp, sb, no_kpad,
-                              mu_pad * no_kpad, ea, mu_pad)))
-    return st;
   {
+    const SliceBuf pa = slices(sa, eb, ng_pad, no_kpad, sp), pb = slices(sb, ea, mu_pad, no_kpad, sp);
+    if ((st = oz_slice_rows_f64(c, phi, ng, no, no, 1, nullptr, 0, pa))) return st;
+    if ((st = oz_slice_rows_f64(c, phimu, nmu, no, no, 1, nullptr, 0, pb))) return st;
     OzArgs g;
     g.M = ng; g.N = nmu; g.K = no;
-    g.a.s = sa; g.a.e = eb; g.a.ld = no_kpad; g.a.slice_stride = ng_pad * no_kpad;
-    g.b.s = sb; g.b.e = ea; g.b.ld = no_kpad; g.b.slice_stride = mu_pad * no_kpad;
-    g.b.k_contig = true;
+    g.a = pa.operand();
+    g.b = pb.operand();
     g.levels = sp; g.epilogue = OZ_SQUARE_DW; g.C = zg; g.ldc = nmu;
+    g.tag = "oz_P";
     if ((st = gemm(g))) return st;
   }
   CholStatus hcs{};
@@ -288,15 +291,15 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
                          cs)))
     return st;
   if (cinv_tc) {
-    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, 1, nmu, nullptr, 0, sz, sa, mu_kpad,
-                                mu_pad * mu_kpad, ea, mu_pad)))   // rows of X^T
+    const SliceBuf xt = slices(sa, ea, mu_pad, mu_kpad, sz);
+    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, 1, nmu, nullptr, 0, xt)))   // rows of X^T
       return st;
     OzArgs g;
     g.M = nmu; g.N = nmu; g.K = nmu;
-    g.a.s = sa; g.a.e = ea; g.a.ld = mu_kpad; g.a.slice_stride = mu_pad * mu_kpad;
+    g.a = xt.operand();
     g.b = g.a;
-    g.b.k_contig = true;
     g.levels = sz; g.epilogue = OZ_STORE_F64; g.C = Cinv; g.ldc = nmu;
+    g.tag = "oz_cinv";
     g.ksplit = oz_choose_split(nmu, nmu, nmu, false);
     if (g.ksplit > 1) {
       g.part = (double*)ws_get(c, WS_PART, sizeof(double) * g.ksplit * nn);
@@ -313,47 +316,37 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     // X instead, each amplifying by ~1/sqrt(shift) only: Y^T = Z X^T, then
     // zeta^T = X^T Y.  (Emulated on the C1 cell this is also more accurate than the FP64
     // C^{-1} product: pair-Coulomb invariant 1.7e-8 against 2.2e-6.)
-    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, sz, sb, mu_kpad, ng_pad * mu_kpad, eb,
-                               ng_pad)))
-      return st;
-    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, nmu, 1, nullptr, 0, sz, sa, mu_kpad,
-                                mu_pad * mu_kpad, ea, mu_pad)))
-      return st;
+    const SliceBuf zs = slices(sb, eb, ng_pad, mu_kpad, sz), xs = slices(sa, ea, mu_pad, mu_kpad, sz);
+    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs))) return st;
+    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, nmu, 1, nullptr, 0, xs))) return st;   // rows of X
     {
       OzArgs g;                                  // Y^T (N_g x N_mu) = Z X^T, into zg
       g.M = ng; g.N = nmu; g.K = nmu;
-      g.a.s = sb; g.a.e = eb; g.a.ld = mu_kpad; g.a.slice_stride = ng_pad * mu_kpad;
-      g.b.s = sa; g.b.e = ea; g.b.ld = mu_kpad; g.b.slice_stride = mu_pad * mu_kpad;
-      g.b.k_contig = true;
+      g.a = zs.operand();
+      g.b = xs.operand();
       g.levels = sz; g.epilogue = OZ_STORE_DW; g.C = zg; g.ldc = nmu;
+      g.tag = "oz_Y";
       if ((st = gemm(g))) return st;
     }
-    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, 1, nmu, nullptr, 0, sz, sa, mu_kpad,
-                                mu_pad * mu_kpad, ea, mu_pad)))   // rows of X^T
-      return st;
-    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, sz, sb, mu_kpad, ng_pad * mu_kpad, eb,
-                               ng_pad)))
-      return st;
+    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, 1, nmu, nullptr, 0, xs))) return st;   // rows of X^T
+    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs))) return st;                    // rows of Y^T
     OzArgs g;                                    // zeta^T = X^T Y
     g.M = nmu; g.N = ng; g.K = nmu;
-    g.a.s = sa; g.a.e = ea; g.a.ld = mu_kpad; g.a.slice_stride = mu_pad * mu_kpad;
-    g.b.s = sb; g.b.e = eb; g.b.ld = mu_kpad; g.b.slice_stride = ng_pad * mu_kpad;
-    g.b.k_contig = true;
+    g.a = xs.operand();
+    g.b = zs.operand();
     g.levels = sz; g.epilogue = f64fft ? OZ_STORE_F64 : OZ_STORE_F32; g.C = zeta; g.ldc = ng;
+    g.tag = "oz_zeta";
     if ((st = gemm(g))) return st;
   } else {
-    if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, sz, sa, mu_kpad,
-                                mu_pad * mu_kpad, ea, mu_pad)))
-      return st;
-    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, sz, sb, mu_kpad, ng_pad * mu_kpad, eb,
-                               ng_pad)))
-      return st;
+    const SliceBuf ci = slices(sa, ea, mu_pad, mu_kpad, sz), zs = slices(sb, eb, ng_pad, mu_kpad, sz);
+    if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, ci))) return st;
+    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs))) return st;
     OzArgs g;
     g.M = nmu; g.N = ng; g.K = nmu;
-    g.a.s = sa; g.a.e = ea; g.a.ld = mu_kpad; g.a.slice_stride = mu_pad * mu_kpad;
-    g.b.s = sb; g.b.e = eb; g.b.ld = mu_kpad; g.b.slice_stride = ng_pad * mu_kpad;
-    g.b.k_contig = true;
+    g.a = ci.operand();
+    g.b = zs.operand();
     g.levels = sz; g.epilogue = f64fft ? OZ_STORE_F64 : OZ_STORE_F32; g.C = zeta; g.ldc = ng;
+    g.tag = "oz_zeta";
     if ((st = gemm(g))) return st;
   }
   // R2C (FP32) or D2Z (FP64) FFT of every interpolating vector.
@@ -365,12 +358,11 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   int h_anti = 0;
   THC_CUDA(c, cudaMemcpyAsync(&h_anti, n_anti, sizeof(int), cudaMemcpyDeviceToHost, s));
   // Re M (lower) = A A^T with A = zeta_hat (interleaved re, im) scaled by sqrt(w v_sym).
+  const SliceBuf zh = slices(sb, ea, mu_pad, k2_pad, sm);
   if (f64fft)
-    st = oz_slice_rows_f64(c, (const double*)zhat, nmu, 2 * nc, 2 * nc, 1, sqd, 1, sm, sb,
-                           k2_pad, mu_pad * k2_pad, ea, mu_pad);
+    st = oz_slice_rows_f64(c, (const double*)zhat, nmu, 2 * nc, 2 * nc, 1, sqd, 1, zh);
   else
-    st = oz_slice_rows_f32(c, (const float*)zhat, nmu, 2 * nc, 2 * nc, sq, 1, sm, sb, k2_pad,
-                           mu_pad * k2_pad, ea, mu_pad);
+    st = oz_slice_rows_f32(c, (const float*)zhat, nmu, 2 * nc, 2 * nc, sq, 1, zh);
   if (st) return st;
   double* mre = Mw;
   double* xim = Mw + nn;
@@ -378,10 +370,10 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   {
     OzArgs g;
     g.M = nmu; g.N = nmu; g.K = 2 * nc;
-    g.a.s = sb; g.a.e = ea; g.a.ld = k2_pad; g.a.slice_stride = mu_pad * k2_pad;
+    g.a = zh.operand();
     g.b = g.a;
-    g.b.k_contig = true;
     g.levels = sm; g.epilogue = OZ_STORE_F64; g.C = mre; g.ldc = nmu; g.lower_only = 1;
+    g.tag = "oz_M";
     // Long K (2 N_c) and a small N_mu x N_mu output: split K over CTAs.
     g.ksplit = oz_choose_split(nmu, nmu, 2 * nc, true);
     if (g.ksplit > 1) {

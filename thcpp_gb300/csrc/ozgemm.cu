@@ -97,17 +97,22 @@ __global__ void __launch_bounds__(128, 2) ozgemm_kernel(OzArgs g)
     __nv_bfloat16* dB = sB + buf * b_stage;
 #pragma unroll
     for (int s = 0; s < LV; s++) {
-      const __nv_bfloat16* ga = g.a.s + s * g.a.slice_stride + m0 * g.a.ld + k0;
+      // Row stride and first element of this slice's k tile (plain or tiled storage).
+      const long long lda = g.a.kt_stride ? 32 : g.a.ld;
+      const __nv_bfloat16* ga = g.a.s + (g.a.kt_stride ? (k0 >> 5) * g.a.kt_stride + s * g.a.slice_stride + m0 * 32
+                                                       : s * g.a.slice_stride + m0 * g.a.ld + k0);
 #pragma unroll
       for (int r = 0; r < 2; r++) {
         int ch = tid + 128 * r;        // 256 chunks of 16 B: 64 rows x 4
         int row = ch >> 2, col = (ch & 3) * 8;
-        cp_async16(dA + (s * OBM + row) * OLDA + col, ga + row * g.a.ld + col);
+        cp_async16(dA + (s * OBM + row) * OLDA + col, ga + row * lda + col);
       }
       if (BK) {
-        const __nv_bfloat16* gb = g.b.s + s * g.b.slice_stride + n0 * g.b.ld + k0;
+        const long long ldb = g.b.kt_stride ? 32 : g.b.ld;
+        const __nv_bfloat16* gb = g.b.s + (g.b.kt_stride ? (k0 >> 5) * g.b.kt_stride + s * g.b.slice_stride + n0 * 32
+                                                         : s * g.b.slice_stride + n0 * g.b.ld + k0);
         int row = tid >> 2, col = (tid & 3) * 8;   // 32 rows (n) x 4 chunks
-        cp_async16(dB + (s * OBN + row) * OLDA + col, gb + row * g.b.ld + col);
+        cp_async16(dB + (s * OBN + row) * OLDA + col, gb + row * ldb + col);
       } else {
         const __nv_bfloat16* gb = g.b.s + s * g.b.slice_stride + k0 * g.b.ld + n0;
         int row = tid >> 2, col = (tid & 3) * 8;   // 32 rows (k) x 4 chunks
@@ -221,6 +226,7 @@ int launch_lv(Ctx* c, const OzArgs& g)
   dim3 grid((unsigned)cdiv(g.M, OBM), (unsigned)cdiv(g.N, OBN), (unsigned)std::max(1, g.ksplit));
   if (grid.y > 65535) return set_error(c, THC_ERR_SHAPE, "ozgemm: N too large");
   ProfScope prof(c, "ozgemm");
+  ProfScope prof_tag(g.tag ? c : nullptr, g.tag ? g.tag : "");
   if (g.b.k_contig) {
     THC_CUDA(c, cudaFuncSetAttribute(ozgemm_kernel<LV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ozgemm_kernel<LV, true><<<grid, 128, smem, c->stream>>>(g);
@@ -274,10 +280,19 @@ __device__ __forceinline__ long long fixed_point(double x, int shift_total)
   return (bits >> 63) ? -(long long)X : (long long)X;
 }
 
+// Offset of element (slice s2, row r, column cc) in a plain (kts == 0) or tiled slice
+// buffer (OzOperand).
+__device__ __forceinline__ long long slice_at(int s2, long long r, long long cc, long long ldo,
+                                              long long sstride, long long kts)
+{
+  return kts ? (cc >> 5) * kts + s2 * sstride + r * 32 + (cc & 31)
+             : s2 * sstride + r * ldo + cc;
+}
+
 __global__ void slice_rows_kernel(const double* __restrict__ X, long long rows, long long cols,
                                   long long ldx, long long sc, const double* __restrict__ scale,
                                   int shift, int ns, __nv_bfloat16* out, long long ldo,
-                                  long long sstride, int* exps, long long rows_pad)
+                                  long long sstride, long long kts, int* exps, long long rows_pad)
 {
   long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
@@ -312,7 +327,7 @@ __global__ void slice_rows_kernel(const double* __restrict__ X, long long rows, 
       R -= S << sh;
       // |S| <= 128: convert through int32 (a 64-bit integer conversion runs on the slow
       // FP64-class path on this part).
-      out[s2 * sstride + r * ldo + cc] = __float2bfloat16_rn((float)(int)S);
+      out[slice_at(s2, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn((float)(int)S);
     }
   }
 }
@@ -346,7 +361,8 @@ __device__ __forceinline__ long long fixed_point_f32(float x, int shift_total)
 // integer is the sum of the two parts' roundings (within one unit of the exact value).
 __global__ void slice_rows_dw_kernel(const float2* __restrict__ X, long long rows, long long cols,
                                      long long ldx, int ns, __nv_bfloat16* out, long long ldo,
-                                     long long sstride, int* exps, long long rows_pad)
+                                     long long sstride, long long kts, int* exps,
+                                     long long rows_pad)
 {
   long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
@@ -373,7 +389,7 @@ __global__ void slice_rows_dw_kernel(const float2* __restrict__ X, long long row
       int sh = 7 * (ns - 1 - s2);
       long long S = sh ? ((R + (1LL << (sh - 1))) >> sh) : R;
       R -= S << sh;
-      out[s2 * sstride + r * ldo + cc] = __float2bfloat16_rn((float)(int)S);
+      out[slice_at(s2, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn((float)(int)S);
     }
   }
 }
@@ -403,7 +419,8 @@ __global__ void slice_rows_f32_kernel(const float* __restrict__ X, long long row
                                       long long cols, long long ldx,
                                       const float* __restrict__ scale, int shift, int ns,
                                       __nv_bfloat16* out, long long ldo, long long sstride,
-                                      const unsigned* __restrict__ rowmax, int* exps)
+                                      long long kts, const unsigned* __restrict__ rowmax,
+                                      int* exps)
 {
   long long r = blockIdx.y;
   long long cc = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -420,7 +437,7 @@ __global__ void slice_rows_f32_kernel(const float* __restrict__ X, long long row
   }
   for (int s = 0; s < ns; s++) {
     float q = rintf(x);
-    out[s * sstride + r * ldo + cc] = __float2bfloat16_rn(q);
+    out[slice_at(s, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn(q);
     x = (x - q) * 128.f;
   }
 }
@@ -438,38 +455,41 @@ int oz_choose_split(long long M, long long N, long long K, bool lower)
 
 int oz_split_reduce(Ctx* c, const OzArgs& g)
 {
+  ProfScope prof(c, "oz_split_reduce");
   oz_reduce_kernel<<<(unsigned)cdiv(g.M * g.N, 256), 256, 0, c->stream>>>(g);
   THC_LAUNCHED(c, "oz_split_reduce");
   return THC_OK;
 }
 
 int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
-                      long long sc, const double* scale, int scale_shift, int nslices,
-                      __nv_bfloat16* out, long long ldo, long long slice_stride, int* exps,
-                      long long rows_pad)
+                      long long sc, const double* scale, int scale_shift, const SliceBuf& out)
 {
-  long long threads = rows_pad * 32;
+  ProfScope prof(c, "slice");
+  long long threads = out.rows_pad * 32;
   slice_rows_kernel<<<(unsigned)cdiv(threads, 256), 256, 0, c->stream>>>(
-      X, rows, cols, ldx, sc, scale, scale_shift, nslices, out, ldo, slice_stride, exps, rows_pad);
+      X, rows, cols, ldx, sc, scale, scale_shift, out.ns, out.s, out.kpad, out.slice_stride(),
+      out.kt_stride(), out.e, out.rows_pad);
   THC_LAUNCHED(c, "slice_rows_f64");
   return THC_OK;
 }
 
 int oz_slice_rows_dw(Ctx* c, const float2* X, long long rows, long long cols, long long ldx,
-                     int nslices, __nv_bfloat16* out, long long ldo, long long slice_stride,
-                     int* exps, long long rows_pad)
+                     const SliceBuf& out)
 {
-  long long threads = rows_pad * 32;
+  ProfScope prof(c, "slice");
+  long long threads = out.rows_pad * 32;
   slice_rows_dw_kernel<<<(unsigned)cdiv(threads, 256), 256, 0, c->stream>>>(
-      X, rows, cols, ldx, nslices, out, ldo, slice_stride, exps, rows_pad);
+      X, rows, cols, ldx, out.ns, out.s, out.kpad, out.slice_stride(), out.kt_stride(), out.e,
+      out.rows_pad);
   THC_LAUNCHED(c, "slice_rows_dw");
   return THC_OK;
 }
 
 int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, long long ldx,
-                      const float* scale, int scale_shift, int nslices, __nv_bfloat16* out,
-                      long long ldo, long long slice_stride, int* exps, long long rows_pad)
+                      const float* scale, int scale_shift, const SliceBuf& out)
 {
+  ProfScope prof(c, "slice");
+  const long long rows_pad = out.rows_pad;
   unsigned* rowmax = (unsigned*)ws_get(c, WS_ROWMAX, sizeof(unsigned) * rows_pad);
   if (!rowmax) return set_error(c, THC_ERR_NOMEM, "slice_rows_f32: row maxima");
   THC_CUDA(c, cudaMemsetAsync(rowmax, 0, sizeof(unsigned) * rows_pad, c->stream));
@@ -477,9 +497,10 @@ int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, lo
   dim3 g1((unsigned)cdiv(cols, 4096), (unsigned)rows_pad);
   rowmax_f32_kernel<<<g1, 256, 0, c->stream>>>(X, rows, cols, ldx, scale, scale_shift, rowmax);
   THC_LAUNCHED(c, "rowmax_f32");
-  dim3 g2((unsigned)cdiv(ldo, 256), (unsigned)rows_pad);
+  dim3 g2((unsigned)cdiv(out.kpad, 256), (unsigned)rows_pad);
   slice_rows_f32_kernel<<<g2, 256, 0, c->stream>>>(X, rows, cols, ldx, scale, scale_shift,
-                                                   nslices, out, ldo, slice_stride, rowmax, exps);
+                                                   out.ns, out.s, out.kpad, out.slice_stride(),
+                                                   out.kt_stride(), rowmax, out.e);
   THC_LAUNCHED(c, "slice_rows_f32");
   return THC_OK;
 }
@@ -487,6 +508,8 @@ int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, lo
 int ozgemm(Ctx* c, const OzArgs& g)
 {
   if (g.M <= 0 || g.N <= 0) return THC_OK;
+  if (!g.b.k_contig && g.b.kt_stride)
+    return set_error(c, THC_ERR_ARG, "ozgemm: tiled B must be K-contiguous");
   switch (g.levels) {
     case 2: return launch_lv<2>(c, g);
     case 3: return launch_lv<3>(c, g);

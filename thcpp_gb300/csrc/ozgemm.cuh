@@ -25,11 +25,17 @@ enum OzEpilogue : int {
   OZ_STORE_F64 = 0, OZ_SQUARE_F64 = 1, OZ_STORE_F32 = 2, OZ_SQUARE_DW = 3, OZ_STORE_DW = 4
 };
 
+// Slice storage.  Plain: element (slice s, row r, k) at s*slice_stride + r*ld + k.
+// Tiled (kt_stride > 0): at (k/32)*kt_stride + s*slice_stride + r*32 + k%32, i.e.
+// [k/32][slice][row][32]: the 32-wide k tile of a block of rows is one contiguous run of
+// memory, so a tile load reads whole DRAM pages instead of 64-byte pieces of rows that lie
+// kilobytes (for the Coulomb product's 1.28e6-long rows, megabytes) apart.
 struct OzOperand {
   const __nv_bfloat16* s = nullptr;  // slices
   const int* e = nullptr;            // exponent per row (A) / per column (B)
-  long long ld = 0;                  // elements between consecutive rows of one slice
-  long long slice_stride = 0;        // elements between slices
+  long long ld = 0;                  // plain: elements between rows; both: padded K
+  long long slice_stride = 0;        // elements between slices (tiled: within one k tile)
+  long long kt_stride = 0;           // tiled: elements between k tiles; 0 = plain
   bool k_contig = true;              // B only: true for [n][k] storage, false for [k][n]
 };
 
@@ -44,6 +50,7 @@ struct OzArgs {
   int lower_only = 0;
   int ksplit = 1;                    // > 1: K split over blockIdx.z (multiples of 512)
   double* part = nullptr;            // ksplit x M x N FP64 partials (scaled, pre-epilogue)
+  const char* tag = nullptr;         // profile name of this product (besides "ozgemm")
 };
 
 // Number of k-splits that fills the GPU for an M x N output with long K (chunk = 512).
@@ -55,20 +62,36 @@ int oz_split_reduce(Ctx* c, const OzArgs& g);
 inline long long oz_pad_mn(long long x) { return (x + 127) / 128 * 128; }
 inline long long oz_pad_k(long long x) { return (x + 31) / 32 * 32; }
 
+// Destination of a slicing call: ns slices of a rows_pad x kpad matrix (kpad a multiple
+// of 32) and one exponent per row, plain or tiled (see OzOperand); ns * rows_pad * kpad
+// elements either way.
+struct SliceBuf {
+  __nv_bfloat16* s = nullptr;
+  int* e = nullptr;
+  long long rows_pad = 0, kpad = 0;
+  int ns = 0;
+  bool tiled = false;
+  long long slice_stride() const { return tiled ? rows_pad * 32 : rows_pad * kpad; }
+  long long kt_stride() const { return tiled ? (long long)ns * rows_pad * 32 : 0; }
+  OzOperand operand() const
+  {
+    OzOperand o;
+    o.s = s; o.e = e; o.ld = kpad; o.slice_stride = slice_stride(); o.kt_stride = kt_stride();
+    o.k_contig = true;
+    return o;
+  }
+};
+
 // Slice rows of a matrix X (rows x cols, element (r, c) at X[r*ldx + c*sc]) into
 // out[slice][r][c] (row length ldo, padded entries zero) with one exponent per row.
 // `scale` (optional, length cols, indexed c >> scale_shift) multiplies entries first.
 int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
-                      long long sc, const double* scale, int scale_shift, int nslices,
-                      __nv_bfloat16* out, long long ldo, long long slice_stride, int* exps,
-                      long long rows_pad);
+                      long long sc, const double* scale, int scale_shift, const SliceBuf& out);
 // Slices of a double-word matrix (float2 {hi, lo} entries, row-major, ld = ldx).
 int oz_slice_rows_dw(Ctx* c, const float2* X, long long rows, long long cols, long long ldx,
-                     int nslices, __nv_bfloat16* out, long long ldo, long long slice_stride,
-                     int* exps, long long rows_pad);
+                     const SliceBuf& out);
 int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, long long ldx,
-                      const float* scale, int scale_shift, int nslices, __nv_bfloat16* out,
-                      long long ldo, long long slice_stride, int* exps, long long rows_pad);
+                      const float* scale, int scale_shift, const SliceBuf& out);
 // Warp-level mma.sync implementation (reference for the tensor-core kernel below).
 int ozgemm(Ctx* c, const OzArgs& g);
 // tcgen05 / TMEM / TMA implementation; both operands K-contiguous.  err_flag (device int)

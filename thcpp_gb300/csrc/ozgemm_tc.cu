@@ -34,6 +34,7 @@ namespace {
 
 constexpr int TBM = 128, TBN = 64, TBK = 32, TSTAGES = 3, TCHUNK = 16;  // 16 stages = 512 k
 constexpr int TEPI_WARPS = 8;
+constexpr int kGroupM = 8;    // m-tiles per group of the tile order
 constexpr int TTHREADS = 32 * (2 + TEPI_WARPS);
 constexpr long long kSpinLimit = 1LL << 24;
 
@@ -174,6 +175,7 @@ __device__ __forceinline__ double pow2d(int e)
 struct TcArgs {
   long long M, N, K;
   long long a_rows_pad, b_rows_pad;   // rows of one slice in the 2-D tensor maps
+  long long a_tile_rows, b_tile_rows; // tiled operands: map rows per 32-wide k tile; 0 = plain
   const int* ea;
   const int* eb;
   void* C;
@@ -190,8 +192,22 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     ozgemm_tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
                      TcArgs g)
 {
-  const long long m0 = (long long)blockIdx.x * TBM;
-  const long long n0 = (long long)blockIdx.y * TBN;
+  // Grouped tile order: consecutive blocks sweep kGroupM m-tiles for each n-tile, so the
+  // CTAs resident at one time share ~8 A row blocks and ~19 B row blocks through L2
+  // (row-major order would have them read every A block, or one B block each).
+  long long mt, nt;
+  {
+    const long long mtn = gridDim.x, ntn = gridDim.y;
+    const long long b = (long long)blockIdx.y * mtn + blockIdx.x;
+    const long long per_group = (long long)kGroupM * ntn;
+    const long long grp = b / per_group, first_m = grp * kGroupM;
+    const long long gm = mtn - first_m < kGroupM ? mtn - first_m : kGroupM;
+    const long long r = b - grp * per_group;
+    mt = first_m + r % gm;
+    nt = r / gm;
+  }
+  const long long m0 = mt * TBM;
+  const long long n0 = nt * TBN;
   if (g.lower_only && n0 > m0 + TBM - 1) return;
 
   constexpr int A_BYTES = TBM * TBK * 2;          // 8 KB per slice tile
@@ -245,12 +261,17 @@ __global__ void __launch_bounds__(TTHREADS, 1)
         if (!mbar_wait(&empty[s], ph ^ 1, abort)) break;
         unsigned char* st = smem + s * STAGE_BYTES;
         mbar_expect_tx(&full[s], STAGE_BYTES);
-        int kx = (int)(kbeg + (long long)it * TBK);
+        const long long k = kbeg + (long long)it * TBK;
+        // Plain maps: x = k, y = slice row.  Tiled maps (64-byte rows): x = 0 and y walks
+        // the k tiles first.
+        const int ax = g.a_tile_rows ? 0 : (int)k, bx = g.b_tile_rows ? 0 : (int)k;
+        const long long ay0 = g.a_tile_rows ? (k >> 5) * g.a_tile_rows : 0;
+        const long long by0 = g.b_tile_rows ? (k >> 5) * g.b_tile_rows : 0;
 #pragma unroll
         for (int sl = 0; sl < LV; sl++) {
-          tma_load_2d(st + sl * A_BYTES, &ta, kx, (int)(sl * g.a_rows_pad + m0), &full[s]);
-          tma_load_2d(st + LV * A_BYTES + sl * B_BYTES, &tb, kx, (int)(sl * g.b_rows_pad + n0),
-                      &full[s]);
+          tma_load_2d(st + sl * A_BYTES, &ta, ax, (int)(ay0 + sl * g.a_rows_pad + m0), &full[s]);
+          tma_load_2d(st + LV * A_BYTES + sl * B_BYTES, &tb, bx,
+                      (int)(by0 + sl * g.b_rows_pad + n0), &full[s]);
         }
       }
     }
@@ -431,13 +452,16 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encoder()
 }
 
 // 2-D bf16 tensor map over `rows` x `kpad` (row pitch kpad elements), box 32 x box_rows.
-int make_map(Ctx* c, CUtensorMap* map, const void* base, long long kpad, long long rows,
+// 2-D map of a slice buffer: rows of `width` bf16 (kpad for plain storage, 32 for tiled).
+int make_map(Ctx* c, CUtensorMap* map, const void* base, long long width, long long rows,
              int box_rows)
 {
   auto enc = get_encoder();
   if (!enc) return set_error(c, THC_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-  cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)kpad * 2};
+  // Row coordinates are 32-bit in the copy instruction.
+  if (rows > 0x7fffffffLL) return set_error(c, THC_ERR_SHAPE, "ozgemm_tc: slice buffer too tall");
+  cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)width * 2};
   cuuint32_t box[2] = {(cuuint32_t)TBK, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
@@ -451,14 +475,24 @@ template <int LV>
 int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
 {
   CUtensorMap ta, tb;
-  long long a_rows = g.a.slice_stride / g.a.ld, b_rows = g.b.slice_stride / g.b.ld;
-  int st = make_map(c, &ta, g.a.s, g.a.ld, a_rows * LV, TBM);
+  const bool at = g.a.kt_stride > 0, bt = g.b.kt_stride > 0;
+  long long a_rows = at ? g.a.slice_stride / 32 : g.a.slice_stride / g.a.ld;
+  long long b_rows = bt ? g.b.slice_stride / 32 : g.b.slice_stride / g.b.ld;
+  // Tiled: one map row per 64 bytes; k tiles of LV slices x rows each, g.*.ld / 32 of them.
+  if ((at && g.a.kt_stride != LV * g.a.slice_stride) ||
+      (bt && g.b.kt_stride != LV * g.b.slice_stride))
+    return set_error(c, THC_ERR_ARG, "ozgemm_tc: tiled operand with another slice count");
+  int st = at ? make_map(c, &ta, g.a.s, 32, (g.a.ld / 32) * (g.a.kt_stride / 32), TBM)
+              : make_map(c, &ta, g.a.s, g.a.ld, a_rows * LV, TBM);
   if (st) return st;
-  st = make_map(c, &tb, g.b.s, g.b.ld, b_rows * LV, TBN);
+  st = bt ? make_map(c, &tb, g.b.s, 32, (g.b.ld / 32) * (g.b.kt_stride / 32), TBN)
+          : make_map(c, &tb, g.b.s, g.b.ld, b_rows * LV, TBN);
   if (st) return st;
   TcArgs t;
   t.M = g.M; t.N = g.N; t.K = g.K;
   t.a_rows_pad = a_rows; t.b_rows_pad = b_rows;
+  t.a_tile_rows = at ? g.a.kt_stride / 32 : 0;
+  t.b_tile_rows = bt ? g.b.kt_stride / 32 : 0;
   t.ea = g.a.e; t.eb = g.b.e; t.C = g.C; t.ldc = g.ldc;
   t.epilogue = g.epilogue; t.lower_only = g.lower_only; t.error = err_flag;
   t.ksplit = std::max(1, g.ksplit); t.part = g.part;
@@ -469,6 +503,7 @@ int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
   if (grid.y > 65535) return set_error(c, THC_ERR_SHAPE, "ozgemm_tc: N too large");
   {
     ProfScope prof(c, "ozgemm");
+    ProfScope prof_tag(g.tag ? c : nullptr, g.tag ? g.tag : "");
     ozgemm_tc_kernel<LV><<<grid, TTHREADS, smem, c->stream>>>(ta, tb, t);
     THC_LAUNCHED(c, "ozgemm_tc");
   }
@@ -482,8 +517,9 @@ int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
 {
   if (g.M <= 0 || g.N <= 0) return THC_OK;
   if (!g.b.k_contig) return set_error(c, THC_ERR_ARG, "ozgemm_tc: B must be K-contiguous");
-  if (g.a.ld % 32 || g.b.ld % 32 || (g.a.slice_stride / g.a.ld) % TBM ||
-      (g.b.slice_stride / g.b.ld) % TBN)
+  const long long ar = g.a.kt_stride ? g.a.slice_stride / 32 : g.a.slice_stride / g.a.ld;
+  const long long br = g.b.kt_stride ? g.b.slice_stride / 32 : g.b.slice_stride / g.b.ld;
+  if (g.a.ld % 32 || g.b.ld % 32 || ar % TBM || br % TBN)
     return set_error(c, THC_ERR_ARG, "ozgemm_tc: operand padding");
   switch (g.levels) {
     case 2: return launch_tc<2>(c, g, err_flag);
