@@ -85,7 +85,8 @@ int thc_ctx_set_stream(thc_ctx* ctx, void* cuda_stream);
  * P, zeta and Coulomb products, 2..6); "gemm_tc" (1 = tcgen05 tensor-core kernel, the
  * default; 0 = warp-level mma.sync kernel); "km_prune" (1 = spatially pruned k-means
  * assignment, the default; 0 = exhaustive scan -- both exact); "graphs" (1 = replay the
- * k-means iteration block as a CUDA graph, the default); "fft64" (mixed path: 1 = zeta
+ * k-means iteration block as a CUDA graph, the default); "tc_bk" (k-step per
+ * pipeline stage of the tensor-core kernel: 32, the default, or 16); "fft64" (mixed path: 1 = zeta
  * in FP64 through a D2Z FFT, 0 = FP32 and R2C, the default);
  * "profile" (1 = record a CUDA event pair around every launch of the named kernels,
  * 0 = stop and clear). */

@@ -134,13 +134,15 @@ def test_sliced_gemm_tc_matches_mma_sync(lib):
     s = system("c2")
     idx = kmeans_idx("c2")
     out = {}
-    for tc in (0, 1):
+    for key in ((0, 16), (1, 16), (1, 32)):
         with capi.Context(0, capi.THC_PREC_MIXED) as ctx:
-            ctx.set_option("gemm_tc", tc)
-            out[tc] = _cplx(ctx.isdf(s.phi, idx, s.mesh, s.coulG)["M"])
-    d = _rel(out[1], out[0])
-    print(f"tc vs mma.sync ||dM||/||M|| = {d:.3e}")
-    assert d < 1e-7
+            ctx.set_option("gemm_tc", key[0])
+            ctx.set_option("tc_bk", key[1])
+            out[key] = _cplx(ctx.isdf(s.phi, idx, s.mesh, s.coulG)["M"])
+    for key in ((1, 16), (1, 32)):
+        d = _rel(out[key], out[(0, 16)])
+        print(f"tc (k-step {key[1]}) vs mma.sync ||dM||/||M|| = {d:.3e}")
+        assert d < 1e-7
 
 
 def test_isdf_mesh_mismatch(gpu_ctx_fp64):

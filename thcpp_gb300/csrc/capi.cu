@@ -257,6 +257,11 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
     h->c.profile = value != 0.0;
     return THC_OK;
   }
+  if (!strcmp(key, "tc_bk")) {
+    if (value != 16.0 && value != 32.0) return THC_ERR_ARG;
+    h->c.tc_bk = (int)value;
+    return THC_OK;
+  }
   if (!strcmp(key, "fft64")) {
     h->c.fft64 = value != 0.0;
     return THC_OK;

@@ -188,11 +188,11 @@ __global__ void __launch_bounds__(128, 2) ozgemm_kernel(OzArgs g)
     if (((st + 1) * OBK) % OCHUNK == 0 || st + 1 == nsteps) {
 #pragma unroll
       for (int l = 0; l < LV; l++) {
-        const double sc = pow2(-7 * l);
+        // Slices are stored pre-scaled, so every level is already in the final units.
 #pragma unroll
         for (int t = 0; t < 4; t++)
 #pragma unroll
-          for (int q = 0; q < 4; q++) acc64[t][q] = __fma_rn((double)acc[l][t][q], sc, acc64[t][q]);
+          for (int q = 0; q < 4; q++) acc64[t][q] = __dadd_rn((double)acc[l][t][q], acc64[t][q]);
       }
     }
     buf ^= 1;
@@ -280,6 +280,11 @@ __device__ __forceinline__ long long fixed_point(double x, int shift_total)
   return (bits >> 63) ? -(long long)X : (long long)X;
 }
 
+// Slices are stored pre-scaled: digit S_s as S_s 2^{-7s} (exact in BF16), so that a product
+// of slices i and j carries its level's weight 2^{-7(i+j)} and the GEMM kernels need no
+// per-level scaling.
+__device__ __forceinline__ float slice_scale(int s) { return __int_as_float((127 - 7 * s) << 23); }
+
 // Offset of element (slice s2, row r, column cc) in a plain (kts == 0) or tiled slice
 // buffer (OzOperand).
 __device__ __forceinline__ long long slice_at(int s2, long long r, long long cc, long long ldo,
@@ -327,7 +332,7 @@ __global__ void slice_rows_kernel(const double* __restrict__ X, long long rows, 
       R -= S << sh;
       // |S| <= 128: convert through int32 (a 64-bit integer conversion runs on the slow
       // FP64-class path on this part).
-      out[slice_at(s2, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn((float)(int)S);
+      out[slice_at(s2, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn((float)(int)S * slice_scale(s2));
     }
   }
 }
@@ -389,7 +394,7 @@ __global__ void slice_rows_dw_kernel(const float2* __restrict__ X, long long row
       int sh = 7 * (ns - 1 - s2);
       long long S = sh ? ((R + (1LL << (sh - 1))) >> sh) : R;
       R -= S << sh;
-      out[slice_at(s2, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn((float)(int)S);
+      out[slice_at(s2, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn((float)(int)S * slice_scale(s2));
     }
   }
 }
@@ -437,7 +442,7 @@ __global__ void slice_rows_f32_kernel(const float* __restrict__ X, long long row
   }
   for (int s = 0; s < ns; s++) {
     float q = rintf(x);
-    out[slice_at(s, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn(q);
+    out[slice_at(s, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn(q * slice_scale(s));
     x = (x - q) * 128.f;
   }
 }
@@ -446,11 +451,23 @@ __global__ void slice_rows_f32_kernel(const float* __restrict__ X, long long row
 
 int oz_choose_split(long long M, long long N, long long K, bool lower)
 {
-  long long tiles = cdiv(M, 128) * cdiv(N, 64);
-  if (lower) tiles = (tiles + cdiv(M, 128)) / 2;
-  long long chunks = cdiv(K, 512);
-  long long want = cdiv(2 * 152, std::max(1LL, tiles));
-  return (int)std::max(1LL, std::min(want, chunks));
+  // Tiles of the tensor-core kernel (128 x 128); with `lower`, those on or below the
+  // diagonal.  Modelled time of a split k: waves x (k range per CTA, in whole 512-k chunks,
+  // + ~256 k worth of prologue and epilogue); the FP64 partials (k M N doubles) stay below
+  // 4 GB.
+  const long long mt = cdiv(M, 128), nt = cdiv(N, 128);
+  const long long tiles = lower ? mt * (mt + 1) / 2 : mt * nt;
+  const long long chunks = (long long)cdiv(K, 512);
+  const long long kmem = std::max(1LL, (4LL << 30) / std::max(1LL, 8 * M * N));
+  const long long maxk = std::max(1LL, std::min(std::min(chunks, kmem), 1024LL));
+  long long best_k = 1;
+  double best_t = 0.0;
+  for (long long k = 1; k <= maxk; k++) {
+    const long long per = (long long)cdiv(chunks, k) * 512;
+    const double t = (double)cdiv(tiles * k, 152) * (double)(per + 256);
+    if (k == 1 || t < best_t) { best_t = t; best_k = k; }
+  }
+  return (int)best_k;
 }
 
 int oz_split_reduce(Ctx* c, const OzArgs& g)

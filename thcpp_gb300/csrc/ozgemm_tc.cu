@@ -1,20 +1,21 @@
 // Sliced-BF16 GEMM on the 5th-generation tensor cores (tcgen05 + TMEM + TMA).
 //
 // Same arithmetic as ozgemm.cu (see ozgemm.cuh): C = sum over slice pairs (i, j), i + j < LV,
-// of 2^{-7(i+j)} S_i T_j, with exact FP32 chunk sums folded into FP64.
+// of S_i T_j (slices stored pre-scaled by 2^{-7i}), with exact FP32 chunk sums folded into a
+// double-word FP32 total.
 //
-// CTA tile 128 x 64, k-step 32 per pipeline stage, all LV slices of A and B per stage.
+// CTA tile 128 x 128, k-step BK (16 or 32) per pipeline stage, all LV slices of A and B per
+// stage, as many stages as fit in ~200 KB of shared memory.
 // Warp roles (320 threads):
-//   warp 0      TMA producer: 2*LV tiled loads per stage (SWIZZLE_64B, K-major)
+//   warp 0      TMA producer: 2*LV tiled loads per stage (K-major, 32- or 64-byte swizzle)
 //   warp 1      TMEM allocator + single-thread MMA issuer
-//   warps 2-9   epilogue: two warps per TMEM lane quadrant, 32 columns each
-// TMEM holds one 128 x 64 FP32 accumulator per level (LV x 64 columns).  Levels 0-2 carry
-// the bulk of the value and are drained every 512 k (16 stages) while each of their sums
-// is still an exact integer below 2^24; levels >= 3 weigh <= 2^-21 of the total and
-// accumulate in FP32 over the whole K (rounding <= 2^-45 of the total).  The drain copies
-// levels 0-2 to registers and releases TMEM at once, so the FP64 folding overlaps the next
-// chunk's MMAs; within a stage the MMA thread issues the level >= 3 pairs first, which
-// covers the drain.
+//   warps 2-9   epilogue: two warps per TMEM lane quadrant, 64 columns each
+// TMEM (512 columns) holds four 128 x 128 FP32 accumulators: one each for the pair levels
+// 0, 1 and 2, which carry the bulk of the value and are drained every 512 k while each of
+// their sums is still exact (an integer multiple of 2^{-7l} below 2^{24-7l}), and one for
+// all levels >= 3 together, which weigh <= 2^-21 of the total and accumulate in FP32 over
+// the whole K (rounding <= 2^-45 of the total).  Within a stage the MMA thread issues the
+// level >= 3 pairs first, which covers most of the drain.
 // Every mbarrier wait is bounded; on timeout the kernel records an error, stops issuing,
 // and every role falls through to the teardown, which frees TMEM.
 #include <cuda.h>
@@ -32,7 +33,10 @@ namespace thc {
 
 namespace {
 
-constexpr int TBM = 128, TBN = 64, TBK = 32, TSTAGES = 3, TCHUNK = 16;  // 16 stages = 512 k
+constexpr int TBM = 128, TBN = 128;
+constexpr int kChunkK = 512;            // exact levels are drained every 512 k
+constexpr int kStageBudget = 200 * 1024;  // shared memory for the stage buffers
+constexpr int kSmemGuard = 16 * 1024;   // slack after the buffers (descriptor reads stay inside)
 constexpr int TEPI_WARPS = 8;
 constexpr int kGroupM = 8;    // m-tiles per group of the tile order
 constexpr int TTHREADS = 32 * (2 + TEPI_WARPS);
@@ -92,19 +96,22 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// UMMA shared-memory descriptor: K-major, SWIZZLE_64B, 8-row groups 512 B apart.
+// UMMA shared-memory descriptor, K-major with the rows of one tile BK bf16 (2 BK bytes)
+// long: BK = 32 uses the 64-byte swizzle (8-row groups 512 B apart), BK = 16 the 32-byte
+// swizzle (groups 256 B apart).
+template <int BK>
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
 {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-  d |= (uint64_t)1 << 16;                // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(512 >> 4) << 32;       // stride byte offset
-  d |= (uint64_t)1 << 46;                // descriptor version
-  d |= (uint64_t)4 << 61;                // layout: 64-byte swizzle
+  d |= (uint64_t)1 << 16;                       // leading byte offset (unused when swizzled)
+  d |= (uint64_t)((8 * 2 * BK) >> 4) << 32;     // stride byte offset: one 8-row group
+  d |= (uint64_t)1 << 46;                       // descriptor version
+  d |= (uint64_t)(BK == 32 ? 4 : 6) << 61;      // layout: 64- or 32-byte swizzle
   return d;
 }
 
-// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 64.
+// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 128.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TBN >> 3) << 17) |
                             ((uint32_t)(TBM >> 4) << 24);
 
@@ -138,6 +145,21 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+{
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
 // Error-free transformations in FP32 (Knuth's TwoSum; Dekker's FastTwoSum for |a| >= |b|).
@@ -187,14 +209,29 @@ struct TcArgs {
   double* part;
 };
 
-template <int LV>
+// Stage geometry of one (LV, BK) instantiation.
+template <int LV, int BK>
+struct TcCfg {
+  static constexpr int A_BYTES = TBM * BK * 2;            // one slice tile of A
+  static constexpr int B_BYTES = TBN * BK * 2;            // one slice tile of B
+  static constexpr int STAGE_BYTES = LV * (A_BYTES + B_BYTES);
+  static constexpr int STAGES = kStageBudget / STAGE_BYTES < 4 ? kStageBudget / STAGE_BYTES : 4;
+  static constexpr int CHUNK_STAGES = kChunkK / BK;
+  static constexpr int NEXACT = LV < 3 ? LV : 3;          // exact level accumulators
+  static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256 + kSmemGuard;
+  static_assert(STAGES >= 2, "stage buffers");
+};
+
+template <int LV, int BK>
 __global__ void __launch_bounds__(TTHREADS, 1)
     ozgemm_tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
                      TcArgs g)
 {
+  using Cfg = TcCfg<LV, BK>;
+  constexpr int A_BYTES = Cfg::A_BYTES, B_BYTES = Cfg::B_BYTES, STAGE_BYTES = Cfg::STAGE_BYTES;
+  constexpr int NST = Cfg::STAGES;
   // Grouped tile order: consecutive blocks sweep kGroupM m-tiles for each n-tile, so the
-  // CTAs resident at one time share ~8 A row blocks and ~19 B row blocks through L2
-  // (row-major order would have them read every A block, or one B block each).
+  // CTAs resident at one time share a few A and B row blocks through L2.
   long long mt, nt;
   {
     const long long mtn = gridDim.x, ntn = gridDim.y;
@@ -210,14 +247,11 @@ __global__ void __launch_bounds__(TTHREADS, 1)
   const long long n0 = nt * TBN;
   if (g.lower_only && n0 > m0 + TBM - 1) return;
 
-  constexpr int A_BYTES = TBM * TBK * 2;          // 8 KB per slice tile
-  constexpr int B_BYTES = TBN * TBK * 2;          // 4 KB per slice tile
-  constexpr int STAGE_BYTES = LV * (A_BYTES + B_BYTES);
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + TSTAGES * STAGE_BYTES);
-  uint64_t* empty = full + TSTAGES;
-  uint64_t* acc_full = empty + TSTAGES;
+  uint64_t* full = (uint64_t*)(smem + NST * STAGE_BYTES);
+  uint64_t* empty = full + NST;
+  uint64_t* acc_full = empty + NST;
   uint64_t* acc_empty = acc_full + 1;
   uint32_t* tmem_slot = (uint32_t*)(acc_empty + 1);
   volatile int* abort = (volatile int*)(tmem_slot + 1);
@@ -225,15 +259,15 @@ __global__ void __launch_bounds__(TTHREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   long long kbeg = 0, kend = g.K;
   if (g.ksplit > 1) {
-    long long kc = ((g.K + g.ksplit - 1) / g.ksplit + 511) / 512 * 512;
+    long long kc = ((g.K + g.ksplit - 1) / g.ksplit + kChunkK - 1) / kChunkK * kChunkK;
     kbeg = blockIdx.z * kc;
     kend = kbeg + kc < g.K ? kbeg + kc : g.K;
   }
-  const int nstages = kend > kbeg ? (int)((kend - kbeg + TBK - 1) / TBK) : 0;
-  const int nchunks = (nstages + TCHUNK - 1) / TCHUNK;
+  const int nstages = kend > kbeg ? (int)((kend - kbeg + BK - 1) / BK) : 0;
+  const int nchunks = (nstages + Cfg::CHUNK_STAGES - 1) / Cfg::CHUNK_STAGES;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < TSTAGES; s++) {
+    for (int s = 0; s < NST; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -256,15 +290,16 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     // ------------------------------------------------------------------ TMA producer
     if (lane == 0) {
       for (int it = 0; it < nstages; it++) {
-        int s = it % TSTAGES;
-        uint32_t ph = (uint32_t)((it / TSTAGES) & 1);
+        int s = it % NST;
+        uint32_t ph = (uint32_t)((it / NST) & 1);
         if (!mbar_wait(&empty[s], ph ^ 1, abort)) break;
         unsigned char* st = smem + s * STAGE_BYTES;
         mbar_expect_tx(&full[s], STAGE_BYTES);
-        const long long k = kbeg + (long long)it * TBK;
-        // Plain maps: x = k, y = slice row.  Tiled maps (64-byte rows): x = 0 and y walks
-        // the k tiles first.
-        const int ax = g.a_tile_rows ? 0 : (int)k, bx = g.b_tile_rows ? 0 : (int)k;
+        const long long k = kbeg + (long long)it * BK;
+        // Plain maps: x = k, y = slice row.  Tiled maps (64-byte rows): x = k % 32 and y
+        // walks the 32-wide k tiles first.
+        const int ax = g.a_tile_rows ? (int)(k & 31) : (int)k;
+        const int bx = g.b_tile_rows ? (int)(k & 31) : (int)k;
         const long long ay0 = g.a_tile_rows ? (k >> 5) * g.a_tile_rows : 0;
         const long long by0 = g.b_tile_rows ? (k >> 5) * g.b_tile_rows : 0;
 #pragma unroll
@@ -280,47 +315,45 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     if (lane == 0) {
       bool started_hi = false;
       for (int it = 0; it < nstages && !*abort; it++) {
-        int s = it % TSTAGES;
-        uint32_t ph = (uint32_t)((it / TSTAGES) & 1);
-        int chunk = it / TCHUNK;
-        bool chunk_first = (it % TCHUNK) == 0;
-        bool chunk_last = ((it + 1) % TCHUNK) == 0 || it + 1 == nstages;
+        int s = it % NST;
+        uint32_t ph = (uint32_t)((it / NST) & 1);
+        int chunk = it / Cfg::CHUNK_STAGES;
+        bool chunk_first = (it % Cfg::CHUNK_STAGES) == 0;
+        bool chunk_last = ((it + 1) % Cfg::CHUNK_STAGES) == 0 || it + 1 == nstages;
         if (!mbar_wait(&full[s], ph, abort)) break;
         asm volatile("tcgen05.fence::after_thread_sync;\n");
         unsigned char* st = smem + s * STAGE_BYTES;
         uint32_t a0 = su32(st), b0 = su32(st + LV * A_BYTES);
-        // Levels >= 3: accumulate over the whole K.
+        // Levels >= 3, all into the fourth accumulator, over the whole K.
 #pragma unroll
         for (int l = 3; l < LV; l++) {
-          bool first = !started_hi;
 #pragma unroll
           for (int i = 0; i <= l; i++) {
             int j = l - i;
 #pragma unroll
-            for (int kk = 0; kk < 2; kk++) {
-              uint64_t ad = sdesc(a0 + i * A_BYTES + kk * 32);
-              uint64_t bd = sdesc(b0 + j * B_BYTES + kk * 32);
-              umma(tmem + l * TBN, ad, bd, first ? 0u : 1u);
-              first = false;
+            for (int kk = 0; kk < BK / 16; kk++) {
+              uint64_t ad = sdesc<BK>(a0 + i * A_BYTES + kk * 32);
+              uint64_t bd = sdesc<BK>(b0 + j * B_BYTES + kk * 32);
+              umma(tmem + 3 * TBN, ad, bd, started_hi ? 1u : 0u);
+              started_hi = true;
             }
           }
         }
-        if (LV > 3) started_hi = true;
         // Levels 0-2: exact per chunk; wait until the previous chunk has been drained.
         if (chunk_first && chunk > 0) {
           if (!mbar_wait(acc_empty, (uint32_t)((chunk - 1) & 1), abort)) break;
           asm volatile("tcgen05.fence::after_thread_sync;\n");
         }
 #pragma unroll
-        for (int l = 0; l < (LV < 3 ? LV : 3); l++) {
+        for (int l = 0; l < Cfg::NEXACT; l++) {
           bool first = chunk_first;
 #pragma unroll
           for (int i = 0; i <= l; i++) {
             int j = l - i;
 #pragma unroll
-            for (int kk = 0; kk < 2; kk++) {
-              uint64_t ad = sdesc(a0 + i * A_BYTES + kk * 32);
-              uint64_t bd = sdesc(b0 + j * B_BYTES + kk * 32);
+            for (int kk = 0; kk < BK / 16; kk++) {
+              uint64_t ad = sdesc<BK>(a0 + i * A_BYTES + kk * 32);
+              uint64_t bd = sdesc<BK>(b0 + j * B_BYTES + kk * 32);
               umma(tmem + l * TBN, ad, bd, first ? 0u : 1u);
               first = false;
             }
@@ -334,47 +367,51 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     // ------------------------------------------------------------------ epilogue
     const int ew = warp - 2;                 // 0..7
     const int quad = warp & 3;               // TMEM lane quadrant this warp may access
-    const int half = ew >> 2;                // which 32-column half of the 64-wide tile
+    const int half = ew >> 2;                // which 64-column half of the tile
     const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
-    const int col0 = half * 32;
-    // Double-word FP32 accumulators: no FP64 arithmetic until the final FP64 stores.
-    float ah[32], al[32];
+    const int col0 = half * 64;
+    // Double-word FP32 totals of this thread's row, 64 columns.
+    float ah[64], al[64];
 #pragma unroll
-    for (int q = 0; q < 32; q++) { ah[q] = 0.f; al[q] = 0.f; }
-    float v[32];
+    for (int q = 0; q < 64; q++) { ah[q] = 0.f; al[q] = 0.f; }
     bool ok = true;
     for (int ch = 0; ch < nchunks; ch++) {
       if (!mbar_wait(acc_full, (uint32_t)(ch & 1), abort)) { ok = false; break; }
       asm volatile("tcgen05.fence::after_thread_sync;\n");
-      float l0[32], l1[32], l2[32];
-      tmem_ld32(tmem + lane_base + 0 * TBN + col0, l0);
-      if (LV > 1) tmem_ld32(tmem + lane_base + 1 * TBN + col0, l1);
-      if (LV > 2) tmem_ld32(tmem + lane_base + 2 * TBN + col0, l2);
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        float l0[16], l1[16], l2[16];
+        const uint32_t cb = (uint32_t)(col0 + 16 * b);
+        tmem_ld16(tmem + lane_base + 0 * TBN + cb, l0);
+        if (LV > 1) tmem_ld16(tmem + lane_base + 1 * TBN + cb, l1);
+        if (LV > 2) tmem_ld16(tmem + lane_base + 2 * TBN + cb, l2);
+        // l0, l1, l2 are exact (multiples of 1, 2^-7, 2^-14 below 2^24, 2^17, 2^10); their
+        // sum needs <= 38 bits and is carried exactly in (s, e).
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          float s1 = l0[q], e1 = 0.f;
+          if (LV > 1) two_sum(l0[q], l1[q], s1, e1);
+          if (LV > 2) {
+            float s2, e2;
+            two_sum(s1, l2[q], s2, e2);
+            s1 = s2;
+            e1 = __fadd_rn(e1, e2);
+          }
+          dw_add(ah[16 * b + q], al[16 * b + q], s1);
+          dw_add(ah[16 * b + q], al[16 * b + q], e1);
+        }
+      }
       asm volatile("tcgen05.fence::before_thread_sync;\n");
       __syncwarp();
       if (lane == 0) mbar_arrive(acc_empty);
-      // l0, 2^-7 l1, 2^-14 l2 are exact floats (integers below 2^24, scaled by powers of
-      // two); their sum needs <= 38 bits and is carried exactly in (s, e).
-#pragma unroll
-      for (int q = 0; q < 32; q++) {
-        float s1 = l0[q], e1 = 0.f;
-        if (LV > 1) two_sum(l0[q], l1[q] * 0x1p-7f, s1, e1);
-        if (LV > 2) {
-          float s2, e2;
-          two_sum(s1, l2[q] * 0x1p-14f, s2, e2);
-          s1 = s2;
-          e1 = __fadd_rn(e1, e2);
-        }
-        dw_add(ah[q], al[q], s1);
-        dw_add(ah[q], al[q], e1);
-      }
     }
     if (ok && LV > 3 && nstages > 0) {
-      for (int l = 3; l < LV; l++) {
-        tmem_ld32(tmem + lane_base + l * TBN + col0, v);
-        float sc = pow2f(-7 * l);
 #pragma unroll
-        for (int q = 0; q < 32; q++) al[q] = __fmaf_rn(v[q], sc, al[q]);
+      for (int b = 0; b < 4; b++) {
+        float v[16];
+        tmem_ld16(tmem + lane_base + 3 * TBN + (uint32_t)(col0 + 16 * b), v);
+#pragma unroll
+        for (int q = 0; q < 16; q++) al[16 * b + q] = __fadd_rn(al[16 * b + q], v[q]);
       }
     }
     if (ok && !*abort) {
@@ -382,7 +419,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       if (m < g.M) {
         int ea = g.ea[m] - 14;
 #pragma unroll
-        for (int q = 0; q < 32; q++) {
+        for (int q = 0; q < 64; q++) {
           long long n = n0 + col0 + q;
           if (n >= g.N || (g.lower_only && n > m)) continue;
           int ex = ea + g.eb[n];
@@ -451,10 +488,10 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encoder()
   return fn;
 }
 
-// 2-D bf16 tensor map over `rows` x `kpad` (row pitch kpad elements), box 32 x box_rows.
-// 2-D map of a slice buffer: rows of `width` bf16 (kpad for plain storage, 32 for tiled).
+// 2-D map of a slice buffer: rows of `width` bf16 (kpad for plain storage, 32 for tiled),
+// box bk x box_rows with the swizzle that matches the UMMA descriptor (sdesc<bk>).
 int make_map(Ctx* c, CUtensorMap* map, const void* base, long long width, long long rows,
-             int box_rows)
+             int box_rows, int bk)
 {
   auto enc = get_encoder();
   if (!enc) return set_error(c, THC_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
@@ -462,18 +499,20 @@ int make_map(Ctx* c, CUtensorMap* map, const void* base, long long width, long l
   if (rows > 0x7fffffffLL) return set_error(c, THC_ERR_SHAPE, "ozgemm_tc: slice buffer too tall");
   cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)width * 2};
-  cuuint32_t box[2] = {(cuuint32_t)TBK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
-                   box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                   box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   bk == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_error(c, THC_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   return THC_OK;
 }
 
-template <int LV>
+template <int LV, int BK>
 int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
 {
+  using Cfg = TcCfg<LV, BK>;
   CUtensorMap ta, tb;
   const bool at = g.a.kt_stride > 0, bt = g.b.kt_stride > 0;
   long long a_rows = at ? g.a.slice_stride / 32 : g.a.slice_stride / g.a.ld;
@@ -482,11 +521,11 @@ int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
   if ((at && g.a.kt_stride != LV * g.a.slice_stride) ||
       (bt && g.b.kt_stride != LV * g.b.slice_stride))
     return set_error(c, THC_ERR_ARG, "ozgemm_tc: tiled operand with another slice count");
-  int st = at ? make_map(c, &ta, g.a.s, 32, (g.a.ld / 32) * (g.a.kt_stride / 32), TBM)
-              : make_map(c, &ta, g.a.s, g.a.ld, a_rows * LV, TBM);
+  int st = at ? make_map(c, &ta, g.a.s, 32, (g.a.ld / 32) * (g.a.kt_stride / 32), TBM, BK)
+              : make_map(c, &ta, g.a.s, g.a.ld, a_rows * LV, TBM, BK);
   if (st) return st;
-  st = bt ? make_map(c, &tb, g.b.s, 32, (g.b.ld / 32) * (g.b.kt_stride / 32), TBN)
-          : make_map(c, &tb, g.b.s, g.b.ld, b_rows * LV, TBN);
+  st = bt ? make_map(c, &tb, g.b.s, 32, (g.b.ld / 32) * (g.b.kt_stride / 32), TBN, BK)
+          : make_map(c, &tb, g.b.s, g.b.ld, b_rows * LV, TBN, BK);
   if (st) return st;
   TcArgs t;
   t.M = g.M; t.N = g.N; t.K = g.K;
@@ -496,19 +535,32 @@ int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
   t.ea = g.a.e; t.eb = g.b.e; t.C = g.C; t.ldc = g.ldc;
   t.epilogue = g.epilogue; t.lower_only = g.lower_only; t.error = err_flag;
   t.ksplit = std::max(1, g.ksplit); t.part = g.part;
-  size_t smem = (size_t)TSTAGES * LV * (TBM + TBN) * TBK * 2 + 1024 + 256;
-  THC_CUDA(c, cudaFuncSetAttribute(ozgemm_tc_kernel<LV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
+  const size_t smem = Cfg::SMEM;
+  THC_CUDA(c, cudaFuncSetAttribute(ozgemm_tc_kernel<LV, BK>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((unsigned)cdiv(g.M, TBM), (unsigned)cdiv(g.N, TBN), (unsigned)t.ksplit);
   if (grid.y > 65535) return set_error(c, THC_ERR_SHAPE, "ozgemm_tc: N too large");
   {
     ProfScope prof(c, "ozgemm");
     ProfScope prof_tag(g.tag ? c : nullptr, g.tag ? g.tag : "");
-    ozgemm_tc_kernel<LV><<<grid, TTHREADS, smem, c->stream>>>(ta, tb, t);
+    ozgemm_tc_kernel<LV, BK><<<grid, TTHREADS, smem, c->stream>>>(ta, tb, t);
     THC_LAUNCHED(c, "ozgemm_tc");
   }
   if (t.ksplit > 1) return oz_split_reduce(c, g);
   return THC_OK;
+}
+
+template <int BK>
+int launch_bk(Ctx* c, const OzArgs& g, int* err_flag)
+{
+  switch (g.levels) {
+    case 2: return launch_tc<2, BK>(c, g, err_flag);
+    case 3: return launch_tc<3, BK>(c, g, err_flag);
+    case 4: return launch_tc<4, BK>(c, g, err_flag);
+    case 5: return launch_tc<5, BK>(c, g, err_flag);
+    case 6: return launch_tc<6, BK>(c, g, err_flag);
+    default: return set_error(c, THC_ERR_ARG, "ozgemm_tc: levels must be 2..6");
+  }
 }
 
 }  // namespace
@@ -521,14 +573,7 @@ int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
   const long long br = g.b.kt_stride ? g.b.slice_stride / 32 : g.b.slice_stride / g.b.ld;
   if (g.a.ld % 32 || g.b.ld % 32 || ar % TBM || br % TBN)
     return set_error(c, THC_ERR_ARG, "ozgemm_tc: operand padding");
-  switch (g.levels) {
-    case 2: return launch_tc<2>(c, g, err_flag);
-    case 3: return launch_tc<3>(c, g, err_flag);
-    case 4: return launch_tc<4>(c, g, err_flag);
-    case 5: return launch_tc<5>(c, g, err_flag);
-    case 6: return launch_tc<6>(c, g, err_flag);
-    default: return set_error(c, THC_ERR_ARG, "ozgemm_tc: levels must be 2..6");
-  }
+  return c->tc_bk == 32 ? launch_bk<32>(c, g, err_flag) : launch_bk<16>(c, g, err_flag);
 }
 
 }  // namespace thc
