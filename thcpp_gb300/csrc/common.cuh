@@ -61,6 +61,8 @@ enum Slot : int {
   WS_ROWMAX,        // per-row maxima for slicing
   WS_DPART,         // split-K partials chosen inside dgemm
   WS_FFTWORK,       // cuFFT work area of the context's plans
+  WS_KM_SV,         // k-means terms: 4 x ng doubles in point order + 4 x ng sorted
+  WS_KM_WIN,        // k-means windows, cluster window offsets, segment tables
   WS_NSLOTS
 };
 

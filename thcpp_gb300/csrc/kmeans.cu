@@ -80,7 +80,15 @@ struct KmState {
   int diff_exact;                        // st->diff came from the sequential sum
   int ticket;                            // blocks of km_sums finished this iteration
   int scan_ticket;                       // blocks of km_colscan finished this iteration
-  int pad4;
+  int nwin;                              // windows of the exact sums this iteration
+};
+
+// One window of <= kSegWin consecutive terms of one cluster in the sorted term arrays.
+struct KmWin {
+  int pos;     // sorted position of the window's first term
+  int cnt;     // terms in the window
+  int first;   // sorted position of the cluster's first term
+  int k;       // cluster
 };
 
 struct KmBufs {
@@ -105,6 +113,14 @@ struct KmBufs {
   int* pbin;       // [ng] bin of each point
   int* bcount;     // [nbins_max] counts, then offsets, then cursors
   int nbins_max;
+  // Window-parallel exact sums (nwin_max == 0: the one-kernel km_sums path).
+  const double* tq;   // [4][ng] rho_i, rho_i x_i, rho_i y_i, rho_i z_i in point order
+  double* sv;         // [4][ng] the same terms in sorted (cluster, ascending point) order
+  KmWin* win;         // [nwin_max]
+  int* wbase;         // [nmu + 1] first window of each cluster
+  SegScratch* seg;    // [nwin_max][4] segment tables
+  int nwin_max;
+  int pad5;
 };
 
 __device__ __forceinline__ double d2_exact(double cx, double cy, double cz, double gx,
@@ -164,7 +180,17 @@ __global__ void km_prep(const double* __restrict__ grid, const double* __restric
     double x = grid[3 * i], y = grid[3 * i + 1], z = grid[3 * i + 2];
     gx[i] = x; gy[i] = y; gz[i] = z;
     fx[i] = (float)x; fy[i] = (float)y; fz[i] = (float)z;
-    rho[i] = rho_in[i];
+    const double r = rho_in[i];
+    rho[i] = r;
+    if (b.tq) {
+      // The products of the reference's centroid loop (src/kmeans.cpp:121-126), rounded
+      // once each; they do not change between iterations.
+      double* tq = const_cast<double*>(b.tq);
+      tq[i] = r;
+      tq[b.ng + i] = __dmul_rn(r, x);
+      tq[2 * b.ng + i] = __dmul_rn(r, y);
+      tq[3 * b.ng + i] = __dmul_rn(r, z);
+    }
     ax = fabs(x); ay = fabs(y); az = fabs(z);
   }
   for (int off = 16; off; off >>= 1) {
@@ -673,21 +699,16 @@ __global__ void km_hist(KmBufs b)
     if (sh[k]) b.hist[(size_t)k * b.nb + blockIdx.x] = sh[k];
 }
 
-// Exclusive scan of the cluster totals into cluster start offsets (one block).
-__device__ void kscan_block(KmBufs& b)
+// Exclusive block-wide scan of one int per thread (all threads of the block).
+__device__ int block_exscan(int v, int* warp_sums)
 {
-  __shared__ int warp_sums[32];
-  int n = b.nmu;
-  int per = (n + blockDim.x - 1) / blockDim.x;
-  int lo = threadIdx.x * per, hi = min(n, lo + per);
-  int s = 0;
-  for (int k = lo; k < hi; k++) s += __ldcg(b.total + k);
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int x = s;
+  int x = v;
   for (int off = 1; off < 32; off <<= 1) {
     int y = __shfl_up_sync(0xffffffffu, x, off);
     if (lane >= off) x += y;
   }
+  __syncthreads();
   if (lane == 31) warp_sums[wid] = x;
   __syncthreads();
   if (wid == 0) {
@@ -700,11 +721,47 @@ __device__ void kscan_block(KmBufs& b)
     warp_sums[lane] = xw - w;
   }
   __syncthreads();
-  int run = warp_sums[wid] + x - s;
+  return warp_sums[wid] + x - v;
+}
+
+// Exclusive scan of the cluster totals into cluster start offsets (one block); with the
+// window-parallel sums also the window table: cluster k's terms are cut into windows of
+// kSegWin, numbered consecutively from wbase[k].
+__device__ void kscan_block(KmBufs& b)
+{
+  __shared__ int warp_sums[32];
+  int n = b.nmu;
+  int per = (n + blockDim.x - 1) / blockDim.x;
+  int lo = threadIdx.x * per, hi = min(n, lo + per);
+  int s = 0, nw = 0;
   for (int k = lo; k < hi; k++) {
-    b.start[k] = run;
-    run += __ldcg(b.total + k);
+    int t = __ldcg(b.total + k);
+    s += t;
+    nw += (t + kSegWin - 1) / kSegWin;
   }
+  int run = block_exscan(s, warp_sums);
+  int wrun = b.nwin_max ? block_exscan(nw, warp_sums) : 0;
+  for (int k = lo; k < hi; k++) {
+    const int t = __ldcg(b.total + k);
+    b.start[k] = run;
+    if (b.nwin_max) {
+      b.wbase[k] = wrun;
+      for (int j = 0; j * kSegWin < t; j++) {
+        KmWin w;
+        w.pos = run + j * kSegWin;
+        w.cnt = min(kSegWin, t - j * kSegWin);
+        w.first = run;
+        w.k = k;
+        b.win[wrun++] = w;
+      }
+    }
+    run += t;
+  }
+  if (b.nwin_max && hi == n && lo < hi) {
+    b.wbase[n] = wrun;
+    b.st->nwin = wrun;
+  }
+  if (b.nwin_max && n == 0 && threadIdx.x == 0) b.st->nwin = 0;
 }
 
 // One warp per cluster: exclusive scan of its block counts (in place) and its total.  The
@@ -746,14 +803,16 @@ __global__ void __launch_bounds__(256) km_colscan(KmBufs b)
 
 // Stable scatter of point indices into per-cluster member lists.  The block's labels and
 // every cluster's output offset are staged in shared memory by all threads; then warp 0
-// walks the points in ascending order, 32 at a time, and lanes with equal labels take
-// ranks from __match_any_sync, so each cluster keeps ascending grid order.
+// ranks the points in ascending order, 32 at a time (lanes with equal labels take ranks
+// from __match_any_sync, so each cluster keeps ascending grid order), and all threads
+// write the members -- and, for the window-parallel sums, their four terms -- in place.
 __global__ void __launch_bounds__(256) km_scatter(KmBufs b)
 {
   if (b.st->done) return;
   const int it = b.st->iter;
   extern __shared__ int base[];          // nmu offsets
   __shared__ int slab[kBP];
+  __shared__ int spos[kBP];
   const int* lab = b.labels + (size_t)(it & 1) * b.ng;
   const long long blk = (long long)blockIdx.x * kBP;
   for (int k = threadIdx.x; k < b.nmu; k += blockDim.x)
@@ -763,25 +822,37 @@ __global__ void __launch_bounds__(256) km_scatter(KmBufs b)
     int l = i < b.ng ? lab[i] : -1;
     if (i < b.ng && (unsigned)l >= (unsigned)b.nmu) l = 0;  // flagged by km_hist
     slab[t] = l;
+    spos[t] = -1;
   }
   __syncthreads();
-  if (threadIdx.x >= 32) return;
-  const int lane = threadIdx.x;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int c = 0; c < kBP; c += 32) {
-    const int l = slab[c + lane];
-    const bool valid = l >= 0;
-    const unsigned active = __ballot_sync(0xffffffffu, valid);
-    if (!active) break;
-    if (valid) {
-      unsigned peers = __match_any_sync(active, l);
-      int leader = __ffs(peers) - 1;
-      int pos = base[l] + __popc(peers & lt);
-      b.member[pos] = (int)(blk + c + lane);
-      __syncwarp(active);
-      if (lane == leader) base[l] += __popc(peers);
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int c = 0; c < kBP; c += 32) {
+      const int l = slab[c + lane];
+      const bool valid = l >= 0;
+      const unsigned active = __ballot_sync(0xffffffffu, valid);
+      if (!active) break;
+      if (valid) {
+        unsigned peers = __match_any_sync(active, l);
+        int leader = __ffs(peers) - 1;
+        spos[c + lane] = base[l] + __popc(peers & lt);
+        __syncwarp(active);
+        if (lane == leader) base[l] += __popc(peers);
+      }
+      __syncwarp();
     }
-    __syncwarp();
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kBP; t += blockDim.x) {
+    const int pos = spos[t];
+    if (pos < 0) continue;
+    const long long i = blk + t;
+    b.member[pos] = (int)i;
+    if (b.sv) {
+#pragma unroll
+      for (int q = 0; q < 4; q++) b.sv[(size_t)q * b.ng + pos] = __ldg(b.tq + (size_t)q * b.ng + i);
+    }
   }
 }
 
@@ -839,6 +910,84 @@ __device__ double normdiff_terms(const KmBufs& b, const double* a, const double*
   }
   __syncthreads();
   return scale;
+}
+
+// End of an iteration's sums for cluster k (whole block; res[0..3] = w, x, y, z sums): the
+// new centroid, its squared move, and -- in the last block to finish, found by a ticket in
+// the state -- the convergence decision: the normed difference approximated by a
+// fixed-order sum of squared centroid moves (relative deviation from the reference's value
+// below (3 N_mu + 8) u), evaluated exactly when within 1e-10 of the threshold.
+__device__ void sums_finish(const KmBufs& b, int k, int it, double* res, double* red, int& last)
+{
+  KmState* st = b.st;
+  const int nmu = b.nmu;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* part = b.terms + 3 * (size_t)nmu;   // per-cluster squared move
+  if (threadIdx.x < 3) {   // one coordinate each: c_d = sum_d / w (the reference's division)
+    const int d = threadIdx.x;
+    double* nc = b.cen + (size_t)((it + 1) & 1) * 3 * nmu;
+    float* nc32 = b.cen32 + (size_t)((it + 1) & 1) * 3 * nmu;
+    const double* oc = b.cen + (size_t)(it & 1) * 3 * nmu;
+    const double v = __ddiv_rn(res[1 + d], res[0]);
+    nc[d * nmu + k] = v;
+    nc32[d * nmu + k] = (float)v;
+    red[d] = __dsub_rn(v, oc[d * nmu + k]);
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (res[0] < 1e-8) atomicExch(&st->empty, 1);
+    double sq = 0.0;
+    for (int d = 0; d < 3; d++) sq = __fma_rn(red[d], red[d], sq);
+    part[k] = sq;
+    __threadfence();
+    last = atomicAdd(&st->ticket, 1) == nmu - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // ---- last block: the convergence decision and the state update of this iteration ----
+  if (*(volatile int*)&st->empty || *(volatile int*)&st->bad_label) {
+    if (threadIdx.x == 0) { st->done = 1; st->iter = it + 1; st->ticket = 0; }
+    return;
+  }
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nmu; i += blockDim.x) v += __ldcg(part + i);
+  const double approx = sqrt(block_sum(v, red));
+  const double thr = st->threshold;
+  const bool exact = fabs(approx - thr) <= 1e-10 * thr;
+  double diff = approx;
+  if (exact) {
+    const double* a = b.cen + (size_t)((it + 1) & 1) * 3 * nmu;
+    const double* c = b.cen + (size_t)(it & 1) * 3 * nmu;
+    double scale = normdiff_terms(b, a, c, b.terms, red);
+    if (warp == 0) {
+      double ssum = warp_seqsum(0.0, b.terms, 3 * nmu);
+      if (lane == 0) res[0] = __dmul_rn(scale, __dsqrt_rn(ssum));
+    }
+    __syncthreads();
+    diff = res[0];
+  }
+  if (threadIdx.x == 0) {
+    st->diff_exact = exact;
+    st->diff = diff;
+    st->pct = 100.0 * (double)st->changed / (double)b.ng;
+    b.log[it] = diff;
+    b.log[st->max_it + it] = st->pct;
+    st->changed = 0;
+    st->rechecked_total += st->recheck_n;
+    st->recheck_n = 0;
+    st->final_buf = (it + 1) & 1;
+    if (diff < thr) {
+      st->converged = 1;
+      st->done = 1;
+    } else if (it + 1 >= st->max_it) {
+      st->done = 1;
+      st->zero_fill = !(diff > thr);
+    }
+    st->ticket = 0;
+    st->iter = it + 1;
+  }
 }
 
 // One block of sixteen warps per cluster.  All threads gather up to kSumCap members and
@@ -938,70 +1087,53 @@ __global__ void __launch_bounds__(kSumThreads) km_sums(KmBufs b)
   __syncthreads();
   if (threadIdx.x < 4) res[threadIdx.x] = sm.acc[threadIdx.x];
   __syncthreads();
-  double* part = b.terms + 3 * (size_t)nmu;   // per-cluster squared move
-  if (threadIdx.x == 0) {
-    const double wsum = res[0];
-    if (wsum < 1e-8) atomicExch(&st->empty, 1);
-    double* nc = b.cen + (size_t)((it + 1) & 1) * 3 * nmu;
-    float* nc32 = b.cen32 + (size_t)((it + 1) & 1) * 3 * nmu;
-    const double* oc = b.cen + (size_t)(it & 1) * 3 * nmu;
-    double sq = 0.0;
-    for (int d = 0; d < 3; d++) {
-      double v = __ddiv_rn(res[1 + d], wsum);
-      nc[d * nmu + k] = v;
-      nc32[d * nmu + k] = (float)v;
-      double dv = v - oc[d * nmu + k];
-      sq += dv * dv;
-    }
-    part[k] = sq;
-    __threadfence();
-    last = atomicAdd(&st->ticket, 1) == nmu - 1;
+  sums_finish(b, k, it, res, red, last);
+}
+
+// Window-parallel exact sums, phase 1: one warp per (window, quantity) builds the window's
+// segment table (seg_build), steered by an FP32 estimate of the cluster's running sum at
+// the window's start (the sum of the cluster's earlier terms; it only has to predict
+// binades).  Windows are independent, so every SM takes part however uneven the clusters.
+constexpr int kBuildThreads = 256;
+__global__ void __launch_bounds__(kBuildThreads) km_sbuild(KmBufs b)
+{
+  const KmState* st = b.st;
+  if (st->done) return;
+  const int gw = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int w = gw >> 2, q = gw & 3;
+  if (w >= st->nwin) return;
+  const int lane = threadIdx.x & 31;
+  const KmWin wi = b.win[w];
+  const double* t = b.sv + (size_t)q * b.ng;
+  float f = 0.f;
+  for (int i = wi.first + lane; i < wi.pos; i += 32) f += (float)t[i];
+  for (int off = 16; off; off >>= 1) f += __shfl_xor_sync(0xffffffffu, f, off);
+  seg_build((double)f, t + wi.pos, wi.cnt, b.seg[(size_t)w * 4 + q]);
+}
+
+// Phase 2: one block of four warps per cluster; warp q walks quantity q (0 = w, 1 = x,
+// 2 = y, 3 = z) over the cluster's windows in order with the exact running sum, strictly in
+// ascending member order as the reference's loop (src/kmeans.cpp:121-126).  Then the new
+// centroid and, in the last block, the convergence decision (sums_finish).
+__global__ void __launch_bounds__(128) km_swalk(KmBufs b)
+{
+  KmState* st = b.st;
+  if (st->done) return;
+  __shared__ double res[4];
+  __shared__ double red[32];
+  __shared__ int last;
+  const int it = st->iter;
+  const int k = blockIdx.x, q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w0 = b.wbase[k], w1 = b.wbase[k + 1];
+  const double* t = b.sv + (size_t)q * b.ng;
+  double acc = 0.0;
+  for (int w = w0; w < w1; w++) {
+    const KmWin wi = b.win[w];
+    acc = seg_walk_reg(acc, t + wi.pos, wi.cnt, b.seg[(size_t)w * 4 + q]);
   }
+  if (lane == 0) res[q] = acc;
   __syncthreads();
-  if (!last) return;
-  __threadfence();
-  // ---- last block: the convergence decision and the state update of this iteration ----
-  if (*(volatile int*)&st->empty || *(volatile int*)&st->bad_label) {
-    if (threadIdx.x == 0) { st->done = 1; st->iter = it + 1; st->ticket = 0; }
-    return;
-  }
-  double v = 0.0;
-  for (int i = threadIdx.x; i < nmu; i += kSumThreads) v += __ldcg(part + i);
-  const double approx = sqrt(block_sum(v, red));
-  const double thr = st->threshold;
-  const bool exact = fabs(approx - thr) <= 1e-10 * thr;
-  double diff = approx;
-  if (exact) {
-    const double* a = b.cen + (size_t)((it + 1) & 1) * 3 * nmu;
-    const double* c = b.cen + (size_t)(it & 1) * 3 * nmu;
-    double scale = normdiff_terms(b, a, c, b.terms, red);
-    if (warp == 0) {
-      double ssum = warp_seqsum(0.0, b.terms, 3 * nmu);
-      if (lane == 0) res[0] = __dmul_rn(scale, __dsqrt_rn(ssum));
-    }
-    __syncthreads();
-    diff = res[0];
-  }
-  if (threadIdx.x == 0) {
-    st->diff_exact = exact;
-    st->diff = diff;
-    st->pct = 100.0 * (double)st->changed / (double)b.ng;
-    b.log[it] = diff;
-    b.log[st->max_it + it] = st->pct;
-    st->changed = 0;
-    st->rechecked_total += st->recheck_n;
-    st->recheck_n = 0;
-    st->final_buf = (it + 1) & 1;
-    if (diff < thr) {
-      st->converged = 1;
-      st->done = 1;
-    } else if (it + 1 >= st->max_it) {
-      st->done = 1;
-      st->zero_fill = !(diff > thr);
-    }
-    st->ticket = 0;
-    st->iter = it + 1;
-  }
+  sums_finish(b, k, it, res, red, last);
 }
 
 // The reference's normed difference of the last iteration, exactly (one block).
@@ -1288,6 +1420,21 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   b.cen = cen; b.cen32 = cen32; b.labels = labels; b.hist = hist; b.total = tot;
   b.start = tot + nmu; b.member = member; b.terms = terms; b.recheck = recheck;
   b.log = logb; b.st = st;
+  if (!fixed) {
+    // Window-parallel exact sums (the caller-provided fixed scratch keeps the one-kernel
+    // sums, whose footprint is smaller).
+    const long long nwin_max = ng / kSegWin + nmu + 1;
+    double* svb = (double*)al.get(WS_KM_SV, sizeof(double) * 8 * ng);
+    const size_t win_bytes = ((sizeof(KmWin) * nwin_max + sizeof(int) * (nmu + 1) + 255) / 256) * 256;
+    char* wb = (char*)al.get(WS_KM_WIN, win_bytes + sizeof(SegScratch) * 4 * nwin_max);
+    if (!svb || !wb) return set_error(c, THC_ERR_NOMEM, "thc_kmeans: workspace allocation failed");
+    b.tq = svb;
+    b.sv = svb + 4 * ng;
+    b.win = (KmWin*)wb;
+    b.wbase = (int*)(wb + sizeof(KmWin) * nwin_max);
+    b.seg = (SegScratch*)(wb + win_bytes);
+    b.nwin_max = (int)nwin_max;
+  }
 
   KmState h{};
   h.max_it = max_it;
@@ -1358,8 +1505,15 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     THC_LAUNCHED(c, "km_colscan");
     km_scatter<<<b.nb, 256, hist_smem, s>>>(b);
     THC_LAUNCHED(c, "km_scatter");
-    km_sums<<<nmu, kSumThreads, sizeof(SumSmem), s>>>(b);
-    THC_LAUNCHED(c, "km_sums");
+    if (b.nwin_max) {
+      km_sbuild<<<(int)cdiv((long long)b.nwin_max * 4 * 32, kBuildThreads), kBuildThreads, 0, s>>>(b);
+      THC_LAUNCHED(c, "km_sbuild");
+      km_swalk<<<nmu, 128, 0, s>>>(b);
+      THC_LAUNCHED(c, "km_swalk");
+    } else {
+      km_sums<<<nmu, kSumThreads, sizeof(SumSmem), s>>>(b);
+      THC_LAUNCHED(c, "km_sums");
+    }
     return THC_OK;
   };
   // A CUDA graph of kCheckEvery iterations, cached on the context for these buffers.

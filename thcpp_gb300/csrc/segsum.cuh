@@ -40,6 +40,7 @@ struct SegScratch {
   int seg_e[kSegMax];
   long long seg_c0[kSegMax];   // -1: the segment holds an invalid step
   long long seg_c1[kSegMax];
+  double seg_t[kSegMax];       // the segment's first term
 };
 
 // Composite of the parity maps x then y: c_p = x_p + y_[(p + x_p) & 1].
@@ -54,9 +55,16 @@ __device__ __forceinline__ void seg_compose(long long x0, long long x1, long lon
 
 // The parity map of one non-start term t (finite, non-negative) on the grid of biased
 // exponent e, without branches so that the eight terms of a lane overlap.  A term of at
-// least 2^52 grid units (shift <= 0) cannot stay inside the binade: flagged invalid.
+// least 2^52 grid units (shift <= 0) cannot stay inside the binade: flagged invalid.  In a
+// segment predicted to stay at +0 (e == 0: leading zero terms of a quantity, e.g. rho x at
+// x = 0) a step is valid only for t == +0, and it leaves the sum at +0 (c = 0).
 __device__ __forceinline__ void seg_term(double t, int e, long long& c0, long long& c1, bool& bad)
 {
+  if (e == 0) {
+    c0 = c1 = 0;
+    bad = __double_as_longlong(t) != 0;
+    return;
+  }
   const unsigned long long tb = (unsigned long long)__double_as_longlong(t);
   const int et = (int)((tb >> 52) & 0x7ff);
   unsigned long long m = tb & ((1ULL << 52) - 1);
@@ -204,6 +212,7 @@ __device__ __noinline__ void seg_build(double acc_pred, const double* tw, int cn
         sidx++;
         sc.seg_pos[sidx] = i;
         sc.seg_e[sidx] = E[u];
+        sc.seg_t[sidx] = term(u);
         c0 = c1 = 0;
         cbad = false;
       } else {
@@ -243,8 +252,53 @@ __device__ __noinline__ double seg_walk(double acc, const double* tw, int cnt, c
     const int ea = (int)((ab >> 52) & 0x7ff);
     const long long S = (ab & (kLo - 1)) + kLo;
     const long long c0 = sc.seg_c0[j];
+    if (ab == 0 && sc.seg_e[j] == 0 && c0 >= 0) continue;   // +0 through +0 terms
     const long long R = S + ((S & 1) ? sc.seg_c1[j] : c0);
     if (ab > 0 && ea >= 1 && ea < 0x7fe && ea == sc.seg_e[j] && c0 >= 0 && R < kHi) {
+      acc = __longlong_as_double(((long long)ea << 52) | (R - kLo));
+    } else {
+      acc = warp_seqsum(acc, tw + a + 1, cnt - a - 1);
+      break;
+    }
+  }
+  return acc;
+}
+
+// seg_walk for a table in global memory: the warp first loads the whole table into
+// registers (lane l holds entries l and l + 32), so the serial walk waits on no memory.
+__device__ __noinline__ double seg_walk_reg(double acc, const double* tw, int cnt,
+                                            const SegScratch& sc)
+{
+  const unsigned full = 0xffffffffu;
+  const long long kLo = 1LL << 52, kHi = 1LL << 53;
+  const int lane = threadIdx.x & 31;
+  const int total = sc.nseg;
+  if (total < 0) return warp_seqsum(acc, tw, cnt);
+  const bool ha = lane < total, hb = lane + 32 < total;
+  const int pA = ha ? sc.seg_pos[lane] : cnt, pB = hb ? sc.seg_pos[lane + 32] : cnt;
+  const int eA = ha ? sc.seg_e[lane] : 0, eB = hb ? sc.seg_e[lane + 32] : 0;
+  const long long aA = ha ? sc.seg_c0[lane] : 0, aB = hb ? sc.seg_c0[lane + 32] : 0;
+  const long long bA = ha ? sc.seg_c1[lane] : 0, bB = hb ? sc.seg_c1[lane + 32] : 0;
+  const double tA = ha ? sc.seg_t[lane] : 0.0, tB = hb ? sc.seg_t[lane + 32] : 0.0;
+  for (int j = 0; j < total; j++) {
+    const int src = j & 31;
+    const bool hi = j >= 32;
+    const int a = __shfl_sync(full, hi ? pB : pA, src);
+    const int jn = j + 1;
+    const int nx = __shfl_sync(full, jn >= 32 ? pB : pA, jn & 31);
+    const int bnd = (jn < total ? nx : cnt) - 1;
+    const int e = __shfl_sync(full, hi ? eB : eA, src);
+    const long long c0 = __shfl_sync(full, hi ? aB : aA, src);
+    const long long c1 = __shfl_sync(full, hi ? bB : bA, src);
+    const double t0 = __shfl_sync(full, hi ? tB : tA, src);
+    acc = __dadd_rn(acc, t0);
+    if (bnd == a) continue;
+    const long long ab = __double_as_longlong(acc);
+    if (ab == 0 && e == 0 && c0 >= 0) continue;   // +0 through +0 terms
+    const int ea = (int)((ab >> 52) & 0x7ff);
+    const long long S = (ab & (kLo - 1)) + kLo;
+    const long long R = S + ((S & 1) ? c1 : c0);
+    if (ab > 0 && ea >= 1 && ea < 0x7fe && ea == e && c0 >= 0 && R < kHi) {
       acc = __longlong_as_double(((long long)ea << 52) | (R - kLo));
     } else {
       acc = warp_seqsum(acc, tw + a + 1, cnt - a - 1);
