@@ -1127,9 +1127,21 @@ __global__ void __launch_bounds__(128) km_swalk(KmBufs b)
   const int w0 = b.wbase[k], w1 = b.wbase[k + 1];
   const double* t = b.sv + (size_t)q * b.ng;
   double acc = 0.0;
-  for (int w = w0; w < w1; w++) {
-    const KmWin wi = b.win[w];
-    acc = seg_walk_reg(acc, t + wi.pos, wi.cnt, b.seg[(size_t)w * 4 + q]);
+  if (w0 < w1) {
+    // The next window's position and table are loaded while the current one is walked.
+    KmWin wi = b.win[w0];
+    SegRegs cur = seg_load(b.seg[(size_t)w0 * 4 + q], wi.cnt);
+    for (int w = w0; w < w1; w++) {
+      KmWin wn = wi;
+      SegRegs nxt = cur;
+      if (w + 1 < w1) {
+        wn = b.win[w + 1];
+        nxt = seg_load(b.seg[(size_t)(w + 1) * 4 + q], wn.cnt);
+      }
+      acc = seg_walk_regs(acc, t + wi.pos, wi.cnt, cur);
+      wi = wn;
+      cur = nxt;
+    }
   }
   if (lane == 0) res[q] = acc;
   __syncthreads();

@@ -264,33 +264,54 @@ __device__ __noinline__ double seg_walk(double acc, const double* tw, int cnt, c
   return acc;
 }
 
-// seg_walk for a table in global memory: the warp first loads the whole table into
-// registers (lane l holds entries l and l + 32), so the serial walk waits on no memory.
-__device__ __noinline__ double seg_walk_reg(double acc, const double* tw, int cnt,
-                                            const SegScratch& sc)
+// A segment table held in registers: lane l holds entries l and l + 32.
+struct SegRegs {
+  int total;
+  int pA, pB, eA, eB;
+  long long aA, aB, bA, bB;
+  double tA, tB;
+};
+
+// Loads a table from global memory into registers (one round trip; the loads are issued
+// together and can be in flight while the warp walks the previous window).
+__device__ __forceinline__ SegRegs seg_load(const SegScratch& sc, int cnt)
+{
+  const int lane = threadIdx.x & 31;
+  SegRegs r;
+  r.total = sc.nseg;
+  const bool ha = lane < r.total, hb = lane + 32 < r.total;
+  r.pA = ha ? sc.seg_pos[lane] : cnt;
+  r.pB = hb ? sc.seg_pos[lane + 32] : cnt;
+  r.eA = ha ? sc.seg_e[lane] : 0;
+  r.eB = hb ? sc.seg_e[lane + 32] : 0;
+  r.aA = ha ? sc.seg_c0[lane] : 0;
+  r.aB = hb ? sc.seg_c0[lane + 32] : 0;
+  r.bA = ha ? sc.seg_c1[lane] : 0;
+  r.bB = hb ? sc.seg_c1[lane + 32] : 0;
+  r.tA = ha ? sc.seg_t[lane] : 0.0;
+  r.tB = hb ? sc.seg_t[lane + 32] : 0.0;
+  return r;
+}
+
+// seg_walk with the table in registers, so the serial walk waits on no memory.
+__device__ __forceinline__ double seg_walk_regs(double acc, const double* tw, int cnt,
+                                                const SegRegs& r)
 {
   const unsigned full = 0xffffffffu;
   const long long kLo = 1LL << 52, kHi = 1LL << 53;
-  const int lane = threadIdx.x & 31;
-  const int total = sc.nseg;
+  const int total = r.total;
   if (total < 0) return warp_seqsum(acc, tw, cnt);
-  const bool ha = lane < total, hb = lane + 32 < total;
-  const int pA = ha ? sc.seg_pos[lane] : cnt, pB = hb ? sc.seg_pos[lane + 32] : cnt;
-  const int eA = ha ? sc.seg_e[lane] : 0, eB = hb ? sc.seg_e[lane + 32] : 0;
-  const long long aA = ha ? sc.seg_c0[lane] : 0, aB = hb ? sc.seg_c0[lane + 32] : 0;
-  const long long bA = ha ? sc.seg_c1[lane] : 0, bB = hb ? sc.seg_c1[lane + 32] : 0;
-  const double tA = ha ? sc.seg_t[lane] : 0.0, tB = hb ? sc.seg_t[lane + 32] : 0.0;
   for (int j = 0; j < total; j++) {
     const int src = j & 31;
     const bool hi = j >= 32;
-    const int a = __shfl_sync(full, hi ? pB : pA, src);
+    const int a = __shfl_sync(full, hi ? r.pB : r.pA, src);
     const int jn = j + 1;
-    const int nx = __shfl_sync(full, jn >= 32 ? pB : pA, jn & 31);
+    const int nx = __shfl_sync(full, jn >= 32 ? r.pB : r.pA, jn & 31);
     const int bnd = (jn < total ? nx : cnt) - 1;
-    const int e = __shfl_sync(full, hi ? eB : eA, src);
-    const long long c0 = __shfl_sync(full, hi ? aB : aA, src);
-    const long long c1 = __shfl_sync(full, hi ? bB : bA, src);
-    const double t0 = __shfl_sync(full, hi ? tB : tA, src);
+    const int e = __shfl_sync(full, hi ? r.eB : r.eA, src);
+    const long long c0 = __shfl_sync(full, hi ? r.aB : r.aA, src);
+    const long long c1 = __shfl_sync(full, hi ? r.bB : r.bA, src);
+    const double t0 = __shfl_sync(full, hi ? r.tB : r.tA, src);
     acc = __dadd_rn(acc, t0);
     if (bnd == a) continue;
     const long long ab = __double_as_longlong(acc);
