@@ -147,6 +147,19 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v)
+{
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
 {
   uint32_t r[16];
@@ -218,7 +231,12 @@ struct TcCfg {
   static constexpr int STAGES = kStageBudget / STAGE_BYTES < 4 ? kStageBudget / STAGE_BYTES : 4;
   static constexpr int CHUNK_STAGES = kChunkK / BK;
   static constexpr int NEXACT = LV < 3 ? LV : 3;          // exact level accumulators
-  static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256 + kSmemGuard;
+  // The stage buffers, reused after the main loop to stage the epilogue's 8 warps x 32 x 64
+  // 8-byte results; the barriers follow.
+  static constexpr int EPI_BYTES = TEPI_WARPS * 32 * 64 * 8;
+  static constexpr int BUF_BYTES = STAGES * STAGE_BYTES > EPI_BYTES ? STAGES * STAGE_BYTES : EPI_BYTES;
+  // + barriers (256 B) + the tile's 128 column exponents (512 B) + guard.
+  static constexpr size_t SMEM = (size_t)BUF_BYTES + 1024 + 256 + 512 + kSmemGuard;
   static_assert(STAGES >= 2, "stage buffers");
 };
 
@@ -249,7 +267,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
 
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + NST * STAGE_BYTES);
+  uint64_t* full = (uint64_t*)(smem + Cfg::BUF_BYTES);
   uint64_t* empty = full + NST;
   uint64_t* acc_full = empty + NST;
   uint64_t* acc_empty = acc_full + 1;
@@ -370,6 +388,17 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     const int half = ew >> 2;                // which 64-column half of the tile
     const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
     const int col0 = half * 64;
+    // Exponents of this row and of the half's 64 columns, loaded while the MMAs run (both
+    // warps of a half store the same values).
+    int* seb = (int*)((unsigned char*)full + 256) + col0;
+    {
+      const long long na = n0 + col0 + lane, nb = na + 32;
+      seb[lane] = na < g.N ? g.eb[na] : 0;
+      seb[lane + 32] = nb < g.N ? g.eb[nb] : 0;
+    }
+    const long long m = m0 + quad * 32 + lane;
+    const int ea = (m < g.M ? g.ea[m] : 0) - 14;
+    __syncwarp();
     // Double-word FP32 totals of this thread's row, 64 columns.
     float ah[64], al[64];
 #pragma unroll
@@ -379,16 +408,16 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       if (!mbar_wait(acc_full, (uint32_t)(ch & 1), abort)) { ok = false; break; }
       asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
-      for (int b = 0; b < 4; b++) {
-        float l0[16], l1[16], l2[16];
-        const uint32_t cb = (uint32_t)(col0 + 16 * b);
-        tmem_ld16(tmem + lane_base + 0 * TBN + cb, l0);
-        if (LV > 1) tmem_ld16(tmem + lane_base + 1 * TBN + cb, l1);
-        if (LV > 2) tmem_ld16(tmem + lane_base + 2 * TBN + cb, l2);
+      for (int b = 0; b < 8; b++) {   // 8 columns at a time (register pressure)
+        float l0[8], l1[8], l2[8];
+        const uint32_t cb = (uint32_t)(col0 + 8 * b);
+        tmem_ld8(tmem + lane_base + 0 * TBN + cb, l0);
+        if (LV > 1) tmem_ld8(tmem + lane_base + 1 * TBN + cb, l1);
+        if (LV > 2) tmem_ld8(tmem + lane_base + 2 * TBN + cb, l2);
         // l0, l1, l2 are exact (multiples of 1, 2^-7, 2^-14 below 2^24, 2^17, 2^10); their
         // sum needs <= 38 bits and is carried exactly in (s, e).
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
+        for (int q = 0; q < 8; q++) {
           float s1 = l0[q], e1 = 0.f;
           if (LV > 1) two_sum(l0[q], l1[q], s1, e1);
           if (LV > 2) {
@@ -397,8 +426,8 @@ __global__ void __launch_bounds__(TTHREADS, 1)
             s1 = s2;
             e1 = __fadd_rn(e1, e2);
           }
-          dw_add(ah[16 * b + q], al[16 * b + q], s1);
-          dw_add(ah[16 * b + q], al[16 * b + q], e1);
+          dw_add(ah[8 * b + q], al[8 * b + q], s1);
+          dw_add(ah[8 * b + q], al[8 * b + q], e1);
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n");
@@ -415,51 +444,81 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       }
     }
     if (ok && !*abort) {
-      long long m = m0 + quad * 32 + lane;
-      if (m < g.M) {
-        int ea = g.ea[m] - 14;
+      // The warp's 32 x 64 results go through shared memory (the stage buffers are free:
+      // every MMA has completed, so every TMA load has landed and been consumed) and are
+      // written row by row, so each store instruction covers 256-512 contiguous bytes
+      // instead of 32 rows kilobytes apart.
+      const bool split = g.ksplit > 1;
+      const bool f32 = !split && g.epilogue == OZ_STORE_F32;
+      unsigned char* stg = smem + (size_t)ew * (32 * 64 * 8);
+      float* stg32 = (float*)stg;
+      double* stg64 = (double*)stg;
 #pragma unroll
-        for (int q = 0; q < 64; q++) {
-          long long n = n0 + col0 + q;
-          if (n >= g.N || (g.lower_only && n > m)) continue;
-          int ex = ea + g.eb[n];
-          if (g.epilogue == OZ_STORE_F32 && g.ksplit <= 1 && ex > -126 && ex < 127) {
-            float sc = pow2f(ex);
-            ((float*)g.C)[m * g.ldc + n] = __fadd_rn(ah[q], al[q]) * sc;
-            continue;
-          }
-          if (g.epilogue == OZ_STORE_DW && g.ksplit <= 1 && ex > -100 && ex < 100) {
-            float sc = pow2f(ex);
-            float zh, zl;
-            fast_two_sum(ah[q] * sc, al[q] * sc, zh, zl);
-            ((float2*)g.C)[m * g.ldc + n] = make_float2(zh, zl);
-            continue;
-          }
-          if (g.epilogue == OZ_SQUARE_DW && g.ksplit <= 1 && ex > -60 && ex < 60) {
-            // (h + l)^2 in double-word FP32: p + e = h^2 exactly (FMA), plus 2 h l.
-            float sc = pow2f(ex);
-            float h = ah[q] * sc, l = al[q] * sc;
-            float p = __fmul_rn(h, h);
-            float e = __fmaf_rn(h, h, -p);
-            e = __fmaf_rn(2.f * h, l, e);
-            float zh, zl;
-            fast_two_sum(p, e, zh, zl);
-            ((float2*)g.C)[m * g.ldc + n] = make_float2(zh, zl);
-            continue;
-          }
+      for (int q = 0; q < 64; q++) {
+        const int ex = ea + seb[q];
+        if (f32) {
+          float v;
+          if (ex > -126 && ex < 127) v = __fadd_rn(ah[q], al[q]) * pow2f(ex);
+          else v = (float)(((double)ah[q] + (double)al[q]) * pow2d(ex));
+          stg32[lane * 64 + (q ^ lane)] = v;
+          continue;
+        }
+        double w;   // the 8-byte result: FP64 value, or a double-word pair's bits
+        if (!split && g.epilogue == OZ_STORE_DW && ex > -100 && ex < 100) {
+          float sc = pow2f(ex);
+          float zh, zl;
+          fast_two_sum(ah[q] * sc, al[q] * sc, zh, zl);
+          w = __hiloint2double(__float_as_int(zl), __float_as_int(zh));
+        } else if (!split && g.epilogue == OZ_SQUARE_DW && ex > -60 && ex < 60) {
+          // (h + l)^2 in double-word FP32: p + e = h^2 exactly (FMA), plus 2 h l.
+          float sc = pow2f(ex);
+          float h = ah[q] * sc, l = al[q] * sc;
+          float pp = __fmul_rn(h, h);
+          float e = __fmaf_rn(h, h, -pp);
+          e = __fmaf_rn(2.f * h, l, e);
+          float zh, zl;
+          fast_two_sum(pp, e, zh, zl);
+          w = __hiloint2double(__float_as_int(zl), __float_as_int(zh));
+        } else {
           double val = ((double)ah[q] + (double)al[q]) * pow2d(ex);
-          if (g.ksplit > 1) {
-            g.part[((long long)blockIdx.z * g.M + m) * g.N + n] = val;
-            continue;
-          }
-          if (g.epilogue == OZ_SQUARE_F64 || g.epilogue == OZ_SQUARE_DW) val = val * val;
-          if (g.epilogue == OZ_STORE_F32) {
-            ((float*)g.C)[m * g.ldc + n] = (float)val;
-          } else if (g.epilogue == OZ_SQUARE_DW || g.epilogue == OZ_STORE_DW) {
-            float hi = (float)val;
-            ((float2*)g.C)[m * g.ldc + n] = make_float2(hi, (float)(val - (double)hi));
+          if (!split && (g.epilogue == OZ_SQUARE_F64 || g.epilogue == OZ_SQUARE_DW)) val = val * val;
+          if (!split && (g.epilogue == OZ_SQUARE_DW || g.epilogue == OZ_STORE_DW)) {
+            float hi = (float)val, lo = (float)(val - (double)hi);
+            w = __hiloint2double(__float_as_int(lo), __float_as_int(hi));
           } else {
-            ((double*)g.C)[m * g.ldc + n] = val;
+            w = val;
+          }
+        }
+        stg64[lane * 64 + (q ^ (lane & 15))] = w;
+      }
+      __syncwarp();
+      // Row r of the staging: lane l writes columns 2l and 2l + 1.
+      const long long ld = split ? g.N : g.ldc;
+      const int c0 = 2 * lane;
+      const long long n = n0 + col0 + c0;
+      for (int r = 0; r < 32; r++) {
+        const long long mr = m0 + quad * 32 + r;
+        if (mr >= g.M) break;
+        const bool v0 = n < g.N && !(g.lower_only && n > mr);
+        const bool v1 = n + 1 < g.N && !(g.lower_only && n + 1 > mr);
+        const long long off = mr * ld + n;
+        if (f32) {
+          const float a = stg32[r * 64 + (c0 ^ r)], bb = stg32[r * 64 + ((c0 + 1) ^ r)];
+          float* dst = (float*)g.C + off;
+          if (v0 && v1 && !(off & 1)) *(float2*)dst = make_float2(a, bb);
+          else {
+            if (v0) dst[0] = a;
+            if (v1) dst[1] = bb;
+          }
+        } else {
+          const double a = stg64[r * 64 + (c0 ^ (r & 15))];
+          const double bb = stg64[r * 64 + ((c0 + 1) ^ (r & 15))];
+          double* dst = split ? g.part + (long long)blockIdx.z * g.M * g.N + off
+                              : (double*)g.C + off;
+          if (v0 && v1 && !(off & 1)) *(double2*)dst = make_double2(a, bb);
+          else {
+            if (v0) dst[0] = a;
+            if (v1) dst[1] = bb;
           }
         }
       }
