@@ -136,18 +136,16 @@ __device__ __forceinline__ double rsqrt_fast(double d)
   return __fma_rn(y * e, __fma_rn(0.375, e, 0.5), y);
 }
 
-constexpr int kPanel = 4;   // columns factored per barrier round in potrf_diag_inv
-
 // Factor the diagonal block at (k0, k0) and invert its triangle: writes L_kk into A
 // (upper part zeroed) and L_kk^{-1} into dinv (nb x nb, row-major, zero above the diagonal).
 // Pivots at or below thr stop the factorisation (info = global 1-based index).
-// Blocked by panels of kPanel columns, with three barriers per panel:
-//   (a) one thread factors the panel's kPanel x kPanel diagonal block and inverts it
-//       (registers; the pivots' reciprocal square roots are its only long chain);
-//   (b) the panel rows below, L_ip = A_ip D^{-T}, and the panel's rows of V = L^{-1}
-//       (forward substitution L V = I: V_panel = D^{-1} (rows updated by earlier panels));
-//   (c) the rank-kPanel update of the trailing lower triangle of A and of the rows of V
-//       below the panel.
+// Right-looking, two barriers per column j: (1) column j of L (a_ij r_j, r_j = 1/sqrt(d_j))
+// and row j of V = L^{-1} (v_jc r_j) are scaled in place; (2) the trailing triangle takes
+// a_ic -= a_ij a_cj (c > j) and the rows of V below j take v_ic -= a_ij v_jc (c <= j).  The
+// FP64 pipe (two lanes per clock per SM on this part, whatever the active mask) bounds the
+// block's ~nb^3/3 FMAs, so phase (2) runs as one flat list of work items with every lane
+// busy (a triangle ordered by decreasing column makes the items of step j a prefix).  The
+// thread that updates the next pivot a_{j+1,j+1} forms its reciprocal root at once.
 __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, int n, int k0,
                                                       const double* thr_p, CholStatus* cs,
                                                       double* dinv)
@@ -157,141 +155,71 @@ __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, i
   extern __shared__ double dsm[];                       // 2 x NB x (NB + 1) doubles
   double (*a)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm);
   double (*v)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm + NB * (NB + 1));
-  __shared__ double dinv_p[kPanel][kPanel];
-  __shared__ int bad;
+  __shared__ double rr[NB], piv[NB];
+  __shared__ unsigned short tri[NB * (NB - 1) / 2];     // (i << 8) | c, c descending
   const int nb = min(NB, n - k0);
   for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
     int r = e / NB, c = e % NB;
     a[r][c] = (r < nb && c < nb) ? A[(long long)(k0 + r) * ld + k0 + c] : (r == c ? 1.0 : 0.0);
     v[r][c] = r == c ? 1.0 : 0.0;
   }
-  double pmin = 0.0, pmax = 0.0;
-  if (threadIdx.x == 0) {
-    bad = 0;
-    pmin = cs->min_piv;
-    pmax = cs->max_piv;
+  // Column c (1 <= c < nb) holds items (c..nb-1, c); columns nb-1, nb-2, ... come first, so
+  // column c starts at T(c) = sum_{c' > c} (nb - c') = (nb - 1 - c)(nb - c) / 2.
+  for (int c = 1 + (int)threadIdx.x; c < nb; c += blockDim.x) {
+    const int base = (nb - 1 - c) * (nb - c) / 2;
+    for (int i = c; i < nb; i++) tri[base + (i - c)] = (unsigned short)((i << 8) | c);
   }
+  double pmin = cs->min_piv, pmax = cs->max_piv;
   __syncthreads();
-  for (int j0 = 0; j0 < nb; j0 += kPanel) {
-    const int w = min(kPanel, nb - j0);
-    // ---- (a) the panel's diagonal block and its inverse, by one thread
+  auto pivot = [&](int j, double d) {
+    piv[j] = d;
+    rr[j] = d > 0.0 ? rsqrt_fast(d) : 1.0;
+  };
+  if (threadIdx.x == 0) pivot(0, a[0][0]);
+  __syncthreads();
+  bool bad = false;
+  // d > thr (thr >= 0) as an integer comparison of the bit patterns, which order like the
+  // values for non-negative doubles (a negative d compares below): the FP64 pipe is the
+  // scarce resource here, and every thread takes this test every step.
+  const long long thr_bits = __double_as_longlong(thr > 0.0 ? thr : 0.0);
+  for (int j = 0; j < nb; j++) {
+    const double d = piv[j];                             // the same value in every thread
+    const long long db = __double_as_longlong(d);
+    if (!(db > thr_bits && ((db >> 52) & 0x7ff) != 0x7ff)) {
+      if (threadIdx.x == 0) {
+        cs->flag = 1;
+        cs->info = k0 + j + 1;
+      }
+      bad = true;
+      break;
+    }
     if (threadIdx.x == 0) {
-      // Fully unrolled over kPanel (registers only); rows/columns >= w are an identity pad.
-      double L[kPanel][kPanel], D[kPanel][kPanel], r[kPanel];
-#pragma unroll
-      for (int i = 0; i < kPanel; i++)
-#pragma unroll
-        for (int c = 0; c < kPanel; c++)
-          L[i][c] = (i < w && c <= i) ? a[j0 + i][j0 + c] : (i == c ? 1.0 : 0.0);
-      bool ok = true;
-#pragma unroll
-      for (int q = 0; q < kPanel; q++) {
-        const double d = L[q][q];
-        if (ok && q < w && !(d > thr)) {
-          ok = false;
-          bad = 1;
-          cs->flag = 1;
-          cs->info = k0 + j0 + q + 1;
-        }
-        if (q < w) {
-          pmin = fmin(pmin, d);
-          pmax = fmax(pmax, d);
-        }
-        r[q] = ok ? rsqrt_fast(d) : 1.0;
-        L[q][q] = d * r[q];
-#pragma unroll
-        for (int i = q + 1; i < kPanel; i++) L[i][q] *= r[q];
-#pragma unroll
-        for (int i = q + 1; i < kPanel; i++)
-#pragma unroll
-          for (int c = q + 1; c <= i; c++) L[i][c] = __fma_rn(-L[i][q], L[c][q], L[i][c]);
-      }
-      if (ok) {
-        // D = L^{-1}: D_qq = 1 / L_qq = r_q, D_iq = -r_i sum_{p=q}^{i-1} L_ip D_pq.
-#pragma unroll
-        for (int q = 0; q < kPanel; q++) {
-#pragma unroll
-          for (int i = 0; i < kPanel; i++) D[i][q] = 0.0;
-          D[q][q] = r[q];
-#pragma unroll
-          for (int i = q + 1; i < kPanel; i++) {
-            double t = 0.0;
-#pragma unroll
-            for (int p = q; p < i; p++) t = __fma_rn(L[i][p], D[p][q], t);
-            D[i][q] = -t * r[i];
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < kPanel; i++)
-#pragma unroll
-          for (int c = 0; c < kPanel; c++) {
-            if (i < w && c <= i) a[j0 + i][j0 + c] = L[i][c];
-            dinv_p[i][c] = (i < w && c <= i) ? D[i][c] : 0.0;
-          }
-      }
+      pmin = fmin(pmin, d);
+      pmax = fmax(pmax, d);
     }
-    __syncthreads();
-    if (bad) break;
-    // ---- (b) panel rows below (thread per row) and the panel rows of V (thread per column)
-    for (int t = threadIdx.x; t < (nb - j0 - w) + (j0 + w); t += blockDim.x) {
-      if (t < nb - j0 - w) {
-        const int i = j0 + w + t;
-        double x[kPanel], y[kPanel];
-#pragma unroll
-        for (int p = 0; p < kPanel; p++) x[p] = p < w ? a[i][j0 + p] : 0.0;
-#pragma unroll
-        for (int q = 0; q < kPanel; q++) {
-          double s2 = 0.0;
-#pragma unroll
-          for (int p = 0; p <= q; p++) s2 = __fma_rn(x[p], dinv_p[q][p], s2);
-          y[q] = s2;
-        }
-#pragma unroll
-        for (int q = 0; q < kPanel; q++)
-          if (q < w) a[i][j0 + q] = y[q];
-      } else {
-        const int c = t - (nb - j0 - w);                    // column of V, c < j0 + w
-        double x[kPanel], y[kPanel];
-#pragma unroll
-        for (int p = 0; p < kPanel; p++) x[p] = p < w ? v[j0 + p][c] : 0.0;
-#pragma unroll
-        for (int q = 0; q < kPanel; q++) {
-          double s2 = 0.0;
-#pragma unroll
-          for (int p = 0; p <= q; p++) s2 = __fma_rn(dinv_p[q][p], x[p], s2);
-          y[q] = s2;
-        }
-#pragma unroll
-        for (int q = 0; q < kPanel; q++)
-          if (q < w) v[j0 + q][c] = y[q];
-      }
-    }
-    __syncthreads();
-    // ---- (c) rank-w update of rows i >= j0 + w: a[i][c] for j0 + w <= c <= i and
-    //          v[i][c] for c < j0 + w, i.e. columns 0..i of each row.
+    const double r = rr[j];
+    // (1) scale column j of L (rows j..nb-1) and row j of V (columns 0..j)
     {
-      const int r0 = j0 + w;
-      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-      for (int i = r0 + ty; i < nb; i += 16) {
-        double l[kPanel];
-#pragma unroll
-        for (int p = 0; p < kPanel; p++) l[p] = p < w ? a[i][j0 + p] : 0.0;
-        for (int c = tx; c <= i; c += 16) {
-          double acc;
-          if (c < r0) {
-            acc = v[i][c];
-#pragma unroll
-            for (int p = 0; p < kPanel; p++)
-              if (p < w) acc = __fma_rn(-l[p], v[j0 + p][c], acc);
-            v[i][c] = acc;
-          } else {
-            acc = a[i][c];
-#pragma unroll
-            for (int p = 0; p < kPanel; p++)
-              if (p < w) acc = __fma_rn(-l[p], a[c][j0 + p], acc);
-            a[i][c] = acc;
-          }
-        }
+      const int t = threadIdx.x, na = nb - j;
+      if (t < na) a[j + t][j] *= r;
+      else if (t - na <= j) v[j][t - na] *= r;
+    }
+    __syncthreads();
+    // (2) the trailing triangle (T(j) items) and the rows of V below j ((nb-1-j)(j+1) items)
+    const int ntri = (nb - 1 - j) * (nb - j) / 2;
+    const int nrect = (nb - 1 - j) * (j + 1);
+    const int pe = ntri - (nb - 1 - j);                  // item (j+1, j+1): the next pivot
+    for (int e = threadIdx.x; e < ntri + nrect; e += blockDim.x) {
+      if (e < ntri) {
+        const unsigned code = tri[e];
+        const int i = code >> 8, c = code & 255;
+        const double nv = __fma_rn(-a[i][j], a[c][j], a[i][c]);
+        a[i][c] = nv;
+        if (e == pe) pivot(j + 1, nv);
+      } else {
+        const int q = e - ntri;
+        const int i = j + 1 + q / (j + 1), c = q % (j + 1);
+        v[i][c] = __fma_rn(-a[i][j], v[j][c], v[i][c]);
       }
     }
     __syncthreads();

@@ -526,33 +526,63 @@ __global__ void __launch_bounds__(kAssignThreads) km_assign32p(KmBufs b)
   }
   __syncthreads();   // every thread reads every candidate written above
   int nc = ncand;
-  if (!valid) return;
-  float m1 = INFINITY, m2 = INFINITY;
-  int k1 = 0;
-  if (nc <= kPruneMax) {
-    for (int j = 0; j < nc; j++) {
-      float dx = ccx[j] - g[0], dy = ccy[j] - g[1], dz = ccz[j] - g[2];
-      float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
-      if (d2 < m1) { m2 = m1; m1 = d2; k1 = cand[j]; }
-      else if (d2 < m2) { m2 = d2; }
+  int* lab = b.labels + (size_t)(it & 1) * b.ng;
+  bool amb = false;
+  if (valid) {
+    float m1 = INFINITY, m2 = INFINITY;
+    int k1 = 0;
+    if (nc <= kPruneMax) {
+      for (int j = 0; j < nc; j++) {
+        float dx = ccx[j] - g[0], dy = ccy[j] - g[1], dz = ccz[j] - g[2];
+        float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+        if (d2 < m1) { m2 = m1; m1 = d2; k1 = cand[j]; }
+        else if (d2 < m2) { m2 = d2; }
+      }
+    } else {
+      for (int k = 0; k < b.nmu; k++) {
+        float dx = cx[k] - g[0], dy = cy[k] - g[1], dz = cz[k] - g[2];
+        float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+        if (d2 < m1) { m2 = m1; m1 = d2; k1 = k; }
+        else if (d2 < m2) { m2 = d2; }
+      }
     }
-  } else {
-    for (int k = 0; k < b.nmu; k++) {
-      float dx = cx[k] - g[0], dy = cy[k] - g[1], dz = cz[k] - g[2];
-      float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
-      if (d2 < m1) { m2 = m1; m1 = d2; k1 = k; }
-      else if (d2 < m2) { m2 = d2; }
-    }
+    const double uu = 5.9604644775390625e-08;
+    double a = st->abound;
+    double e1 = 2.0 * uu * (2.0 * sqrt((double)m1) * a + 5.0 * (double)m1);
+    double e2 = 2.0 * uu * (2.0 * sqrt((double)m2) * a + 5.0 * (double)m2);
+    if ((double)m2 - (double)m1 > e1 + e2 + 1e-300) lab[i] = k1;
+    else amb = true;
   }
-  const double uu = 5.9604644775390625e-08;
-  double a = st->abound;
-  double e1 = 2.0 * uu * (2.0 * sqrt((double)m1) * a + 5.0 * (double)m1);
-  double e2 = 2.0 * uu * (2.0 * sqrt((double)m2) * a + 5.0 * (double)m2);
-  if ((double)m2 - (double)m1 > e1 + e2 + 1e-300) {
-    b.labels[(size_t)(it & 1) * b.ng + i] = k1;
-  } else {
-    int slot = atomicAdd(&st->recheck_n, 1);
-    b.recheck[slot] = (int)i;
+  // FP64 rescue of the near ties, at once and by the whole warp, one point at a time: the
+  // exact first argmin of the sqrt distances (as km_recheck) over the tile's candidates in
+  // ascending index order, which hold the FP64 nearest centroid.
+  unsigned todo = __ballot_sync(0xffffffffu, amb);
+  if (todo && lane == 0) atomicAdd(&st->recheck_n, __popc(todo));
+  const double* px = b.cen + (size_t)(it & 1) * 3 * b.nmu;
+  const double* py = px + b.nmu;
+  const double* pz = py + b.nmu;
+  while (todo) {
+    const int p = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const long long ip = __shfl_sync(0xffffffffu, i, p);
+    const double gx = b.gx[ip], gy = b.gy[ip], gz = b.gz[ip];
+    ArgMin am;
+    am.init();
+    if (nc <= kPruneMax) {
+      for (int j = lane; j < nc; j += 32) {
+        const int k = cand[j];
+        am.push(d2_exact(px[k], py[k], pz[k], gx, gy, gz), k);
+      }
+    } else {
+      for (int k = lane; k < b.nmu; k += 32) am.push(d2_exact(px[k], py[k], pz[k], gx, gy, gz), k);
+    }
+    for (int off = 16; off; off >>= 1) {
+      double s2 = __shfl_xor_sync(0xffffffffu, am.s, off);
+      double m2 = __shfl_xor_sync(0xffffffffu, am.m, off);
+      int k2 = __shfl_xor_sync(0xffffffffu, am.k, off);
+      am.merge(s2, m2, k2);
+    }
+    if (lane == 0) lab[ip] = am.k;
   }
 }
 
@@ -1500,8 +1530,10 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
         else km_assign32<<<nassign, kAssignThreads, 0, s>>>(b);
       }
       THC_LAUNCHED(c, "km_assign32");
-      km_recheck<<<152 * 4, 256, 0, s>>>(b);
-      THC_LAUNCHED(c, "km_recheck");
+      if (!prune) {   // the pruned kernel rescues its near ties itself
+        km_recheck<<<152 * 4, 256, 0, s>>>(b);
+        THC_LAUNCHED(c, "km_recheck");
+      }
     } else {
       {
         ProfScope p(prof ? c : nullptr, "km_assign");
