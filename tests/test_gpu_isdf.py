@@ -104,6 +104,22 @@ def test_isdf_rank_deficient_c1(request, prec):
     assert inv < 1e-4
 
 
+def test_isdf_mixed_odd_nmu_split_k(gpu_ctx_mixed):
+    """An odd N_mu (15 orbitals x 5 = 75) with the Coulomb product split over K: the split
+    partials of odd z start at odd offsets (paired stores must check the address)."""
+    from thcpp_gb300 import synth
+    lat, atoms = synth.diamond_supercell(1)
+    s = synth.make_system("odd", lat, atoms, (16, 16, 16), 15, 5, 1234, 77)
+    assert s.nmu % 2 == 1
+    idx = oracle.kmeans_system(s).idx
+    r = gpu_ctx_mixed.isdf(s.phi, idx, s.mesh, s.coulG)
+    assert r["status"] == 0
+    ref = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG)
+    err = _rel(_cplx(r["M"]), ref["M"])
+    print(f"odd N_mu: mixed ||dM||/||M|| = {err:.3e}")
+    assert err < 1e-6
+
+
 def test_isdf_mixed_fft64_option(lib):
     """zeta in FP64 through a D2Z FFT (the fft64 option) against the oracle on C2, and the
     slice-depth knob of the Coulomb product: fewer slices must not be more accurate."""

@@ -257,6 +257,12 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
     h->c.profile = value != 0.0;
     return THC_OK;
   }
+  if (!strcmp(key, "tc_hi")) {   // 1, 2, 4, ... 32 sixteen-k steps per drain
+    const int v = (int)value;
+    if (v < 1 || v > 32 || (v & (v - 1))) return THC_ERR_ARG;
+    h->c.tc_hi_stages = v;
+    return THC_OK;
+  }
   if (!strcmp(key, "tc_bk")) {
     if (value != 16.0 && value != 32.0) return THC_ERR_ARG;
     h->c.tc_bk = (int)value;

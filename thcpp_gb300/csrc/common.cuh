@@ -91,6 +91,7 @@ struct Ctx {
   // faster: 0.90 s against 1.00 s for the zeta product at N_g 1.26e6, N_mu 5184) or 16
   // (4 stages of half the size).
   int tc_bk = 32;
+  int tc_hi_stages = 8; // drain period of the level >= 3 accumulator, in 16-k MMA steps
   int fft64 = 0;        // mixed path: zeta in FP64 and a D2Z FFT (else FP32 and R2C)
   // Instantiated k-means iteration graphs, most recently used last, keyed by every kernel
   // argument they bake in.

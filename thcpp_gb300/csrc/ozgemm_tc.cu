@@ -13,9 +13,9 @@
 // TMEM (512 columns) holds four 128 x 128 FP32 accumulators: one each for the pair levels
 // 0, 1 and 2, which carry the bulk of the value and are drained every 512 k while each of
 // their sums is still exact (an integer multiple of 2^{-7l} below 2^{24-7l}), and one for
-// all levels >= 3 together, which weigh <= 2^-21 of the total and accumulate in FP32 over
-// the whole K (rounding <= 2^-45 of the total).  Within a stage the MMA thread issues the
-// level >= 3 pairs first, which covers most of the drain.
+// all levels >= 3 together, which weigh <= 2^-21 of the total and are inexact FP32 sums
+// (drained every 128 k, so that no running sum grows over the whole K).  Around a drain the
+// MMA thread issues the pairs of the other accumulators first, which covers it.
 // Every mbarrier wait is bounded; on timeout the kernel records an error, stops issuing,
 // and every role falls through to the teardown, which frees TMEM.
 #include <cuda.h>
@@ -211,6 +211,7 @@ struct TcArgs {
   long long M, N, K;
   long long a_rows_pad, b_rows_pad;   // rows of one slice in the 2-D tensor maps
   long long a_tile_rows, b_tile_rows; // tiled operands: map rows per 32-wide k tile; 0 = plain
+  int hi_stages;                      // stages between drains of the level >= 3 accumulator
   const int* ea;
   const int* eb;
   void* C;
@@ -270,8 +271,10 @@ __global__ void __launch_bounds__(TTHREADS, 1)
   uint64_t* full = (uint64_t*)(smem + Cfg::BUF_BYTES);
   uint64_t* empty = full + NST;
   uint64_t* acc_full = empty + NST;
-  uint64_t* acc_empty = acc_full + 1;
-  uint32_t* tmem_slot = (uint32_t*)(acc_empty + 1);
+  uint64_t* acc_empty = acc_full + 1;      // exact levels drained
+  uint64_t* acc_empty_hi = acc_empty + 1;  // the level >= 3 accumulator drained
+  uint64_t* acc_full_hi = acc_empty_hi + 1;  // the level >= 3 accumulator ready
+  uint32_t* tmem_slot = (uint32_t*)(acc_full_hi + 1);
   volatile int* abort = (volatile int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -283,6 +286,11 @@ __global__ void __launch_bounds__(TTHREADS, 1)
   }
   const int nstages = kend > kbeg ? (int)((kend - kbeg + BK - 1) / BK) : 0;
   const int nchunks = (nstages + Cfg::CHUNK_STAGES - 1) / Cfg::CHUNK_STAGES;
+  const int HS = g.hi_stages;                       // divides CHUNK_STAGES
+  // The level >= 3 periods are offset by half a period from the exact chunks, so the two
+  // accumulators never need draining at the same stage (each drain is covered by the other
+  // accumulator's MMAs).
+  const int HOFF = HS / 2;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; s++) {
@@ -291,6 +299,8 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     }
     mbar_init(acc_full, 1);
     mbar_init(acc_empty, TEPI_WARPS);
+    mbar_init(acc_empty_hi, TEPI_WARPS);
+    mbar_init(acc_full_hi, 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
@@ -331,7 +341,6 @@ __global__ void __launch_bounds__(TTHREADS, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      bool started_hi = false;
       for (int it = 0; it < nstages && !*abort; it++) {
         int s = it % NST;
         uint32_t ph = (uint32_t)((it / NST) & 1);
@@ -342,42 +351,73 @@ __global__ void __launch_bounds__(TTHREADS, 1)
         asm volatile("tcgen05.fence::after_thread_sync;\n");
         unsigned char* st = smem + s * STAGE_BYTES;
         uint32_t a0 = su32(st), b0 = su32(st + LV * A_BYTES);
-        // Levels >= 3, all into the fourth accumulator, over the whole K.
+        const int hp = (it + HOFF) / HS;
+        const bool hp_first = it == 0 || ((it + HOFF) % HS) == 0;
+        const bool hp_last = ((it + HOFF + 1) % HS) == 0 || it + 1 == nstages;
+        // Levels >= 3 into the fourth accumulator, which the epilogue drains every HS
+        // stages: the tensor cores' FP32 accumulation loses low bits of each addend relative
+        // to the running sum, and a sum over the whole K (~2000 instructions at N_mu 2048)
+        // cost 8x in the final error; a drain every 128 k brings it to within 15 % of an
+        // FP64 fold per 256 k.
+        auto issue_hi = [&]() {
+          bool first = hp_first;
 #pragma unroll
-        for (int l = 3; l < LV; l++) {
+          for (int l = 3; l < LV; l++) {
 #pragma unroll
-          for (int i = 0; i <= l; i++) {
-            int j = l - i;
+            for (int i = 0; i <= l; i++) {
+              int j = l - i;
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; kk++) {
-              uint64_t ad = sdesc<BK>(a0 + i * A_BYTES + kk * 32);
-              uint64_t bd = sdesc<BK>(b0 + j * B_BYTES + kk * 32);
-              umma(tmem + 3 * TBN, ad, bd, started_hi ? 1u : 0u);
-              started_hi = true;
+              for (int kk = 0; kk < BK / 16; kk++) {
+                uint64_t ad = sdesc<BK>(a0 + i * A_BYTES + kk * 32);
+                uint64_t bd = sdesc<BK>(b0 + j * B_BYTES + kk * 32);
+                umma(tmem + 3 * TBN, ad, bd, first ? 0u : 1u);
+                first = false;
+              }
             }
           }
-        }
-        // Levels 0-2: exact per chunk; wait until the previous chunk has been drained.
-        if (chunk_first && chunk > 0) {
+        };
+        // Levels 0-2: exact per chunk.
+        auto issue_ex = [&]() {
+#pragma unroll
+          for (int l = 0; l < Cfg::NEXACT; l++) {
+            bool first = chunk_first;
+#pragma unroll
+            for (int i = 0; i <= l; i++) {
+              int j = l - i;
+#pragma unroll
+              for (int kk = 0; kk < BK / 16; kk++) {
+                uint64_t ad = sdesc<BK>(a0 + i * A_BYTES + kk * 32);
+                uint64_t bd = sdesc<BK>(b0 + j * B_BYTES + kk * 32);
+                umma(tmem + l * TBN, ad, bd, first ? 0u : 1u);
+                first = false;
+              }
+            }
+          }
+        };
+        const bool wait_hi = LV > 3 && hp_first && hp > 0;
+        const bool wait_ex = chunk_first && chunk > 0;
+        if (wait_ex) {
+          // Both drains pending: the epilogue empties the level >= 3 accumulator first, so
+          // those pairs go first and cover the drain of the exact levels.
+          if (wait_hi) {
+            if (!mbar_wait(acc_empty_hi, (uint32_t)((hp - 1) & 1), abort)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+          }
+          issue_hi();
           if (!mbar_wait(acc_empty, (uint32_t)((chunk - 1) & 1), abort)) break;
           asm volatile("tcgen05.fence::after_thread_sync;\n");
-        }
-#pragma unroll
-        for (int l = 0; l < Cfg::NEXACT; l++) {
-          bool first = chunk_first;
-#pragma unroll
-          for (int i = 0; i <= l; i++) {
-            int j = l - i;
-#pragma unroll
-            for (int kk = 0; kk < BK / 16; kk++) {
-              uint64_t ad = sdesc<BK>(a0 + i * A_BYTES + kk * 32);
-              uint64_t bd = sdesc<BK>(b0 + j * B_BYTES + kk * 32);
-              umma(tmem + l * TBN, ad, bd, first ? 0u : 1u);
-              first = false;
-            }
+          issue_ex();
+        } else {
+          // At most the level >= 3 drain pending: the exact pairs cover it.
+          issue_ex();
+          if (wait_hi) {
+            if (!mbar_wait(acc_empty_hi, (uint32_t)((hp - 1) & 1), abort)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
           }
+          issue_hi();
         }
         umma_commit(&empty[s]);
+        if (LV > 3 && hp_last) umma_commit(acc_full_hi);
         if (chunk_last) umma_commit(acc_full);
       }
     }
@@ -404,7 +444,27 @@ __global__ void __launch_bounds__(TTHREADS, 1)
 #pragma unroll
     for (int q = 0; q < 64; q++) { ah[q] = 0.f; al[q] = 0.f; }
     bool ok = true;
+    const int nhp = nstages > 0 ? (nstages - 1 + HOFF) / HS + 1 : 0;
+    int hpd = 0;                                     // level >= 3 periods drained
     for (int ch = 0; ch < nchunks; ch++) {
+      // The level >= 3 periods of this chunk first (the MMA waits for each).
+      const int hp_end = min(nhp, (ch + 1) * (Cfg::CHUNK_STAGES / HS));
+      for (; LV > 3 && hpd < hp_end; hpd++) {
+        if (!mbar_wait(acc_full_hi, (uint32_t)(hpd & 1), abort)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+          float v[8];
+          tmem_ld8(tmem + lane_base + 3 * TBN + (uint32_t)(col0 + 8 * b), v);
+          // |v| <= 2^-21 |ah|: the low word takes it with an FP32 rounding of ~2^-45 |ah|.
+#pragma unroll
+          for (int q = 0; q < 8; q++) al[8 * b + q] = __fadd_rn(al[8 * b + q], v[q]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acc_empty_hi);
+      }
+      if (!ok) break;
       if (!mbar_wait(acc_full, (uint32_t)(ch & 1), abort)) { ok = false; break; }
       asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
@@ -434,14 +494,20 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(acc_empty);
     }
-    if (ok && LV > 3 && nstages > 0) {
+    // The level >= 3 period that ends with the last stage.
+    for (; ok && LV > 3 && hpd < nhp; hpd++) {
+      if (!mbar_wait(acc_full_hi, (uint32_t)(hpd & 1), abort)) { ok = false; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
-      for (int b = 0; b < 4; b++) {
-        float v[16];
-        tmem_ld16(tmem + lane_base + 3 * TBN + (uint32_t)(col0 + 16 * b), v);
+      for (int b = 0; b < 8; b++) {
+        float v[8];
+        tmem_ld8(tmem + lane_base + 3 * TBN + (uint32_t)(col0 + 8 * b), v);
 #pragma unroll
-        for (int q = 0; q < 16; q++) al[16 * b + q] = __fadd_rn(al[16 * b + q], v[q]);
+        for (int q = 0; q < 8; q++) al[8 * b + q] = __fadd_rn(al[8 * b + q], v[q]);
       }
+      asm volatile("tcgen05.fence::before_thread_sync;\n");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_empty_hi);
     }
     if (ok && !*abort) {
       // The warp's 32 x 64 results go through shared memory (the stage buffers are free:
@@ -505,7 +571,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
         if (f32) {
           const float a = stg32[r * 64 + (c0 ^ r)], bb = stg32[r * 64 + ((c0 + 1) ^ r)];
           float* dst = (float*)g.C + off;
-          if (v0 && v1 && !(off & 1)) *(float2*)dst = make_float2(a, bb);
+          if (v0 && v1 && !((uintptr_t)dst & 7)) *(float2*)dst = make_float2(a, bb);
           else {
             if (v0) dst[0] = a;
             if (v1) dst[1] = bb;
@@ -515,7 +581,9 @@ __global__ void __launch_bounds__(TTHREADS, 1)
           const double bb = stg64[r * 64 + ((c0 + 1) ^ (r & 15))];
           double* dst = split ? g.part + (long long)blockIdx.z * g.M * g.N + off
                               : (double*)g.C + off;
-          if (v0 && v1 && !(off & 1)) *(double2*)dst = make_double2(a, bb);
+          // Paired stores only at 16-byte aligned addresses (the partials of split z start at
+          // z M N, odd for odd M N).
+          if (v0 && v1 && !((uintptr_t)dst & 15)) *(double2*)dst = make_double2(a, bb);
           else {
             if (v0) dst[0] = a;
             if (v1) dst[1] = bb;
@@ -591,6 +659,7 @@ int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
   t.a_rows_pad = a_rows; t.b_rows_pad = b_rows;
   t.a_tile_rows = at ? g.a.kt_stride / 32 : 0;
   t.b_tile_rows = bt ? g.b.kt_stride / 32 : 0;
+  t.hi_stages = std::max(1, std::min(Cfg::CHUNK_STAGES, c->tc_hi_stages / (BK / 16)));
   t.ea = g.a.e; t.eb = g.b.e; t.C = g.C; t.ldc = g.ldc;
   t.epilogue = g.epilogue; t.lower_only = g.lower_only; t.error = err_flag;
   t.ksplit = std::max(1, g.ksplit); t.part = g.part;
