@@ -105,11 +105,12 @@ def test_isdf_rank_deficient_c1(request, prec):
 
 
 def test_isdf_mixed_odd_nmu_split_k(gpu_ctx_mixed):
-    """An odd N_mu (15 orbitals x 5 = 75) with the Coulomb product split over K: the split
-    partials of odd z start at odd offsets (paired stores must check the address)."""
+    """An odd N_mu (21 orbitals x 3 = 63, cond(C) ~ 1e5) with the Coulomb product split
+    over K (9 ways): the partials of odd splits start at odd offsets, so paired stores must
+    check the address."""
     from thcpp_gb300 import synth
     lat, atoms = synth.diamond_supercell(1)
-    s = synth.make_system("odd", lat, atoms, (16, 16, 16), 15, 5, 1234, 77)
+    s = synth.make_system("odd", lat, atoms, (16, 16, 16), 21, 3, 1234, 77)
     assert s.nmu % 2 == 1
     idx = oracle.kmeans_system(s).idx
     r = gpu_ctx_mixed.isdf(s.phi, idx, s.mesh, s.coulG)
