@@ -1203,61 +1203,68 @@ __global__ void __launch_bounds__(1024) km_normdiff_exact(KmBufs b)
 }
 
 // Bounding boxes of the 256-point tiles of the binned order (for the pruned map_to_grid).
-__global__ void km_tile_boxes(KmBufs b, double* box)
+// Bounding box of each 256-point tile of the binned order, from the FP32 coordinates.
+__global__ void km_tile_boxes(KmBufs b, float* box)
 {
-  __shared__ double red[6][8];
+  __shared__ float red[6][8];
   long long t = blockIdx.x * 256LL + threadIdx.x;
   bool valid = t < b.ng;
   long long i = valid ? b.perm[t] : 0;
-  double g[3] = {valid ? b.gx[i] : 0.0, valid ? b.gy[i] : 0.0, valid ? b.gz[i] : 0.0};
+  float g[3] = {valid ? b.fx[i] : 0.f, valid ? b.fy[i] : 0.f, valid ? b.fz[i] : 0.f};
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int d = 0; d < 3; d++) {
-    double mn = valid ? g[d] : CUDART_INF, mx = valid ? g[d] : -CUDART_INF;
+    float mn = valid ? g[d] : INFINITY, mx = valid ? g[d] : -INFINITY;
     for (int off = 16; off; off >>= 1) {
-      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, off));
-      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, off));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
     }
     if (lane == 0) { red[d][wid] = mn; red[3 + d][wid] = mx; }
   }
   __syncthreads();
   if (threadIdx.x < 6) {
     int d = threadIdx.x;
-    double v = red[d][0];
-    for (int w = 1; w < 8; w++) v = d < 3 ? fmin(v, red[d][w]) : fmax(v, red[d][w]);
+    float v = red[d][0];
+    for (int w = 1; w < 8; w++) v = d < 3 ? fminf(v, red[d][w]) : fmaxf(v, red[d][w]);
     box[(long long)blockIdx.x * 6 + d] = v;
   }
 }
 
-// map_to_grid with exact pruning: one warp per centroid.  U = min over tiles of the largest
-// squared distance from the centroid to the tile box bounds the nearest squared distance;
-// only tiles whose smallest squared distance is <= U (1 + 1e-9) are scanned.  Tiles are not
-// in grid-index order, so candidates merge on (sqrt distance, grid index), which keeps the
-// reference's first-index rule (classify with the roles swapped, src/kmeans.cpp:146-150).
-__global__ void km_map_pruned(KmBufs b, const double* __restrict__ box, int ntiles, int* idx)
+// map_to_grid with exact pruning: one warp per centroid (two per block, so that every SM
+// takes part).  U = min over tiles of the largest squared distance from the centroid to the
+// tile box bounds the nearest squared distance; only tiles whose smallest squared distance
+// is <= U (1 + 1e-4) + slack32 are scanned.  The bounds are FP32 (the FP64 pipe runs two
+// lanes per clock here); the margins are those of the pruned FP32 assign, far above the FP32
+// rounding of the boxes and distances, so the FP64 nearest point and every sqrt tie survive.
+// Tiles are not in grid-index order, so candidates merge on (sqrt distance, grid index),
+// which keeps the reference's first-index rule (classify with the roles swapped,
+// src/kmeans.cpp:146-150).
+constexpr int kMapThreads = 64;
+__global__ void __launch_bounds__(kMapThreads) km_map_pruned(KmBufs b, const float* __restrict__ box,
+                                                             int ntiles, int* idx)
 {
   const double* cen = b.cen + (size_t)b.st->final_buf * 3 * b.nmu;
   int lane = threadIdx.x & 31;
   long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   if (k >= b.nmu) return;
   double c3[3] = {cen[k], cen[b.nmu + k], cen[2 * b.nmu + k]};
-  double u = CUDART_INF;
+  const float* cf = b.cen32 + (size_t)b.st->final_buf * 3 * b.nmu;
+  const float f3[3] = {cf[k], cf[b.nmu + k], cf[2 * b.nmu + k]};
+  float u = INFINITY;
   for (int t = lane; t < ntiles; t += 32) {
-    double ub = 0.0;
+    float ub = 0.f;
     for (int d = 0; d < 3; d++) {
-      double a = c3[d] - box[t * 6 + d], e = c3[d] - box[t * 6 + 3 + d];
-      ub += fmax(a * a, e * e);
+      float a = f3[d] - box[t * 6 + d], e = f3[d] - box[t * 6 + 3 + d];
+      ub += fmaxf(a * a, e * e);
     }
-    u = fmin(u, ub);
+    u = fminf(u, ub);
   }
-  for (int off = 16; off; off >>= 1) u = fmin(u, __shfl_xor_sync(0xffffffffu, u, off));
-  double cut = u * (1.0 + 1e-9);
+  for (int off = 16; off; off >>= 1) u = fminf(u, __shfl_xor_sync(0xffffffffu, u, off));
+  const float cut = u * (1.0f + 1e-4f) + (float)b.st->slack32;
   // The candidate tiles' points are scanned twice: first in FP32 for the smallest squared
   // distance m, then in FP64 only for points whose FP32 squared distance is within
   // m (1 + 1e-4) + slack32 -- a margin far above the FP32 rounding of the distances (the
   // same one the pruned assign uses) -- so the FP64 pipe, which GB300 runs at two lanes
   // per clock, sees a handful of points per centroid.
-  const float* cf = b.cen32 + (size_t)b.st->final_buf * 3 * b.nmu;
-  const float f3[3] = {cf[k], cf[b.nmu + k], cf[2 * b.nmu + k]};
   float m32 = INFINITY;
   for (int pass = 0; pass < 2; pass++) {
     const float thr32 = pass ? m32 * (1.0f + 1e-4f) + (float)b.st->slack32 : 0.f;
@@ -1267,9 +1274,9 @@ __global__ void km_map_pruned(KmBufs b, const double* __restrict__ box, int ntil
       int t = t0 + lane;
       bool cand = false;
       if (t < ntiles) {
-        double lb = 0.0;
+        float lb = 0.f;
         for (int d = 0; d < 3; d++) {
-          double v = fmax(0.0, fmax(box[t * 6 + d] - c3[d], c3[d] - box[t * 6 + 3 + d]));
+          float v = fmaxf(0.f, fmaxf(box[t * 6 + d] - f3[d], f3[d] - box[t * 6 + 3 + d]));
           lb += v * v;
         }
         cand = lb <= cut;
@@ -1626,10 +1633,10 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   THC_CUDA(c, cudaMemsetAsync(dups, 0, sizeof(int), s));
   if (prune) {
     int ntiles = (int)cdiv(ng, 256);
-    double* box = part_s;   // 6 doubles per tile fit in the partials buffer
+    float* box = (float*)part_s;   // 6 floats per tile fit in the partials buffer
     km_tile_boxes<<<ntiles, 256, 0, s>>>(b, box);
     THC_LAUNCHED(c, "km_tile_boxes");
-    km_map_pruned<<<(int)cdiv((long long)nmu * 32, 256), 256, 0, s>>>(b, box, ntiles, didx);
+    km_map_pruned<<<(int)cdiv((long long)nmu * 32, kMapThreads), kMapThreads, 0, s>>>(b, box, ntiles, didx);
     THC_LAUNCHED(c, "km_map_pruned");
   } else {
     dim3 mg((unsigned)nch, (unsigned)cdiv(nmu, 256));
