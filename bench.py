@@ -343,6 +343,15 @@ def main():
     M_mixed = d_M.cpu().numpy().copy()
     oz_ms, oz_n = ctx.kernel_time("ozgemm")
     km_ms, km_n = ctx.kernel_time("km_assign")
+    # Device time per system of each stage of the timed steps (CUDA events the library
+    # records around its launches; stages nest: "ozgemm" is the sum of the oz_* products,
+    # "dgemm" includes the FP64 GEMMs inside potrf_inv and chol_inverse).
+    stage_ms = {}
+    for name in ("kmeans", "oz_P", "oz_cinv", "oz_Y", "oz_zeta", "oz_M", "ozgemm", "slice",
+                 "fft", "potrf_inv", "chol_inverse", "dgemm", "oz_split_reduce"):
+        ms_, n_ = ctx.kernel_time(name)
+        if n_:
+            stage_ms[name] = round(ms_ / args.steps, 4)
     ctx.set_option("profile", 0)
 
     paths = set(args.paths.split(","))
@@ -459,6 +468,7 @@ def main():
             "kmeans": {"iterations": kst.iterations, "rechecked_points": int(kst.rechecked),
                        "assign_us_per_iteration": (1e3 * km_ms / km_n) if km_n else None},
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "stage_ms_per_system": stage_ms,
         }
         # Whole-job s/system: ws replicas each factorised one system per step in t_step.
         line["value"] = t_step * 1e-3 / ws

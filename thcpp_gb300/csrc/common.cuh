@@ -21,7 +21,7 @@ namespace thc {
 enum Slot : int {
   // k-means
   WS_KM_GRID = 0,   // 3 x ng doubles (SoA)
-  WS_KM_GRID32,     // 3 x ng floats (SoA)
+  WS_KM_GRID32,     // 3 x ng floats (SoA) in point order, 3 x ng in the binned order
   WS_KM_RHO,
   WS_KM_CENT,       // 2 buffers x 3 x nmu doubles
   WS_KM_CENT32,     // 2 buffers x 3 x nmu floats

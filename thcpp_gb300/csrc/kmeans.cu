@@ -113,6 +113,7 @@ struct KmBufs {
   int* pbin;       // [ng] bin of each point
   int* bcount;     // [nbins_max] counts, then offsets, then cursors
   int nbins_max;
+  float* pf;       // [3][ng] FP32 coordinates in the binned order (pf[d][t] of point perm[t])
   // Window-parallel exact sums (nwin_max == 0: the one-kernel km_sums path).
   const double* tq;   // [4][ng] rho_i, rho_i x_i, rho_i y_i, rho_i z_i in point order
   double* sv;         // [4][ng] the same terms in sorted (cluster, ascending point) order
@@ -325,6 +326,11 @@ __global__ void km_bin_scatter(KmBufs b)
   int bin = b.pbin[i];
   int pos = b.bcount[bin] + atomicAdd(&b.bcount[b.nbins_max + bin], 1);
   b.perm[pos] = (int)i;
+  // The binned order's own copy of the FP32 coordinates: the pruned kernels read them
+  // coalesced instead of through perm (a dependent gather).
+  b.pf[pos] = b.fx[i];
+  b.pf[b.ng + pos] = b.fy[i];
+  b.pf[2 * b.ng + pos] = b.fz[i];
 }
 
 // Ordered block-wide compaction of `flag` over the block's threads: returns this thread's
@@ -470,7 +476,7 @@ __global__ void __launch_bounds__(kAssignThreads) km_assign32p(KmBufs b)
   bool valid = t < b.ng;
   long long i = valid ? b.perm[t] : 0;
   float g[3] = {0, 0, 0};
-  if (valid) { g[0] = b.fx[i]; g[1] = b.fy[i]; g[2] = b.fz[i]; }
+  if (valid) { g[0] = b.pf[t]; g[1] = b.pf[b.ng + t]; g[2] = b.pf[2 * b.ng + t]; }
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   float lo[3], hi[3];
   for (int d = 0; d < 3; d++) {
@@ -1210,7 +1216,8 @@ __global__ void km_tile_boxes(KmBufs b, float* box)
   long long t = blockIdx.x * 256LL + threadIdx.x;
   bool valid = t < b.ng;
   long long i = valid ? b.perm[t] : 0;
-  float g[3] = {valid ? b.fx[i] : 0.f, valid ? b.fy[i] : 0.f, valid ? b.fz[i] : 0.f};
+  float g[3] = {valid ? b.pf[t] : 0.f, valid ? b.pf[b.ng + t] : 0.f,
+                valid ? b.pf[2 * b.ng + t] : 0.f};
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int d = 0; d < 3; d++) {
     float mn = valid ? g[d] : INFINITY, mx = valid ? g[d] : -INFINITY;
@@ -1287,14 +1294,14 @@ __global__ void __launch_bounds__(kMapThreads) km_map_pruned(KmBufs b, const flo
         m &= m - 1;
         long long p0 = (long long)tt * 256, p1 = min((long long)b.ng, p0 + 256);
         for (long long q = p0 + lane; q < p1; q += 32) {
-          int i = b.perm[q];
-          float dx = b.fx[i] - f3[0], dy = b.fy[i] - f3[1], dz = b.fz[i] - f3[2];
+          float dx = b.pf[q] - f3[0], dy = b.pf[b.ng + q] - f3[1], dz = b.pf[2 * b.ng + q] - f3[2];
           float d32 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
           if (!pass) {
             m32 = fminf(m32, d32);
             continue;
           }
           if (d32 > thr32) continue;
+          const int i = b.perm[q];
           double d2 = d2_exact(b.gx[i], b.gy[i], b.gz[i], c3[0], c3[1], c3[2]);
           // Any order: a candidate can win on a smaller sqrt or on an equal sqrt and a
           // smaller index; equal sqrt values come from squared distances within a few ulps.
@@ -1441,7 +1448,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   b.nmu = nmu;
   b.nb = (int)cdiv(ng, kBP);
   double* g64 = (double*)al.get(WS_KM_GRID, sizeof(double) * 4 * ng);
-  float* g32 = (float*)al.get(WS_KM_GRID32, sizeof(float) * 3 * ng);
+  float* g32 = (float*)al.get(WS_KM_GRID32, sizeof(float) * 6 * ng);
   double* cen = (double*)al.get(WS_KM_CENT, sizeof(double) * 6 * nmu);
   float* cen32 = (float*)al.get(WS_KM_CENT32, sizeof(float) * 6 * nmu);
   int* labels = (int*)al.get(WS_KM_LABELS, sizeof(int) * 2 * ng);
@@ -1466,6 +1473,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   int* part_i = (int*)(part_s + (size_t)nmu * nch);
   b.gx = g64; b.gy = g64 + ng; b.gz = g64 + 2 * ng; b.rho = g64 + 3 * ng;
   b.fx = g32; b.fy = g32 + ng; b.fz = g32 + 2 * ng;
+  b.pf = g32 + 3 * ng;
   b.cen = cen; b.cen32 = cen32; b.labels = labels; b.hist = hist; b.total = tot;
   b.start = tot + nmu; b.member = member; b.terms = terms; b.recheck = recheck;
   b.log = logb; b.st = st;
