@@ -209,6 +209,8 @@ __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, i
     const int ntri = (nb - 1 - j) * (nb - j) / 2;
     const int nrect = (nb - 1 - j) * (j + 1);
     const int pe = ntri - (nb - 1 - j);                  // item (j+1, j+1): the next pivot
+    const int w = j + 1;                                 // rectangle row length
+    const float rw = 1.0f / (float)w;
     for (int e = threadIdx.x; e < ntri + nrect; e += blockDim.x) {
       if (e < ntri) {
         const unsigned code = tri[e];
@@ -217,8 +219,14 @@ __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, i
         a[i][c] = nv;
         if (e == pe) pivot(j + 1, nv);
       } else {
+        // q = r w + c without an integer division: the FP32 quotient of q < 2^12 is off by
+        // at most one, which the two corrections fix.
         const int q = e - ntri;
-        const int i = j + 1 + q / (j + 1), c = q % (j + 1);
+        int r = (int)((float)q * rw);
+        int c = q - r * w;
+        if (c < 0) { r--; c += w; }
+        if (c >= w) { r++; c -= w; }
+        const int i = j + 1 + r;
         v[i][c] = __fma_rn(-a[i][j], v[j][c], v[i][c]);
       }
     }
