@@ -354,6 +354,24 @@ __device__ __forceinline__ int block_compact(bool flag, int* wsum, int* total)
   return slot;
 }
 
+// A final label of the pruned assign kernels, with the counting sort's histogram entry
+// (cluster k, block of kBP consecutive point indices) and the changed-label count: the
+// separate histogram pass is not needed on this path.
+__device__ __forceinline__ void put_label(const KmBufs& b, int it, long long i, int k,
+                                          unsigned& changed)
+{
+  b.labels[(size_t)(it & 1) * b.ng + i] = k;
+  atomicAdd(&b.hist[(size_t)k * b.nb + i / kBP], 1);
+  if (it > 0 && b.labels[(size_t)((it + 1) & 1) * b.ng + i] != k) changed++;
+}
+
+// Warp sums of the changed-label counts into the state (whole warp).
+__device__ __forceinline__ void flush_changed(KmState* st, unsigned changed)
+{
+  for (int off = 16; off; off >>= 1) changed += __shfl_xor_sync(0xffffffffu, changed, off);
+  if ((threadIdx.x & 31) == 0 && changed) atomicAdd(&st->changed, (unsigned long long)changed);
+}
+
 constexpr int kPruneMax = 2048;   // candidate centroids kept in shared memory per tile
 
 // FP64 assign with exact spatial pruning.  A tile is 256 consecutive points of the
@@ -449,7 +467,9 @@ __global__ void __launch_bounds__(kAssignThreads) km_assign64p(KmBufs b)
   } else if (valid) {
     for (int k = 0; k < b.nmu; k++) am.push(d2_exact(cx[k], cy[k], cz[k], g[0], g[1], g[2]), k);
   }
-  if (valid) b.labels[(size_t)(it & 1) * b.ng + i] = am.k;
+  unsigned changed = 0;
+  if (valid) put_label(b, it, i, am.k, changed);
+  flush_changed(const_cast<KmState*>(st), changed);
 }
 
 // FP32 filter with pruning.  Bounds are computed in FP32 with a relative margin 1e-4 and
@@ -532,8 +552,8 @@ __global__ void __launch_bounds__(kAssignThreads) km_assign32p(KmBufs b)
   }
   __syncthreads();   // every thread reads every candidate written above
   int nc = ncand;
-  int* lab = b.labels + (size_t)(it & 1) * b.ng;
   bool amb = false;
+  unsigned changed = 0;
   if (valid) {
     float m1 = INFINITY, m2 = INFINITY;
     int k1 = 0;
@@ -556,7 +576,7 @@ __global__ void __launch_bounds__(kAssignThreads) km_assign32p(KmBufs b)
     double a = st->abound;
     double e1 = 2.0 * uu * (2.0 * sqrt((double)m1) * a + 5.0 * (double)m1);
     double e2 = 2.0 * uu * (2.0 * sqrt((double)m2) * a + 5.0 * (double)m2);
-    if ((double)m2 - (double)m1 > e1 + e2 + 1e-300) lab[i] = k1;
+    if ((double)m2 - (double)m1 > e1 + e2 + 1e-300) put_label(b, it, i, k1, changed);
     else amb = true;
   }
   // FP64 rescue of the near ties, at once and by the whole warp, one point at a time: the
@@ -588,8 +608,9 @@ __global__ void __launch_bounds__(kAssignThreads) km_assign32p(KmBufs b)
       int k2 = __shfl_xor_sync(0xffffffffu, am.k, off);
       am.merge(s2, m2, k2);
     }
-    if (lane == 0) lab[ip] = am.k;
+    if (lane == 0) put_label(b, it, ip, am.k, changed);
   }
+  flush_changed(st, changed);
 }
 
 // FP64 assign: one thread per grid point, centroids staged through shared memory.
@@ -1538,6 +1559,8 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   // One k-means iteration; every kernel reads the iteration index from device state and
   // returns at once after convergence, so the same launch sequence serves any iteration.
   auto iteration = [&](bool prof) -> int {
+    // The pruned assign kernels count the histogram themselves (put_label).
+    THC_CUDA(c, cudaMemsetAsync(hist, 0, sizeof(int) * (size_t)nmu * b.nb, s));
     if (mixed) {
       {
         ProfScope p(prof ? c : nullptr, "km_assign");
@@ -1557,9 +1580,10 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
       }
       THC_LAUNCHED(c, "km_assign64");
     }
-    THC_CUDA(c, cudaMemsetAsync(hist, 0, sizeof(int) * (size_t)nmu * b.nb, s));
-    km_hist<<<b.nb, 256, hist_smem, s>>>(b);
-    THC_LAUNCHED(c, "km_hist");
+    if (!prune) {
+      km_hist<<<b.nb, 256, hist_smem, s>>>(b);
+      THC_LAUNCHED(c, "km_hist");
+    }
     km_colscan<<<(int)cdiv((long long)nmu * 32, 256), 256, 0, s>>>(b);
     THC_LAUNCHED(c, "km_colscan");
     km_scatter<<<b.nb, 256, hist_smem, s>>>(b);
