@@ -20,6 +20,9 @@
  *                               setup_pseudo_dm/setup_CZt (:59-141), setup_CCt (:163-190),
  *                               least_squares (:416), fft_vectors (:331-404),
  *                               construct_muv (:247-281), dump_thc_data's Cholesky (:283-315)
+ *   thc_isdf_half               IVecs with rotate = true (src/interpolating_vectors.cpp:45-49):
+ *                               setup_CZt_half (:143-161), the IVMG product of
+ *                               construct_muv (:271-273), dump_thc_data's Muv (:317-328)
  *
  * Threading: calls on distinct contexts may run concurrently from different host
  * threads; one context must not be used by two threads at once.
@@ -175,6 +178,24 @@ int thc_kmeans_noalloc(thc_ctx* ctx, const double* grid, const double* rho, long
 int thc_isdf(thc_ctx* ctx, const double* phi, long long ng, int norb, const int* idx, int nmu,
              const int* mesh, const double* coulG, double shift_rel, double* out_orbitals,
              double* out_M, double* out_L, thc_isdf_stats* stats);
+
+/*
+ * Half-rotated ISDF (the reference's `half_rotated` input option).  Same inputs as
+ * thc_isdf plus the occupied orbitals; the pseudo-density products become
+ *   Z = P_occ o P,  P = Phi_mu Phi^T,  P_occ = Phi_occ,mu Phi_occ^T,  C = Z[:, idx],
+ * and M is written without a Cholesky factor.
+ *   phi_occ            ng x nocc doubles, C order: the real part of `aoR_half`
+ *   out_orbitals       norb x nmu x 2: `/Hamiltonian/THC/HalfTransformedFullOrbitals`
+ *   out_occ_orbitals   nocc x nmu x 2: `/Hamiltonian/THC/HalfTransformedOccOrbitals`
+ *   out_M              nmu x nmu x 2: `/Hamiltonian/THC/HalfTransformedMuv`
+ * (each may be NULL).  C is symmetric positive semi-definite (a Schur product of two Gram
+ * matrices), so the Cholesky solve and shift policy of thc_isdf apply unchanged.  Runs in
+ * FP64 in both precisions.
+ */
+int thc_isdf_half(thc_ctx* ctx, const double* phi, long long ng, int norb, const double* phi_occ,
+                  int nocc, const int* idx, int nmu, const int* mesh, const double* coulG,
+                  double shift_rel, double* out_orbitals, double* out_occ_orbitals,
+                  double* out_M, thc_isdf_stats* stats);
 
 /*
  * One system of a batch: the inputs of thc_kmeans (grid, rho, init_idx, max_it, threshold)

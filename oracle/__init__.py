@@ -8,7 +8,8 @@ Contents
 --------
 ``kmeans_oracle.cpp``  single-rank C++ restatement of ``src/kmeans.cpp`` (k-means points),
                        compiled by :func:`build` into ``oracle/_build/libkmeans_oracle.so``.
-``isdf.py``            numpy/scipy restatement of ``src/interpolating_vectors.cpp``:
+``isdf.py``            numpy/scipy restatement of ``src/interpolating_vectors.cpp``
+                       (plain and half-rotated):
                        the literal complex form (zgels QR, C2C FFT, herk, zpotrf) and the
                        regularised real form (Cholesky, R2C) used as the parity target.
 
@@ -125,4 +126,4 @@ def kmeans_system(system, nthreads: int = 0) -> KMeansResult:
 
 
 from .isdf import (isdf_reference, isdf_real, half_spectrum_weights,  # noqa: E402,F401
-                   pair_coulomb_exact, thc_pair_coulomb)
+                   pair_coulomb_exact, thc_pair_coulomb, isdf_half_reference)

@@ -20,6 +20,16 @@ Two formulations of the reference's interpolating-vector + Coulomb path
     This is the formulation the CUDA path implements, so it is the parity target; it
     agrees with ``isdf_reference`` to ~1e-11 whenever C has full numerical rank.
 
+``isdf_half_reference``  the half-rotated form (IVecs with rotate = true), complex128:
+    P = Phi_mu^H Phi and P_occ = Phi_occ,mu^H Phi_occ (setup_pseudo_dm on aoR and aoR_half),
+    Z = P_occ o conj(P) (setup_CZt_half, :143-161), C = Z[:, idx], X = C^{-1} Z by QR,
+    zeta = X^H, forward and backward unnormalised C2C FFTs of every vector (fft_vectors
+    :384-391), scaling by sqrt(v(G)), M = IVMG^T IVG (construct_muv :261-273, 'T','N'),
+    written without a Cholesky factor as HalfTransformedMuv (dump_thc_data :317-328).
+    ``isdf_real(..., phi_occ=...)`` is its real-arithmetic restatement: for real orbitals the
+    backward transform is the conjugate of the forward one, so M_half has the form of M with
+    Z = P_occ o P and C = (P_occ o P)[:, idx].
+
 The pair-Coulomb helpers give an invariant check for rank-deficient C (where M is not
 unique): the THC reconstruction X M X^T of the orbital-pair Coulomb integrals.
 """
@@ -72,17 +82,25 @@ def half_spectrum_weights(coulG: np.ndarray, mesh):
 
 
 def isdf_real(phi: np.ndarray, idx: np.ndarray, mesh, coulG: np.ndarray, shift: float = 0.0,
-              workers=-1, fft_dtype=np.float64):
+              workers=-1, fft_dtype=np.float64, phi_occ=None):
     """Real-arithmetic formulation (the CUDA path's).  Returns dict(M, L, info, zeta, ...).
 
-    ``shift`` is added to the diagonal of C before the Cholesky factorisation.
+    ``shift`` is added to the diagonal of C before the Cholesky factorisation.  With
+    ``phi_occ`` (N_g x N_occ) the half-rotated products Z = P_occ o P, C = Z[:, idx] replace
+    P o P (C stays symmetric positive semi-definite: a Schur product of two Gram matrices).
     """
     phi = np.asarray(phi, np.float64)
     idx = np.asarray(idx)
     ng = phi.shape[0]
     phimu = phi[idx]
-    Zt = (phimu @ phi.T) ** 2                           # (N_mu, N_g)
-    C = (phimu @ phimu.T) ** 2
+    if phi_occ is None:
+        Zt = (phimu @ phi.T) ** 2                       # (N_mu, N_g)
+        C = (phimu @ phimu.T) ** 2
+    else:
+        po = np.asarray(phi_occ, np.float64)
+        pomu = po[idx]
+        Zt = (phimu @ phi.T) * (pomu @ po.T)
+        C = (phimu @ phimu.T) * (pomu @ pomu.T)
     Cs = C + shift * np.eye(C.shape[0])
     Lc = np.linalg.cholesky(Cs)
     Cinv = sla.cho_solve((Lc, True), np.eye(C.shape[0]))
@@ -101,6 +119,26 @@ def isdf_real(phi: np.ndarray, idx: np.ndarray, mesh, coulG: np.ndarray, shift: 
     L, info = lapack.zpotrf(np.tril(M), lower=1, clean=1)
     return dict(M=M, L=np.tril(L), info=int(info), zeta_t=zt, C=C, Cinv=Cinv, zhat=zh,
                 n_anti=int(nz.size))
+
+
+def isdf_half_reference(phi: np.ndarray, phi_occ: np.ndarray, idx: np.ndarray, mesh,
+                        coulG: np.ndarray):
+    """Half-rotated M as the reference forms it (complex128; see the module docstring)."""
+    phi = np.asarray(phi, np.complex128)
+    po = np.asarray(phi_occ, np.complex128)
+    idx = np.asarray(idx)
+    ng = phi.shape[0]
+    P = phi[idx].conj() @ phi.T                          # (N_mu, N_g)
+    Pocc = po[idx].conj() @ po.T
+    Z = Pocc * P.conj()
+    C = Z[:, idx]
+    X = np.linalg.lstsq(C, Z, rcond=None)[0]             # pzgels: least squares by QR
+    zeta = X.conj()                                      # rows are the vectors zeta_mu(r)
+    f = zeta.reshape((-1,) + tuple(mesh))
+    ivg = sfft.fftn(f, axes=(1, 2, 3)).reshape(zeta.shape[0], -1)
+    ivmg = sfft.ifftn(f, axes=(1, 2, 3), norm="forward").reshape(zeta.shape[0], -1)
+    sq = np.sqrt(np.asarray(coulG, np.float64).reshape(-1))
+    return (ivmg * sq) @ (ivg * sq).T
 
 
 def pair_coulomb_exact(phi: np.ndarray, mesh, coulG: np.ndarray, pairs):

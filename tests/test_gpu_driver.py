@@ -46,6 +46,42 @@ def test_driver_tiny(tmp_path, lib, precision):
     assert f.read("/Hamiltonian/Energies").shape == (1,)
 
 
+def test_driver_half_rotated(tmp_path, lib):
+    """half_rotated with thc_half_cfac != thc_cfac (src/main.cpp:53-72): the plain pass
+    (Orbitals, InterpIndx, Luv), new k-means points for the half pass, then
+    HalfTransformed{Full,Occ}{Orbitals,InterpIndx} and HalfTransformedMuv."""
+    build.build_host()
+    s = system("tiny")
+    orb = str(tmp_path / "orbitals.h5")
+    out = str(tmp_path / "thc.h5")
+    synth.write_orbital_file(s, orb, half_rotate=True)
+    inp = tmp_path / "input.json"
+    d = synth.input_json(s, orb, out)
+    d["half_rotated"] = True
+    d["thc_half_cfac"] = 2
+    inp.write_text(json.dumps(d))
+    r = subprocess.run([build.DRIVER, str(inp)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    f = h5.Reader(out)
+    ref = oracle.kmeans_system(s)
+    assert np.array_equal(f.read("/Hamiltonian/THC/InterpIndx"), ref.idx)
+    assert f.read("/Hamiltonian/THC/Luv").shape == (s.nmu, s.nmu, 2)
+    hs = synth.System(**{**s.__dict__, "thc_cfac": 2})
+    href = oracle.kmeans_system(hs)
+    po = s.phi[:, : s.nocc]
+    for part, src in (("Full", s.phi), ("Occ", po)):
+        idx = f.read(f"/Hamiltonian/THC/HalfTransformed{part}InterpIndx")
+        assert np.array_equal(idx, href.idx)
+        o = f.read(f"/Hamiltonian/THC/HalfTransformed{part}Orbitals")
+        assert o.shape == (src.shape[1], hs.nmu, 2)
+        assert np.array_equal(o[..., 0], src[href.idx].T) and not o[..., 1].any()
+    M = f.read("/Hamiltonian/THC/HalfTransformedMuv")
+    M = M[..., 0] + 1j * M[..., 1]
+    isd = oracle.isdf_real(s.phi, href.idx, s.mesh, s.coulG, phi_occ=po)
+    assert np.linalg.norm(M - isd["M"]) / np.linalg.norm(isd["M"]) < 1e-8
+    assert f.read("/Hamiltonian/THC/dims").tolist() == [s.norb, s.nmu, hs.nmu]
+
+
 def test_driver_empty_cluster_exits(tmp_path, lib):
     """Reference behaviour: CRITICAL ERROR message and exit(1) (src/kmeans.cpp:137-143)."""
     s = system("tiny")

@@ -178,3 +178,30 @@ def test_isdf_device_pointers(gpu_ctx_mixed):
                        torch.from_numpy(s.coulG).cuda(), out_M=dev_M, want=("M",))
     torch.cuda.synchronize()
     assert np.array_equal(dev_M.cpu().numpy(), host["M"])
+
+
+# (config, tolerance on ||dM||/||M||): C_half has cond ~3e10 on tiny, ~6e6 on c2
+HALF_CASES = [("tiny", 1e-6), ("c2", 1e-9)]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("name,tol", HALF_CASES)
+def test_isdf_half_matches_oracle(gpu_ctx_fp64, gpu_ctx_mixed, prec, name, tol):
+    """thc_isdf_half (runs in FP64 in both precisions) against the oracle's half-rotated
+    real form, half the orbitals occupied."""
+    ctx = gpu_ctx_fp64 if prec == "fp64" else gpu_ctx_mixed
+    s = system(name)
+    idx = kmeans_idx(name)
+    nocc = s.norb // 2
+    po = np.ascontiguousarray(s.phi[:, :nocc])
+    r = ctx.isdf_half(s.phi, po, idx, s.mesh, s.coulG)
+    assert r["status"] == 0
+    ref = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG, phi_occ=po)
+    M = _cplx(r["M"])
+    assert _rel(M, ref["M"]) < tol
+    assert np.linalg.norm(M - M.conj().T) <= 1e-14 * np.linalg.norm(M)
+    orb = _cplx(r["orbitals"])
+    assert np.array_equal(orb.real, s.phi[idx].T) and not orb.imag.any()
+    occ = _cplx(r["occ_orbitals"])
+    assert np.array_equal(occ.real, po[idx].T) and not occ.imag.any()
+    assert r["stats"].chol_m_info == 0

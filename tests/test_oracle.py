@@ -190,3 +190,27 @@ def test_thc_reconstructs_pair_coulomb_rank_deficient():
     ex = oracle.pair_coulomb_exact(s.phi, s.mesh, s.coulG, pairs)
     th = oracle.thc_pair_coulomb(s.phi, km.idx, r["M"], pairs)
     assert np.linalg.norm(th - ex) / np.linalg.norm(ex) < 1e-5
+
+
+def test_half_rotated_forms_agree():
+    """Half-rotated M: the complex QR form (setup_CZt_half, forward and backward C2C FFTs,
+    IVMG^T IVG) against the real Cholesky/R2C form, with half the orbitals occupied."""
+    s = synth.config("tiny")
+    km = oracle.kmeans_system(s)
+    po = s.phi[:, : s.norb // 2]
+    a = oracle.isdf_real(s.phi, km.idx, s.mesh, s.coulG, phi_occ=po)
+    b = oracle.isdf_half_reference(s.phi, po, km.idx, s.mesh, s.coulG)
+    # C_half has cond ~3e10 here: QR and Cholesky solutions differ by ~cond * 1e-16.
+    assert np.linalg.norm(a["M"] - b) / np.linalg.norm(b) < 1e-6
+    assert np.allclose(a["C"], a["C"].T, rtol=0, atol=0)
+    assert np.linalg.eigvalsh(a["C"]).min() > 0
+
+
+def test_half_rotated_all_occupied_is_plain():
+    """With every orbital occupied the half-rotated products are P o P."""
+    s = synth.config("tiny")
+    km = oracle.kmeans_system(s)
+    a = oracle.isdf_real(s.phi, km.idx, s.mesh, s.coulG, phi_occ=s.phi)
+    b = oracle.isdf_real(s.phi, km.idx, s.mesh, s.coulG)
+    assert np.array_equal(a["C"], b["C"])
+    assert np.linalg.norm(a["M"] - b["M"]) <= 1e-12 * np.linalg.norm(b["M"])

@@ -34,7 +34,7 @@ EXPORTS = [
     "thc_ctx_last_error", "thc_status_string", "thc_ctx_kernel_launches",
     "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
     "thc_kmeans_history", "thc_factorize_batched", "thc_kmeans_noalloc",
-    "thc_synth_gaussian_basis",
+    "thc_synth_gaussian_basis", "thc_isdf_half",
 ]
 
 
@@ -116,8 +116,11 @@ def load(build_if_missing: bool = False):
     lib.thc_synth_gaussian_basis.restype = ci
     lib.thc_isdf.argtypes = [vp, vp, cll, ci, vp, ci, vp, vp, cd, vp, vp, vp,
                              ctypes.POINTER(IsdfStats)]
+    lib.thc_isdf_half.argtypes = [vp, vp, cll, ci, vp, ci, vp, ci, vp, vp, cd, vp, vp, vp,
+                                  ctypes.POINTER(IsdfStats)]
     for f in ("thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
-              "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_kmeans_noalloc"):
+              "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_kmeans_noalloc",
+              "thc_isdf_half"):
         getattr(lib, f).restype = ci
     _lib = lib
     return lib
@@ -271,3 +274,22 @@ class Context:
         if raise_on_error and st not in (THC_OK, THC_ERR_NOT_PD):
             self._check(st, "thc_isdf")
         return dict(M=out_M, L=out_L, orbitals=out_orbitals, stats=stats, status=st)
+
+    def isdf_half(self, phi, phi_occ, idx, mesh, coulG, shift_rel=-1.0):
+        """thc_isdf_half: half-rotated interpolating vectors and M (no Cholesky factor)."""
+        ng, no = int(phi.shape[0]), int(phi.shape[1])
+        nocc = int(phi_occ.shape[1])
+        if int(phi_occ.shape[0]) != ng:
+            raise ValueError("phi_occ must have N_g rows")
+        nmu = int(idx.shape[0])
+        mesh_a = np.ascontiguousarray(np.asarray(mesh, dtype=np.int32).reshape(3))
+        out_M = np.zeros((nmu, nmu, 2))
+        out_orb = np.zeros((no, nmu, 2))
+        out_occ = np.zeros((nocc, nmu, 2))
+        stats = IsdfStats()
+        st = self.lib.thc_isdf_half(self.h, _ptr(phi), ng, no, _ptr(phi_occ), nocc, _ptr(idx),
+                                    nmu, _ptr(mesh_a), _ptr(coulG), float(shift_rel),
+                                    _ptr(out_orb), _ptr(out_occ), _ptr(out_M),
+                                    ctypes.byref(stats))
+        self._check(st, "thc_isdf_half")
+        return dict(M=out_M, orbitals=out_orb, occ_orbitals=out_occ, stats=stats, status=st)

@@ -63,6 +63,8 @@ enum Slot : int {
   WS_FFTWORK,       // cuFFT work area of the context's plans
   WS_KM_SV,         // k-means terms: 4 x ng doubles in point order + 4 x ng sorted
   WS_KM_WIN,        // k-means windows, cluster window offsets, segment tables
+  WS_PHIOCC,        // half-rotated path: ng x nocc occupied orbitals, then nmu x nocc rows
+  WS_ORB,           // (N_o + N_occ) x N_mu x 2 orbital outputs staged for a host copy
   WS_NSLOTS
 };
 

@@ -125,6 +125,16 @@ __global__ void set_scalar(double* p, double v) { *p = v; }
 
 __global__ void scale_scalar(const double* src, double f, double* dst) { *dst = f * *src; }
 
+// a[r * lda + c] *= b[r * ldb + c] (the Hadamard products of the half-rotated path).
+__global__ void hadamard_k(double* a, long long lda, const double* __restrict__ b,
+                           long long ldb, long long rows, long long cols)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= rows * cols) return;
+  long long r = e / cols, c = e % cols;
+  a[r * lda + c] = __dmul_rn(a[r * lda + c], b[r * ldb + c]);
+}
+
 __global__ void init_chol_status(CholStatus* cs)
 {
   cs->flag = 0;
@@ -193,11 +203,13 @@ int fft_forward(Ctx* c, int n0, int n1, int n2, int count, cufftType type, void*
 
 int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_in, int nmu,
              const int* mesh_in, const double* coul_in, double shift_rel, double* out_orb,
-             double* out_M, double* out_L, thc_isdf_stats* stats)
+             double* out_M, double* out_L, thc_isdf_stats* stats, const double* phiocc_in,
+             int nocc, double* out_orb_occ)
 {
   if (!phi_in || !idx_in || !mesh_in || !coul_in || ng <= 0 || no <= 0 || nmu <= 0 ||
-      nmu > ng)
+      nmu > ng || (phiocc_in && nocc <= 0))
     return set_error(c, THC_ERR_ARG, "thc_isdf: invalid arguments");
+  const bool half = phiocc_in != nullptr;
   int mesh[3];
   if (is_device_ptr(mesh_in)) {
     THC_CUDA(c, cudaMemcpy(mesh, mesh_in, sizeof(mesh), cudaMemcpyDeviceToHost));
@@ -208,7 +220,7 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
       (long long)mesh[0] * mesh[1] * mesh[2] != ng)
     return set_error(c, THC_ERR_SHAPE, "thc_isdf: FFT mesh %dx%dx%d does not match N_g=%lld",
                      mesh[0], mesh[1], mesh[2], ng);
-  if (c->precision == THC_PREC_MIXED) return isdf_run_mixed(c, phi_in, ng, no, idx_in, nmu, mesh,
+  if (c->precision == THC_PREC_MIXED && !half) return isdf_run_mixed(c, phi_in, ng, no, idx_in, nmu, mesh,
                                                             coul_in, shift_rel, out_orb, out_M,
                                                             out_L, stats);
   cudaStream_t s = c->stream;
@@ -219,6 +231,24 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
   if (st) return st;
   const double* coul = (const double*)to_device(c, coul_in, sizeof(double) * ng, WS_COUL, &st);
   if (st) return st;
+  const double* phiocc = nullptr;
+  double* phimu_occ = nullptr;
+  if (half) {
+    // One slot: the occupied orbitals (staged when they are on the host), then their rows
+    // at the interpolating points.
+    const bool dev = is_device_ptr(phiocc_in);
+    double* occ = (double*)ws_get(c, WS_PHIOCC, sizeof(double) * ((dev ? 0 : ng) + nmu) * nocc);
+    if (!occ) return set_error(c, THC_ERR_NOMEM, "thc_isdf: workspace allocation failed");
+    if (dev) {
+      phiocc = phiocc_in;
+      phimu_occ = occ;
+    } else {
+      THC_CUDA(c, cudaMemcpyAsync(occ, phiocc_in, sizeof(double) * ng * nocc,
+                                  cudaMemcpyHostToDevice, s));
+      phiocc = occ;
+      phimu_occ = occ + ng * nocc;
+    }
+  }
 
   const int n0 = mesh[0], n1 = mesh[1], n2 = mesh[2];
   const long long nc = (long long)n0 * n1 * (n2 / 2 + 1);
@@ -248,24 +278,42 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
   double* zero = dmean + 3;
   int* bad = (int*)(scr + 512);
   int* n_anti = bad + 1;
+  // Orbital outputs: written in place on the device, else staged for the host copy.
   double* orb_dev = nullptr;
-  if (out_orb) orb_dev = is_device_ptr(out_orb) ? out_orb : Lw;  // staged through Lw
+  double* occ_dev = nullptr;
+  const bool orb_host = out_orb && !is_device_ptr(out_orb);
+  const bool occ_host = half && out_orb_occ && !is_device_ptr(out_orb_occ);
+  double* orb_stage = nullptr;
+  if (orb_host || occ_host) {
+    orb_stage = (double*)ws_get(c, WS_ORB, sizeof(double) * 2 * nmu * (no + (half ? nocc : 0)));
+    if (!orb_stage) return set_error(c, THC_ERR_NOMEM, "thc_isdf: orbital staging buffer");
+  }
+  if (out_orb) orb_dev = orb_host ? orb_stage : out_orb;
+  if (half && out_orb_occ) occ_dev = occ_host ? orb_stage + 2 * (long long)nmu * no : out_orb_occ;
   THC_CUDA(c, cudaMemsetAsync(scr + 512, 0, 64, s));
   THC_CUDA(c, cudaEventRecord(c->ev0, s));
 
   gather_rows<<<(int)cdiv((long long)nmu * no, 256), 256, 0, s>>>(phi, ng, no, idx, nmu, phimu,
                                                                   orb_dev, bad);
   THC_LAUNCHED(c, "gather_rows");
-  if (out_orb && orb_dev != out_orb)
+  if (orb_host)
     THC_CUDA(c, cudaMemcpyAsync(out_orb, orb_dev, sizeof(double) * 2 * nmu * no,
                                 cudaMemcpyDeviceToHost, s));
+  if (half) {
+    gather_rows<<<(int)cdiv((long long)nmu * nocc, 256), 256, 0, s>>>(phiocc, ng, nocc, idx, nmu,
+                                                                      phimu_occ, occ_dev, bad);
+    THC_LAUNCHED(c, "gather_rows");
+    if (occ_host)
+      THC_CUDA(c, cudaMemcpyAsync(out_orb_occ, occ_dev, sizeof(double) * 2 * nmu * nocc,
+                                  cudaMemcpyDeviceToHost, s));
+  }
   // C = (Phi_mu Phi_mu^T)^2
   {
     GemmArgs g;
     g.M = nmu; g.N = nmu; g.K = no;
     g.A = phimu; g.sam = no; g.sak = 1;
     g.B = phimu; g.sbn = no; g.sbk = 1;
-    g.C = C; g.ldc = nmu; g.mode = GEMM_SQUARE;
+    g.C = C; g.ldc = nmu; g.mode = half ? GEMM_STORE : GEMM_SQUARE;
     if ((st = dgemm(c, g))) return st;
   }
   // Z^T = (Phi_mu Phi^T)^2
@@ -274,8 +322,30 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
     g.M = nmu; g.N = ng; g.K = no;
     g.A = phimu; g.sam = no; g.sak = 1;
     g.B = phi; g.sbn = no; g.sbk = 1;
-    g.C = zt; g.ldc = ng; g.mode = GEMM_SQUARE;
+    g.C = zt; g.ldc = ng; g.mode = half ? GEMM_STORE : GEMM_SQUARE;
     if ((st = dgemm(c, g))) return st;
+  }
+  if (half) {
+    // Half-rotated products: C = (Phi_mu Phi_mu^T) o (Phi_occ,mu Phi_occ,mu^T) and
+    // Z^T = (Phi_mu Phi^T) o (Phi_occ,mu Phi_occ^T) (setup_CZt_half,
+    // src/interpolating_vectors.cpp:143-161).  The occupied products go through Cinv and
+    // zeta, which are written later.
+    GemmArgs g;
+    g.M = nmu; g.N = nmu; g.K = nocc;
+    g.A = phimu_occ; g.sam = nocc; g.sak = 1;
+    g.B = phimu_occ; g.sbn = nocc; g.sbk = 1;
+    g.C = Cinv; g.ldc = nmu; g.mode = GEMM_STORE;
+    if ((st = dgemm(c, g))) return st;
+    GemmArgs h;
+    h.M = nmu; h.N = ng; h.K = nocc;
+    h.A = phimu_occ; h.sam = nocc; h.sak = 1;
+    h.B = phiocc; h.sbn = nocc; h.sbk = 1;
+    h.C = zeta; h.ldc = ng; h.mode = GEMM_STORE;
+    if ((st = dgemm(c, h))) return st;
+    hadamard_k<<<(int)cdiv(nn, 256), 256, 0, s>>>(C, nmu, Cinv, nmu, nmu, nmu);
+    THC_LAUNCHED(c, "hadamard");
+    hadamard_k<<<(int)cdiv((long long)nmu * ng, 256), 256, 0, s>>>(zt, ng, zeta, ng, nmu, ng);
+    THC_LAUNCHED(c, "hadamard");
   }
   // Cholesky of C with breakdown detection, then the shift policy.
   double* Lc = C + nn;
@@ -363,13 +433,15 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
   int nb2 = (int)cdiv(nn, 256);
   assemble_m<<<nb2, 256, 0, s>>>(mre, h_anti > 0 ? xim : nullptr, nmu, mcx);
   THC_LAUNCHED(c, "assemble_m");
-  // Cholesky of M.
+  // Cholesky of M (the half-rotated M is returned as it is).
   init_chol_status<<<1, 1, 0, s>>>(csm);
   THC_LAUNCHED(c, "init_chol_status");
   set_scalar<<<1, 1, 0, s>>>(zero, 0.0);
   THC_LAUNCHED(c, "set_scalar");
   double* Lout = Lw;
-  if (h_anti == 0) {
+  if (half) {
+    // no factor
+  } else if (h_anti == 0) {
     copy_lower_to_full<<<nb2, 256, 0, s>>>(mre, nmu, xim);
     THC_LAUNCHED(c, "copy_lower_to_full");
     if ((st = potrf_inv(c, xim, nmu, nmu, zero, csm, dinv))) return st;
@@ -383,7 +455,8 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
   }
   THC_CUDA(c, cudaEventRecord(c->ev1, s));
   if (out_M) THC_CUDA(c, cudaMemcpyAsync(out_M, mcx, sizeof(double) * 2 * nn, cudaMemcpyDefault, s));
-  if (out_L) THC_CUDA(c, cudaMemcpyAsync(out_L, Lout, sizeof(double) * 2 * nn, cudaMemcpyDefault, s));
+  if (out_L && !half)
+    THC_CUDA(c, cudaMemcpyAsync(out_L, Lout, sizeof(double) * 2 * nn, cudaMemcpyDefault, s));
   CholStatus hm{};
   int hbad = 0;
   THC_CUDA(c, cudaMemcpyAsync(&hm, csm, sizeof(CholStatus), cudaMemcpyDeviceToHost, s));

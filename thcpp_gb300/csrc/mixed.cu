@@ -210,7 +210,11 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   int* n_anti = bad + 1;
   int* gemm_err = bad + 2;
   double* orb_dev = nullptr;
-  if (out_orb) orb_dev = is_device_ptr(out_orb) ? out_orb : Lw;
+  if (out_orb) {
+    orb_dev = is_device_ptr(out_orb) ? out_orb
+                                     : (double*)ws_get(c, WS_ORB, sizeof(double) * 2 * nmu * no);
+    if (!orb_dev) return set_error(c, THC_ERR_NOMEM, "thc_isdf (mixed): orbital staging buffer");
+  }
   THC_CUDA(c, cudaMemsetAsync(scr + 512, 0, 64, s));
   auto gemm = [&](const OzArgs& g) { return c->gemm_tc ? ozgemm_tc(c, g, gemm_err) : ozgemm(c, g); };
   // Slice buffers are k-tiled (both GEMM kernels read either layout).

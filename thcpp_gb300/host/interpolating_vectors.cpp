@@ -6,6 +6,10 @@
 //                           Coulomb matrix and its Cholesky factor; writes THC/Luv in the
 //                           layout of dump_thc_data (:307-315), printing the same warnings
 //   dump_qmcpack_data       hcore, Energies, occups, dims, THC/dims (:210-245)
+//   rotate = true           the half-rotated variant (:45-49, setup_CZt_half :143-161): reads
+//                           aoR_half as well, writes HalfTransformed{Full,Occ}{Orbitals,
+//                           InterpIndx}, and kernel writes HalfTransformedMuv (thc_isdf_half)
+//                           instead of Luv, as dump_thc_data does (:317-328)
 // Datasets are written contiguous rather than gzip-chunked (h5helper.cpp:28-35); values and
 // shapes are identical.
 #include "interpolating_vectors.h"
@@ -31,27 +35,36 @@ IVecs::IVecs(nlohmann::json& input, ContextHandler::BlacsHandler& BH, std::vecto
   std::cout << "##   Setting up interpolative vector solver.   ##" << std::endl;
   std::cout << "#################################################" << std::endl;
   std::cout << std::endl;
-  if (rotate) {
-    std::cerr << " * ERROR: half-rotated THC is not part of the GPU build yet." << std::endl;
-    exit(1);
-  }
-  half_rotate = false;
+  half_rotate = rotate;
+  prefix = rotate ? "HalfTransformed" : "";
   thc_host::context(&input);
   h5lite::Reader f(input_file);
-  std::vector<uint64_t> dims;
-  std::vector<double> aor = f.read_c128("aoR", &dims);
-  ngrid = (long long)dims[0];
-  nbasis = (int)dims[1];
-  phi.resize((size_t)ngrid * nbasis);
-  double max_im = 0.0;
-  for (size_t i = 0; i < phi.size(); i++) {
-    phi[i] = aor[2 * i];
-    max_im = std::max(max_im, std::fabs(aor[2 * i + 1]));
-  }
-  if (max_im != 0.0) {
-    std::cerr << " * ERROR: aoR has a non-zero imaginary part (max " << max_im
-              << "); complex orbitals are not part of the GPU build yet." << std::endl;
-    exit(1);
+  // Real parts of a complex (N_g, n) orbital dataset.
+  auto read_real = [&](const char* name, std::vector<double>& out, long long& rows, int& cols) {
+    std::vector<uint64_t> dims;
+    std::vector<double> aor = f.read_c128(name, &dims);
+    rows = (long long)dims[0];
+    cols = (int)dims[1];
+    out.resize((size_t)rows * cols);
+    double max_im = 0.0;
+    for (size_t i = 0; i < out.size(); i++) {
+      out[i] = aor[2 * i];
+      max_im = std::max(max_im, std::fabs(aor[2 * i + 1]));
+    }
+    if (max_im != 0.0) {
+      std::cerr << " * ERROR: " << name << " has a non-zero imaginary part (max " << max_im
+                << "); complex orbitals are not part of the GPU build yet." << std::endl;
+      exit(1);
+    }
+  };
+  read_real("aoR", phi, ngrid, nbasis);
+  if (rotate) {
+    long long rows = 0;
+    read_real("aoR_half", phi_occ, rows, nocc);
+    if (rows != ngrid) {
+      std::cerr << " * ERROR: aoR_half has " << rows << " grid points, aoR " << ngrid << std::endl;
+      exit(1);
+    }
   }
   fft_grid = f.read_i32("fft_grid");
   interp = interp_indxs;
@@ -61,15 +74,24 @@ IVecs::IVecs(nlohmann::json& input, ContextHandler::BlacsHandler& BH, std::vecto
       exit(1);
     }
   h5lite::Writer w(output_file, append);
-  // Orbitals at the interpolating points: (N_o, N_mu, 2).
+  // Orbitals at the interpolating points, (n, N_mu, 2), and the indices, under the names
+  // setup_pseudo_dm gives them (:75-90).
   int nmu = (int)interp.size();
-  std::vector<double> orb((size_t)nbasis * nmu * 2, 0.0);
-  for (int i = 0; i < nbasis; i++)
-    for (int m = 0; m < nmu; m++) orb[2 * ((size_t)i * nmu + m)] = phi[(size_t)interp[m] * nbasis + i];
-  std::cout << " * Writing aoR_mu to file" << std::endl;
-  w.write_f64("/Hamiltonian/THC/Orbitals", {(uint64_t)nbasis, (uint64_t)nmu, 2}, orb.data());
-  std::cout << " * Writing indices of interpolating points to file" << std::endl;
-  w.write_i32("/Hamiltonian/THC/InterpIndx", {(uint64_t)nmu}, interp.data());
+  auto write_mu = [&](const std::vector<double>& src, int n, const std::string& prfx) {
+    std::vector<double> orb((size_t)n * nmu * 2, 0.0);
+    for (int i = 0; i < n; i++)
+      for (int m = 0; m < nmu; m++) orb[2 * ((size_t)i * nmu + m)] = src[(size_t)interp[m] * n + i];
+    std::cout << " * Writing aoR_mu to file" << std::endl;
+    w.write_f64("/Hamiltonian/THC/" + prfx + "Orbitals", {(uint64_t)n, (uint64_t)nmu, 2}, orb.data());
+    std::cout << " * Writing indices of interpolating points to file" << std::endl;
+    w.write_i32("/Hamiltonian/THC/" + prfx + "InterpIndx", {(uint64_t)nmu}, interp.data());
+  };
+  if (rotate) {
+    write_mu(phi, nbasis, prefix + "Full");
+    write_mu(phi_occ, nocc, prefix + "Occ");
+  } else {
+    write_mu(phi, nbasis, prefix);
+  }
 }
 
 void IVecs::kernel(ContextHandler::BlacsHandler& BH)
@@ -87,8 +109,14 @@ void IVecs::kernel(ContextHandler::BlacsHandler& BH)
   int nmu = (int)interp.size();
   std::vector<double> L((size_t)nmu * nmu * 2);
   thc_isdf_stats st;
-  int status = thc_isdf(thc_host::context(), phi.data(), ngrid, nbasis, interp.data(), nmu,
-                        fft_grid.data(), coul.data(), -1.0, nullptr, nullptr, L.data(), &st);
+  int status;
+  if (half_rotate)
+    status = thc_isdf_half(thc_host::context(), phi.data(), ngrid, nbasis, phi_occ.data(), nocc,
+                           interp.data(), nmu, fft_grid.data(), coul.data(), -1.0, nullptr,
+                           nullptr, L.data(), &st);
+  else
+    status = thc_isdf(thc_host::context(), phi.data(), ngrid, nbasis, interp.data(), nmu,
+                      fft_grid.data(), coul.data(), -1.0, nullptr, nullptr, L.data(), &st);
   if (status != THC_OK && status != THC_ERR_NOT_PD) thc_host::check(status, "ISDF");
   if (st.rank_deficient) {
     std::cout << " * WARNING: CCt matrix is rank deficient (Cholesky pivot " << st.chol_c_info
@@ -98,6 +126,17 @@ void IVecs::kernel(ContextHandler::BlacsHandler& BH)
     std::cout << " * CCt matrix has full rank : " << nmu << std::endl;
     std::cout << std::endl;
   }
+  h5lite::Writer w(output_file, false);
+  if (half_rotate) {
+    // M itself, HalfTransformedMuv (dump_thc_data :317-328).
+    std::cout << " * Dumping half transformed Muv data to: " << output_file << "." << std::endl;
+    std::cout << std::endl;
+    w.write_f64("/Hamiltonian/THC/" + prefix + "Muv", {(uint64_t)nmu, (uint64_t)nmu, 2}, L.data());
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::cout << " * Time for interpolating vectors and Muv : " << secs << " seconds" << std::endl;
+    std::cout << std::endl;
+    return;
+  }
   std::cout << " * Dumping Luv to: " << output_file << "." << std::endl;
   if (status == THC_ERR_NOT_PD) {
     std::cout << "  * WARNING: Cholesky decomposition failed!" << std::endl;
@@ -105,7 +144,6 @@ void IVecs::kernel(ContextHandler::BlacsHandler& BH)
     std::cout << "   * The leading minor of order " << st.chol_m_info << " is not positive definite."
               << std::endl;
   }
-  h5lite::Writer w(output_file, false);
   w.write_f64("/Hamiltonian/THC/Luv", {(uint64_t)nmu, (uint64_t)nmu, 2}, L.data());
   double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   std::cout << " * Time for interpolating vectors and Luv : " << secs << " seconds" << std::endl;

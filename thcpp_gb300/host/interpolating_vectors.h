@@ -25,6 +25,9 @@ class IVecs {
   std::vector<int> fft_grid;
   std::vector<int> interp;
   std::vector<double> phi;   // N_g x N_o real orbitals
+  std::vector<double> phi_occ;  // N_g x N_occ (aoR_half), half-rotated runs only
+  int nocc = 0;
+  std::string prefix;           // "HalfTransformed" for half-rotated runs
   long long ngrid = 0;
 };
 

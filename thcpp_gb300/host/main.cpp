@@ -79,8 +79,16 @@ int main(int argc, char** argv)
     if (!half_rotate) IVSolver.dump_qmcpack_data(thc_cfac, thc_half_cfac, BH);
   }
   if (find_interp_vec && half_rotate) {
-    std::cerr << " * ERROR: half-rotated THC is not part of the GPU build yet." << std::endl;
-    exit(1);
+    // Second pass with the half-rotated products, new points when thc_half_cfac differs
+    // (src/main.cpp:63-72), appended to the same output file.
+    if (thc_half_cfac != thc_cfac) {
+      InterpolatingPoints::IPoints IP(input_data, BH);
+      interp_indxs = IP.kernel(input_data, BH, thc_half_cfac, half_rotate);
+    }
+    bool open_file = false;
+    InterpolatingVectors::IVecs IVSolver(input_data, BH, interp_indxs, half_rotate, open_file);
+    IVSolver.kernel(BH);
+    IVSolver.dump_qmcpack_data(thc_cfac, thc_half_cfac, BH);
   }
   double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   std::cout << " * Total simulation time : " << secs << " seconds." << std::endl;
