@@ -20,6 +20,9 @@
  *                               setup_pseudo_dm/setup_CZt (:59-141), setup_CCt (:163-190),
  *                               least_squares (:416), fft_vectors (:331-404),
  *                               construct_muv (:247-281), dump_thc_data's Cholesky (:283-315)
+ *   thc_qrcp                    QRCP::QRCPSolver::kernel (src/qrcp.cpp:100-173): setup_Z_matrix /
+ *                               setup_Z_half_matrix (:34-67), pzgeqpf (matrix_operations.h:
+ *                               757-790), the first thc_cfac * N_o pivots sorted (:149-160)
  *   thc_isdf_half               IVecs with rotate = true (src/interpolating_vectors.cpp:45-49):
  *                               setup_CZt_half (:143-161), the IVMG product of
  *                               construct_muv (:271-273), dump_thc_data's Muv (:317-328)
@@ -78,6 +81,12 @@ typedef struct thc_isdf_stats {
   double c_min_pivot;      /* min / max squared Cholesky pivot of C (cond estimate^-1)   */
   double device_ms;        /* device time of the call                                    */
 } thc_isdf_stats;
+
+typedef struct thc_qrcp_stats {
+  int numerical_rank;      /* pivots before |R_kk| fell to 1e-7 |R_00| (the residuals of
+                              the Gram form are rounding beyond that)                     */
+  double device_ms;        /* device time of the call                                    */
+} thc_qrcp_stats;
 
 /* Context lifetime.  `precision` is THC_PREC_FP64 or THC_PREC_MIXED. */
 int thc_ctx_create(int device, int precision, thc_ctx** out_ctx);
@@ -196,6 +205,25 @@ int thc_isdf_half(thc_ctx* ctx, const double* phi, long long ng, int norb, const
                   int nocc, const int* idx, int nmu, const int* mesh, const double* coulG,
                   double shift_rel, double* out_orbitals, double* out_occ_orbitals,
                   double* out_M, thc_isdf_stats* stats);
+
+/*
+ * Interpolating points by QR with column pivoting of Z^T (the reference's "qrcp" point
+ * solver): [Z^T]_{(ik)a} = phi_i(r_a) phi_k(r_a) for real orbitals, or with phi_occ the
+ * half-rotated rows phi_occ,i(r_a) phi_k(r_a) in the reference's row layout (rows
+ * i * nocc + k, later pairs overwriting earlier ones when norb > nocc; the context option
+ * "qrcp_all_pairs" = 1 keeps every pair instead).  The pivot sequence is computed as a
+ * pivoted Cholesky factorisation of Z Z^T (the same pivots in exact arithmetic; Z^T is
+ * never formed).  Ties go to the lowest grid index.
+ *   phi         ng x norb doubles (the real part of `aoR`)
+ *   phi_occ     ng x nocc doubles (the real part of `aoR_half`) or NULL
+ *   npts        number of points (thc_cfac * norb), <= ng
+ *   out_idx     npts grid indices, 0-based, sorted ascending
+ *   out_order   npts pivots in the order chosen (may be NULL)
+ *   out_diag    npts values |R_kk| in pivot order (may be NULL)
+ */
+int thc_qrcp(thc_ctx* ctx, const double* phi, long long ng, int norb, const double* phi_occ,
+             int nocc, int npts, int* out_idx, int* out_order, double* out_diag,
+             thc_qrcp_stats* stats);
 
 /*
  * One system of a batch: the inputs of thc_kmeans (grid, rho, init_idx, max_it, threshold)

@@ -12,6 +12,9 @@ Contents
                        (plain and half-rotated):
                        the literal complex form (zgels QR, C2C FFT, herk, zpotrf) and the
                        regularised real form (Cholesky, R2C) used as the parity target.
+``qrcp.py``            numpy/scipy restatement of ``src/qrcp.cpp`` (QRCP points): the
+                       literal Z^T + pivoted Householder QR, and the pivoted Cholesky of
+                       Z Z^T that the CUDA path implements.
 
 Parity pinning
 --------------
@@ -127,3 +130,4 @@ def kmeans_system(system, nthreads: int = 0) -> KMeansResult:
 
 from .isdf import (isdf_reference, isdf_real, half_spectrum_weights,  # noqa: E402,F401
                    pair_coulomb_exact, thc_pair_coulomb, isdf_half_reference)
+from .qrcp import qrcp_reference, qrcp_gram, z_transpose  # noqa: E402,F401

@@ -82,6 +82,31 @@ def test_driver_half_rotated(tmp_path, lib):
     assert f.read("/Hamiltonian/THC/dims").tolist() == [s.norb, s.nmu, hs.nmu]
 
 
+def test_driver_qrcp(tmp_path, lib):
+    """"interpolating_points": {"qrcp": {}} selects QRCPSolver (src/interpolating_points.cpp:
+    43-50): the QRCP points, then the ISDF pass on them."""
+    build.build_host()
+    s = system("tiny")
+    orb = str(tmp_path / "orbitals.h5")
+    out = str(tmp_path / "thc.h5")
+    synth.write_orbital_file(s, orb)
+    inp = tmp_path / "input.json"
+    d = synth.input_json(s, orb, out)
+    d["interpolating_points"] = {"qrcp": {}}
+    inp.write_text(json.dumps(d))
+    r = subprocess.run([build.DRIVER, str(inp)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Using QRCP solver" in r.stdout and "full_ix_diag 47 " in r.stdout
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "qrcp.npz"))
+    f = h5.Reader(out)
+    idx = f.read("/Hamiltonian/THC/InterpIndx")
+    assert np.array_equal(idx, np.sort(g["tiny_order"]))
+    L = f.read("/Hamiltonian/THC/Luv")
+    Lc = L[..., 0] + 1j * L[..., 1]
+    isd = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG)
+    assert np.linalg.norm(Lc @ Lc.conj().T - isd["M"]) / np.linalg.norm(isd["M"]) < 1e-6
+
+
 def test_driver_empty_cluster_exits(tmp_path, lib):
     """Reference behaviour: CRITICAL ERROR message and exit(1) (src/kmeans.cpp:137-143)."""
     s = system("tiny")

@@ -214,3 +214,57 @@ def test_half_rotated_all_occupied_is_plain():
     b = oracle.isdf_real(s.phi, km.idx, s.mesh, s.coulG)
     assert np.array_equal(a["C"], b["C"])
     assert np.linalg.norm(a["M"] - b["M"]) <= 1e-12 * np.linalg.norm(b["M"])
+
+
+def _golden_qrcp():
+    import os
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "qrcp.npz"))
+
+
+def test_qrcp_gram_matches_householder_golden():
+    """The pivoted Cholesky of Z Z^T (the CUDA formulation) picks the pivots of the literal
+    Householder QRCP of Z^T (fixtures from tests/golden/make_golden.py)."""
+    g = _golden_qrcp()
+    tiny = synth.config("tiny")
+    c2 = synth.config("c2")
+    cases = [(c2.phi, 256, None, "c2"), (tiny.phi, 48, None, "tiny"),
+             (tiny.phi, 20, tiny.phi[:, : tiny.nocc], "tiny_half")]
+    for phi, npts, po, key in cases:
+        r = oracle.qrcp_gram(phi, npts, po)
+        assert np.array_equal(r["order"], g[key + "_order"]), key
+        d = g[key + "_diag"]
+        assert np.max(np.abs(r["diag"] - d)) <= 1e-10 * d[0], key
+        assert np.array_equal(r["idx"], np.sort(g[key + "_order"]))
+
+
+def test_qrcp_literal_small_matches_gram():
+    s = synth.config("tiny")
+    a = oracle.qrcp_reference(s.phi, 48)
+    b = oracle.qrcp_gram(s.phi, 48)
+    assert np.array_equal(a["order"], b["order"])
+
+
+def test_qrcp_half_row_layout():
+    """setup_Z_half_matrix writes pair (i, k) to row i * N_occ + k: with N_o > N_occ later
+    pairs overwrite earlier ones and the tail rows stay zero."""
+    s = synth.config("tiny")
+    po = s.phi[:, : s.nocc]
+    ne, nb = po.shape[1], s.phi.shape[1]
+    zt = oracle.z_transpose(s.phi, po)
+    for i in range(ne - 1):
+        for k in range(ne):
+            assert np.array_equal(zt[i * ne + k], po[:, i] * s.phi[:, k])
+    for k in range(nb):
+        assert np.array_equal(zt[(ne - 1) * ne + k], po[:, ne - 1] * s.phi[:, k])
+    assert not zt[(ne - 1) * ne + nb:].any()
+
+
+def test_qrcp_all_pairs_matches_explicit():
+    """The all-pairs option: Gram form against Householder QRCP of every (occ, orbital) row."""
+    import scipy.linalg as sla
+    s = synth.config("tiny")
+    po = s.phi[:, : s.nocc]
+    zt = np.einsum("gi,gk->ikg", po, s.phi).reshape(-1, s.ng)
+    _, perm = sla.qr(zt, mode="r", pivoting=True)
+    r = oracle.qrcp_gram(s.phi, 30, po, all_pairs=True)
+    assert np.array_equal(r["order"], perm[:30])

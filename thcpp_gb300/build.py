@@ -21,10 +21,10 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libthc_gb300.so")
 
 CUDA_SOURCES = ["capi.cu", "kmeans.cu", "dense64.cu", "isdf.cu", "mixed.cu", "ozgemm.cu",
-                "ozgemm_tc.cu", "noalloc.cu", "synthgen.cu"]
+                "ozgemm_tc.cu", "noalloc.cu", "synthgen.cu", "qrcp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST = os.path.join(PKG, "host")
-HOST_SOURCES = ["h5lite.cpp", "h5lite_capi.cpp", "gpu_context.cpp", "kmeans.cpp", "interpolating_points.cpp",
+HOST_SOURCES = ["h5lite.cpp", "h5lite_capi.cpp", "gpu_context.cpp", "kmeans.cpp", "qrcp.cpp", "interpolating_points.cpp",
                 "interpolating_vectors.cpp"]
 HOST_LIB = os.path.join(LIBDIR, "libthcpp_host.so")
 BINDIR = os.path.join(PKG, "bin")

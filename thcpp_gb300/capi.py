@@ -34,7 +34,7 @@ EXPORTS = [
     "thc_ctx_last_error", "thc_status_string", "thc_ctx_kernel_launches",
     "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
     "thc_kmeans_history", "thc_factorize_batched", "thc_kmeans_noalloc",
-    "thc_synth_gaussian_basis", "thc_isdf_half",
+    "thc_synth_gaussian_basis", "thc_isdf_half", "thc_qrcp",
 ]
 
 
@@ -50,6 +50,10 @@ class IsdfStats(ctypes.Structure):
                 ("rank_deficient", ctypes.c_int), ("n_anti", ctypes.c_int),
                 ("shift_used", ctypes.c_double), ("c_min_pivot", ctypes.c_double),
                 ("device_ms", ctypes.c_double)]
+
+
+class QrcpStats(ctypes.Structure):
+    _fields_ = [("numerical_rank", ctypes.c_int), ("device_ms", ctypes.c_double)]
 
 
 class System(ctypes.Structure):
@@ -118,9 +122,10 @@ def load(build_if_missing: bool = False):
                              ctypes.POINTER(IsdfStats)]
     lib.thc_isdf_half.argtypes = [vp, vp, cll, ci, vp, ci, vp, ci, vp, vp, cd, vp, vp, vp,
                                   ctypes.POINTER(IsdfStats)]
+    lib.thc_qrcp.argtypes = [vp, vp, cll, ci, vp, ci, ci, vp, vp, vp, ctypes.POINTER(QrcpStats)]
     for f in ("thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
               "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_kmeans_noalloc",
-              "thc_isdf_half"):
+              "thc_isdf_half", "thc_qrcp"):
         getattr(lib, f).restype = ci
     _lib = lib
     return lib
@@ -274,6 +279,19 @@ class Context:
         if raise_on_error and st not in (THC_OK, THC_ERR_NOT_PD):
             self._check(st, "thc_isdf")
         return dict(M=out_M, L=out_L, orbitals=out_orbitals, stats=stats, status=st)
+
+    def qrcp(self, phi, npts, phi_occ=None):
+        """thc_qrcp: QRCP interpolating points (sorted), pivot order and |R_kk|."""
+        ng, no = int(phi.shape[0]), int(phi.shape[1])
+        nocc = 0 if phi_occ is None else int(phi_occ.shape[1])
+        idx = np.zeros(npts, np.int32)
+        order = np.zeros(npts, np.int32)
+        diag = np.zeros(npts)
+        stats = QrcpStats()
+        st = self.lib.thc_qrcp(self.h, _ptr(phi), ng, no, _ptr(phi_occ), nocc, int(npts),
+                               _ptr(idx), _ptr(order), _ptr(diag), ctypes.byref(stats))
+        self._check(st, "thc_qrcp")
+        return dict(idx=idx, order=order, diag=diag, stats=stats)
 
     def isdf_half(self, phi, phi_occ, idx, mesh, coulG, shift_rel=-1.0):
         """thc_isdf_half: half-rotated interpolating vectors and M (no Cholesky factor)."""

@@ -268,6 +268,10 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
     h->c.tc_bk = (int)value;
     return THC_OK;
   }
+  if (!strcmp(key, "qrcp_all_pairs")) {
+    h->c.qrcp_all_pairs = value != 0.0;
+    return THC_OK;
+  }
   if (!strcmp(key, "fft64")) {
     h->c.fft64 = value != 0.0;
     return THC_OK;
@@ -359,6 +363,17 @@ int thc_isdf_half(thc_ctx* h, const double* phi, long long ng, int norb, const d
   if (stats) memset(stats, 0, sizeof(*stats));
   return thc::isdf_run(&h->c, phi, ng, norb, idx, nmu, mesh, coulG, shift_rel, out_orbitals,
                        out_M, nullptr, stats, phi_occ, nocc, out_occ_orbitals);
+}
+
+int thc_qrcp(thc_ctx* h, const double* phi, long long ng, int norb, const double* phi_occ,
+             int nocc, int npts, int* out_idx, int* out_order, double* out_diag,
+             thc_qrcp_stats* stats)
+{
+  if (!h) return THC_ERR_ARG;
+  if (cudaSetDevice(h->c.device) != cudaSuccess) return THC_ERR_CUDA;
+  if (stats) memset(stats, 0, sizeof(*stats));
+  return thc::qrcp_run(&h->c, phi, ng, norb, phi_occ, nocc, npts, out_idx, out_order, out_diag,
+                       stats);
 }
 
 namespace {

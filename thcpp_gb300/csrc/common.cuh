@@ -95,6 +95,7 @@ struct Ctx {
   int tc_bk = 32;
   int tc_hi_stages = 8; // drain period of the level >= 3 accumulator, in 16-k MMA steps
   int fft64 = 0;        // mixed path: zeta in FP64 and a D2Z FFT (else FP32 and R2C)
+  int qrcp_all_pairs = 0;  // half-rotated QRCP: every (occupied, orbital) pair as a row
   // Instantiated k-means iteration graphs, most recently used last, keyed by every kernel
   // argument they bake in.
   std::vector<std::pair<std::vector<long long>, cudaGraphExec_t>> km_graphs;

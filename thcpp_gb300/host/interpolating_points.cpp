@@ -1,11 +1,12 @@
 // InterpolatingPoints::IPoints (reference: src/interpolating_points.cpp:11-63): solver
-// selection from the JSON and dispatch.  Only the k-means selector is built for the GPU.
+// selection from the JSON and dispatch to the k-means or QRCP selector.
 #include "interpolating_points.h"
 
 #include <cstdlib>
 #include <iostream>
 
 #include "kmeans.h"
+#include "qrcp.h"
 
 namespace InterpolatingPoints {
 
@@ -34,12 +35,13 @@ IPoints::IPoints(nlohmann::json& input, ContextHandler::BlacsHandler& BH)
 std::vector<int> IPoints::kernel(nlohmann::json& input, ContextHandler::BlacsHandler& BH,
                                  int thc_cfac, bool half_rotate)
 {
-  (void)half_rotate;
   std::vector<int> interp_indxs;
   if (solver == "qrcp") {
-    std::cerr << " * ERROR: the QRCP interpolating-point solver is not part of the GPU build;"
-                 " use \"kmeans\"." << std::endl;
-    exit(1);
+    std::cout << " * Using QRCP solver." << std::endl;
+    std::cout << std::endl;
+    QRCP::QRCPSolver QR(input, BH);
+    QR.kernel(BH, interp_indxs, thc_cfac, half_rotate);
+    return interp_indxs;
   }
   std::cout << " * Using K-Means solver." << std::endl;
   std::cout << std::endl;
