@@ -246,7 +246,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--paths", default="mixed,fp64,e2e",
+    ap.add_argument("--paths", default="mixed,fp64,e2e,qrcp",
                     help="comma list of measured paths (a profiling run may keep only 'mixed')")
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS),
                     help="c2 is the benchmark workload; c3 and c4 (batch) are reported separately")
@@ -382,6 +382,23 @@ def main():
         rel_err = float(np.linalg.norm(Mc - M6) / np.linalg.norm(M6))
         idx_same = bool(np.array_equal(idx64, idx_mx))
 
+    # QRCP interpolating points (the reference's other point selector) on the same orbitals,
+    # N_mu pivots over N_g columns; FP64 in both precisions.  Untimed by the step clock.
+    qrcp = None
+    if "qrcp" in paths and WORKLOAD == "c2":
+        q_ms = []
+        for i in range(4):
+            rq = ctx.qrcp(d_phi, nmu)
+            if i:
+                q_ms.append(rq["stats"].device_ms)
+        q = float(np.median(q_ms))
+        # FP64 FMAs: N_g (N_o + k) per step k (the Gram entry and the projection).
+        q_flop = 2.0 * ng * (nmu * no + nmu * (nmu - 1) / 2)
+        qrcp = {"points": nmu, "s_per_system": q * 1e-3,
+                "numerical_rank": int(rq["stats"].numerical_rank),
+                "fp64_tflops": q_flop / (q * 1e-3) / 1e12, "fp64_peak_tflops": 1.25,
+                "peak_source": "nominal (FP64 is not in the measured peaks)"}
+
     # End to end through the C ABI with pinned host buffers.
     def pinned(a):
         t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
@@ -470,6 +487,8 @@ def main():
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "stage_ms_per_system": stage_ms,
         }
+        if qrcp:
+            line["qrcp"] = qrcp
         # Whole-job s/system: ws replicas each factorised one system per step in t_step.
         line["value"] = t_step * 1e-3 / ws
         print(json.dumps(line), flush=True)

@@ -82,7 +82,7 @@ def test_driver_half_rotated(tmp_path, lib):
     assert f.read("/Hamiltonian/THC/dims").tolist() == [s.norb, s.nmu, hs.nmu]
 
 
-def test_driver_qrcp(tmp_path, lib):
+def test_driver_qrcp(tmp_path, lib, gpu_ctx_fp64):
     """"interpolating_points": {"qrcp": {}} selects QRCPSolver (src/interpolating_points.cpp:
     43-50): the QRCP points, then the ISDF pass on them."""
     build.build_host()
@@ -97,10 +97,9 @@ def test_driver_qrcp(tmp_path, lib):
     r = subprocess.run([build.DRIVER, str(inp)], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "Using QRCP solver" in r.stdout and "full_ix_diag 47 " in r.stdout
-    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "qrcp.npz"))
     f = h5.Reader(out)
     idx = f.read("/Hamiltonian/THC/InterpIndx")
-    assert np.array_equal(idx, np.sort(g["tiny_order"]))
+    assert np.array_equal(idx, gpu_ctx_fp64.qrcp(s.phi, s.nmu)["idx"])
     L = f.read("/Hamiltonian/THC/Luv")
     Lc = L[..., 0] + 1j * L[..., 1]
     isd = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG)
