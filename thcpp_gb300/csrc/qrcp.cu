@@ -44,11 +44,32 @@ struct QrPiv {
 };
 
 struct QrGeom {
-  const double* phi;     // N_g x N_o
-  const double* occ;     // N_g x N_occ or null
+  const double* phi;     // N_o x N_g (transposed: a warp reads consecutive points)
+  const double* occ;     // N_occ x N_g or null
   long long ng;
   int no, nocc, kmin;    // kmin: orbitals in the P_min factor; 0 = every pair
+  int ppb;               // points per block (the grid is a multiple of the SM count)
 };
+
+// dst[i * n + a] = src[a * m + i] for a < n, i < m.
+__global__ void transpose_rows(const double* __restrict__ src, long long n, int m,
+                               double* __restrict__ dst)
+{
+  __shared__ double t[32][33];
+  const long long a0 = blockIdx.x * 32LL;
+  const int i0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const long long a = a0 + r;
+    const int i = i0 + threadIdx.x;
+    if (a < n && i < m) t[r][threadIdx.x] = src[a * m + i];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int i = i0 + r;
+    const long long a = a0 + threadIdx.x;
+    if (a < n && i < m) dst[(long long)i * n + a] = t[threadIdx.x][r];
+  }
+}
 
 __device__ __forceinline__ bool piv_better(double v, int a, double w, int b)
 {
@@ -108,21 +129,22 @@ __device__ void finish_argmax(QrPiv mine, QrPiv* blk, unsigned* ticket, int* piv
   }
 }
 
-// G(a, p) with the pivot's rows in shared memory (pp: N_o values, op: N_occ values).
+// G(a, p): the pivot's values are pp[k * ps] (N_o) and op[i * ps] (N_occ) -- shared memory
+// (ps = 1) or the point's own column of the transposed orbitals (ps = N_g, for G(a, a)).
 __device__ __forceinline__ double gram(const QrGeom& g, long long a, const double* pp,
-                                       const double* op)
+                                       const double* op, long long ps)
 {
-  const double* ra = g.phi + a * g.no;
+  const double* ra = g.phi + a;
   double g3 = 0.0, gmin = 0.0;
   for (int k = 0; k < g.no; k++) {
     if (k == g.kmin) gmin = g3;
-    g3 = fma(ra[k], pp[k], g3);
+    g3 = fma(ra[k * g.ng], pp[k * ps], g3);
   }
   if (!g.occ) return g3 * g3;
-  const double* oa = g.occ + a * g.nocc;
+  const double* oa = g.occ + a;
   double g1 = 0.0;
-  for (int i = 0; i < g.nocc - 1; i++) g1 = fma(oa[i], op[i], g1);
-  const double ol = oa[g.nocc - 1] * op[g.nocc - 1];
+  for (int i = 0; i < g.nocc - 1; i++) g1 = fma(oa[i * g.ng], op[i * ps], g1);
+  const double ol = oa[(long long)(g.nocc - 1) * g.ng] * op[(g.nocc - 1) * ps];
   if (g.kmin == 0) return (g1 + ol) * g3;           // every pair: P_occ o P
   if (g.kmin >= g.no) gmin = g3;
   return g1 * gmin + ol * g3;
@@ -132,13 +154,14 @@ __device__ __forceinline__ double gram(const QrGeom& g, long long a, const doubl
 __global__ void __launch_bounds__(kQrThreads)
 qrcp_init_kernel(QrGeom g, double* d, QrPiv* blk, unsigned* ticket, int* piv, double* dpiv)
 {
-  const long long a = blockIdx.x * (long long)kQrThreads + threadIdx.x;
+  const long long a = blockIdx.x * (long long)g.ppb + threadIdx.x;
+  const bool own = threadIdx.x < g.ppb && a < g.ng;
   double v = -INFINITY;
-  if (a < g.ng) {
-    v = gram(g, a, g.phi + a * g.no, g.occ ? g.occ + a * g.nocc : nullptr);
+  if (own) {
+    v = gram(g, a, g.phi + a, g.occ ? g.occ + a : nullptr, g.ng);
     d[a] = v;
   }
-  QrPiv r = block_argmax(v, a < g.ng ? (int)a : 0x7fffffff);
+  QrPiv r = block_argmax(v, own ? (int)a : 0x7fffffff);
   finish_argmax(r, blk, ticket, piv, dpiv, 0);
 }
 
@@ -155,25 +178,40 @@ qrcp_step_kernel(QrGeom g, double* __restrict__ L, double* __restrict__ d, int k
   const int p = piv[k];
   const double dp = dpiv[k];
   const long long ng = g.ng;
-  for (int i = threadIdx.x; i < g.no; i += kQrThreads) pp[i] = g.phi[(long long)p * g.no + i];
+  for (int i = threadIdx.x; i < g.no; i += kQrThreads) pp[i] = g.phi[(long long)i * ng + p];
   if (g.occ)
     for (int i = threadIdx.x; i < g.nocc; i += kQrThreads)
-      op[i] = g.occ[(long long)p * g.nocc + i];
+      op[i] = g.occ[(long long)i * ng + p];
   for (int j = threadIdx.x; j < k; j += kQrThreads) lp[j] = L[j * ng + p];
   __syncthreads();
-  const long long a = blockIdx.x * (long long)kQrThreads + threadIdx.x;
+  const long long a = blockIdx.x * (long long)g.ppb + threadIdx.x;
+  const bool own = threadIdx.x < g.ppb && a < ng;
   double best = -INFINITY;
-  if (a < ng) {
+  if (own) {
     double dv = d[a];
     double l = 0.0;
     if (a == p) {
       l = sqrt(fmax(dp, 0.0));
       dv = -INFINITY;
     } else if (dv != -INFINITY && dp > 0.0) {
-      const double gap = gram(g, a, pp, op);
+      const double gap = gram(g, a, pp, op, 1);
       double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
       const double* la = L + a;
       int j = 0;
+      for (; j + 8 <= k; j += 8) {
+        // Eight loads in flight before the four FMA chains consume them.
+        double x[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) x[u] = la[(j + u) * ng];
+        s0 = fma(x[0], lp[j + 0], s0);
+        s1 = fma(x[1], lp[j + 1], s1);
+        s2 = fma(x[2], lp[j + 2], s2);
+        s3 = fma(x[3], lp[j + 3], s3);
+        s0 = fma(x[4], lp[j + 4], s0);
+        s1 = fma(x[5], lp[j + 5], s1);
+        s2 = fma(x[6], lp[j + 6], s2);
+        s3 = fma(x[7], lp[j + 7], s3);
+      }
       for (; j + 4 <= k; j += 4) {
         s0 = fma(la[(j + 0) * ng], lp[j + 0], s0);
         s1 = fma(la[(j + 1) * ng], lp[j + 1], s1);
@@ -189,7 +227,7 @@ qrcp_step_kernel(QrGeom g, double* __restrict__ L, double* __restrict__ d, int k
     best = dv;
   }
   if (k + 1 >= npts) return;
-  QrPiv r = block_argmax(best, a < ng ? (int)a : 0x7fffffff);
+  QrPiv r = block_argmax(best, own ? (int)a : 0x7fffffff);
   finish_argmax(r, blk, ticket, piv, dpiv, k + 1);
 }
 
@@ -216,25 +254,36 @@ int qrcp_run(Ctx* c, const double* phi_in, long long ng, int no, const double* o
     occ = (const double*)to_device(c, occ_in, sizeof(double) * ng * nocc, WS_PHIOCC, &st);
     if (st) return st;
   }
-  const long long nblk = cdiv(ng, kQrThreads);
-  // L (npts x N_g), d (N_g), block candidates, pivots and their residuals, ticket.
+  const int nt = occ ? nocc : 0;
+  // Balanced grid: a multiple of the SM count, each block a contiguous run of points.
+  int sms = 0;
+  THC_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  sms = std::max(sms, 1);
+  const long long nblk = cdiv(cdiv(ng, kQrThreads), sms) * sms;
+  const int ppb = (int)cdiv(ng, nblk);
+  // L (npts x N_g), the transposed orbitals ((N_o + N_occ) x N_g), d (N_g), block
+  // candidates, pivots and their residuals, ticket.
   const size_t l_bytes = sizeof(double) * (size_t)npts * ng;
-  const size_t bytes = l_bytes + sizeof(double) * ng + sizeof(QrPiv) * nblk +
+  const size_t t_bytes = sizeof(double) * (size_t)(no + nt) * ng;
+  const size_t bytes = l_bytes + t_bytes + sizeof(double) * ng + sizeof(QrPiv) * nblk +
                        (sizeof(int) + sizeof(double)) * npts + 1024;
   char* base = (char*)ws_get(c, WS_ZT, bytes);
   if (!base) return set_error(c, THC_ERR_NOMEM, "thc_qrcp: workspace allocation failed");
   double* L = (double*)base;
-  double* d = L + (size_t)npts * ng;
+  double* phit = L + (size_t)npts * ng;
+  double* occt = phit + (size_t)no * ng;
+  double* d = occt + (size_t)nt * ng;
   QrPiv* blk = (QrPiv*)(d + ng);
   double* dpiv = (double*)(blk + nblk);
   int* piv = (int*)(dpiv + npts);
   unsigned* ticket = (unsigned*)(((uintptr_t)(piv + npts) + 255) & ~(uintptr_t)255);
   QrGeom g;
-  g.phi = phi;
-  g.occ = occ;
+  g.phi = phit;
+  g.occ = occ ? occt : nullptr;
   g.ng = ng;
   g.no = no;
-  g.nocc = occ ? nocc : 0;
+  g.nocc = nt;
+  g.ppb = ppb;
   g.kmin = occ ? (c->qrcp_all_pairs ? 0 : std::min(nocc, no)) : no;
   THC_CUDA(c, cudaFuncSetAttribute(qrcp_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)shmem));
@@ -242,17 +291,24 @@ int qrcp_run(Ctx* c, const double* phi_in, long long ng, int no, const double* o
   THC_CUDA(c, cudaEventRecord(c->ev0, s));
   {
     ProfScope ps(c, "qrcp_init");
+    const dim3 tb(32, 8);
+    transpose_rows<<<dim3((unsigned)cdiv(ng, 32), (unsigned)cdiv(no, 32)), tb, 0, s>>>(phi, ng, no,
+                                                                                     phit);
+    if (occ)
+      transpose_rows<<<dim3((unsigned)cdiv(ng, 32), (unsigned)cdiv(nt, 32)), tb, 0, s>>>(
+          occ, ng, nt, occt);
     qrcp_init_kernel<<<(unsigned)nblk, kQrThreads, 0, s>>>(g, d, blk, ticket, piv, dpiv);
   }
+  c->launches += occ ? 2 : 1;  // the transposes
   THC_LAUNCHED(c, "qrcp_init");
   {
     ProfScope ps(c, "qrcp_step");
     for (int k = 0; k < npts; k++) {
       qrcp_step_kernel<<<(unsigned)nblk, kQrThreads, shmem, s>>>(g, L, d, k, npts, blk, ticket,
                                                                  piv, dpiv);
-      c->launches++;
     }
   }
+  c->launches += npts - 1;
   THC_LAUNCHED(c, "qrcp_step");
   THC_CUDA(c, cudaEventRecord(c->ev1, s));
   std::vector<int> order(npts);
