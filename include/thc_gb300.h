@@ -23,6 +23,7 @@
  *   thc_qrcp                    QRCP::QRCPSolver::kernel (src/qrcp.cpp:100-173): setup_Z_matrix /
  *                               setup_Z_half_matrix (:34-67), pzgeqpf (matrix_operations.h:
  *                               757-790), the first thc_cfac * N_o pivots sorted (:149-160)
+ *   thc_isdf_complex            the same for complex aoR (P = Phi_mu^H Phi, :117; Z = P o conj(P))
  *   thc_isdf_half               IVecs with rotate = true (src/interpolating_vectors.cpp:45-49):
  *                               setup_CZt_half (:143-161), the IVMG product of
  *                               construct_muv (:271-273), dump_thc_data's Muv (:317-328)
@@ -187,6 +188,17 @@ int thc_kmeans_noalloc(thc_ctx* ctx, const double* grid, const double* rho, long
 int thc_isdf(thc_ctx* ctx, const double* phi, long long ng, int norb, const int* idx, int nmu,
              const int* mesh, const double* coulG, double shift_rel, double* out_orbitals,
              double* out_M, double* out_L, thc_isdf_stats* stats);
+
+/*
+ * thc_isdf for complex orbitals (k-point data): phi is ng x norb x 2 doubles, the `aoR`
+ * dataset as stored ((re, im) pairs, C order); out_orbitals receives the complex values.
+ * P = Phi_mu^H Phi is complex, but Z = P o conj(P) = |P|^2 and C = Z[:, idx] are real, so
+ * the interpolating vectors, M and its factor follow the real path.  Runs in FP64 in both
+ * precisions.
+ */
+int thc_isdf_complex(thc_ctx* ctx, const double* phi, long long ng, int norb, const int* idx,
+                     int nmu, const int* mesh, const double* coulG, double shift_rel,
+                     double* out_orbitals, double* out_M, double* out_L, thc_isdf_stats* stats);
 
 /*
  * Half-rotated ISDF (the reference's `half_rotated` input option).  Same inputs as

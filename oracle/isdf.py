@@ -85,15 +85,31 @@ def isdf_real(phi: np.ndarray, idx: np.ndarray, mesh, coulG: np.ndarray, shift: 
               workers=-1, fft_dtype=np.float64, phi_occ=None):
     """Real-arithmetic formulation (the CUDA path's).  Returns dict(M, L, info, zeta, ...).
 
-    ``shift`` is added to the diagonal of C before the Cholesky factorisation.  With
+    ``shift`` is added to the diagonal of C before the Cholesky factorisation.  Complex
+    ``phi`` (k-point orbitals) gives Z = |Phi_mu^H Phi|^2, still real.  With
     ``phi_occ`` (N_g x N_occ) the half-rotated products Z = P_occ o P, C = Z[:, idx] replace
     P o P (C stays symmetric positive semi-definite: a Schur product of two Gram matrices).
     """
-    phi = np.asarray(phi, np.float64)
     idx = np.asarray(idx)
-    ng = phi.shape[0]
-    phimu = phi[idx]
-    if phi_occ is None:
+    if np.iscomplexobj(phi):
+        # Complex orbitals: P = Phi_mu^H Phi, Z = P o conj(P) = |P|^2 is real.
+        phi = np.asarray(phi, np.complex128)
+        ng = phi.shape[0]
+        phimu = phi[idx]
+        if phi_occ is not None:
+            raise ValueError("the half-rotated form takes real orbitals")
+        P = phimu.conj() @ phi.T
+        Pc = phimu.conj() @ phimu.T
+        Zt = P.real ** 2 + P.imag ** 2
+        C = Pc.real ** 2 + Pc.imag ** 2
+        phi_occ = False
+    else:
+        phi = np.asarray(phi, np.float64)
+        ng = phi.shape[0]
+        phimu = phi[idx]
+    if phi_occ is False:
+        pass
+    elif phi_occ is None:
         Zt = (phimu @ phi.T) ** 2                       # (N_mu, N_g)
         C = (phimu @ phimu.T) ** 2
     else:

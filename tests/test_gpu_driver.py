@@ -106,6 +106,32 @@ def test_driver_qrcp(tmp_path, lib, gpu_ctx_fp64):
     assert np.linalg.norm(Lc @ Lc.conj().T - isd["M"]) / np.linalg.norm(isd["M"]) < 1e-6
 
 
+def test_driver_complex_orbitals(tmp_path, lib):
+    """A complex aoR (k-point orbitals) runs thc_isdf_complex; Orbitals keep the imaginary
+    parts."""
+    from tests.test_oracle import complex_orbitals
+    build.build_host()
+    s = system("tiny")
+    pc = complex_orbitals(s.phi)
+    z = synth.System(**{**s.__dict__, "phi": pc})
+    orb = str(tmp_path / "orbitals.h5")
+    out = str(tmp_path / "thc.h5")
+    synth.write_orbital_file(z, orb)
+    inp = tmp_path / "input.json"
+    inp.write_text(json.dumps(synth.input_json(z, orb, out)))
+    r = subprocess.run([build.DRIVER, str(inp)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    ref = oracle.kmeans_system(s)
+    f = h5.Reader(out)
+    assert np.array_equal(f.read("/Hamiltonian/THC/InterpIndx"), ref.idx)
+    o = f.read("/Hamiltonian/THC/Orbitals")
+    assert np.array_equal(o[..., 0] + 1j * o[..., 1], pc[ref.idx].T)
+    L = f.read("/Hamiltonian/THC/Luv")
+    Lc = L[..., 0] + 1j * L[..., 1]
+    isd = oracle.isdf_real(pc, ref.idx, s.mesh, s.coulG)
+    assert np.linalg.norm(Lc @ Lc.conj().T - isd["M"]) / np.linalg.norm(isd["M"]) < 1e-6
+
+
 def test_driver_empty_cluster_exits(tmp_path, lib):
     """Reference behaviour: CRITICAL ERROR message and exit(1) (src/kmeans.cpp:137-143)."""
     s = system("tiny")

@@ -205,3 +205,24 @@ def test_isdf_half_matches_oracle(gpu_ctx_fp64, gpu_ctx_mixed, prec, name, tol):
     occ = _cplx(r["occ_orbitals"])
     assert np.array_equal(occ.real, po[idx].T) and not occ.imag.any()
     assert r["stats"].chol_m_info == 0
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("name,tol", [("tiny", 1e-7), ("c2", 1e-9)])
+def test_isdf_complex_matches_oracle(gpu_ctx_fp64, gpu_ctx_mixed, prec, name, tol):
+    """thc_isdf_complex (FP64 in both precisions): complex orbitals Phi A against the
+    oracle's real form with Z = |Phi_mu^H Phi|^2."""
+    from tests.test_oracle import complex_orbitals
+    ctx = gpu_ctx_fp64 if prec == "fp64" else gpu_ctx_mixed
+    s = system(name)
+    idx = kmeans_idx(name)
+    pc = complex_orbitals(s.phi)
+    r = ctx.isdf_complex(pc, idx, s.mesh, s.coulG)
+    assert r["status"] == 0
+    ref = oracle.isdf_real(pc, idx, s.mesh, s.coulG)
+    M = _cplx(r["M"])
+    assert _rel(M, ref["M"]) < tol
+    L = _cplx(r["L"])
+    assert np.allclose(np.triu(L, 1), 0)
+    assert _rel(L @ L.conj().T, M) < 1e-12
+    assert np.array_equal(_cplx(r["orbitals"]), pc[idx].T)

@@ -268,3 +268,29 @@ def test_qrcp_all_pairs_matches_explicit():
     _, perm = sla.qr(zt, mode="r", pivoting=True)
     r = oracle.qrcp_gram(s.phi, 30, po, all_pairs=True)
     assert np.array_equal(r["order"], perm[:30])
+
+
+def complex_orbitals(phi, seed=7):
+    """Complex orbitals Phi A (A = I + 0.3 (R1 + i R2) / sqrt(N_o)): a genuinely complex
+    P = Phi_mu^H Phi with the span of the real set."""
+    rng = np.random.default_rng(seed)
+    no = phi.shape[1]
+    a = np.eye(no) + 0.3 * (rng.standard_normal((no, no)) + 1j * rng.standard_normal((no, no))) / np.sqrt(no)
+    return phi @ a
+
+
+def test_isdf_complex_forms_agree():
+    """Complex orbitals: the real form (Z = |P|^2, Cholesky, R2C) against the literal complex
+    QR form; and invariance of M under a unitary mixing of the orbitals."""
+    s = synth.config("tiny")
+    km = oracle.kmeans_system(s)
+    pc = complex_orbitals(s.phi)
+    a = oracle.isdf_real(pc, km.idx, s.mesh, s.coulG)
+    b = oracle.isdf_reference(pc, km.idx, s.mesh, s.coulG)
+    assert np.linalg.norm(a["M"] - b["M"]) / np.linalg.norm(b["M"]) < 1e-7   # cond(C) 1.6e9
+    rng = np.random.default_rng(3)
+    u, _ = np.linalg.qr(rng.standard_normal((s.norb, s.norb))
+                        + 1j * rng.standard_normal((s.norb, s.norb)))
+    x = oracle.isdf_real(s.phi @ u, km.idx, s.mesh, s.coulG)
+    r = oracle.isdf_real(s.phi, km.idx, s.mesh, s.coulG)
+    assert np.linalg.norm(x["M"] - r["M"]) / np.linalg.norm(r["M"]) < 1e-7

@@ -34,7 +34,7 @@ EXPORTS = [
     "thc_ctx_last_error", "thc_status_string", "thc_ctx_kernel_launches",
     "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
     "thc_kmeans_history", "thc_factorize_batched", "thc_kmeans_noalloc",
-    "thc_synth_gaussian_basis", "thc_isdf_half", "thc_qrcp",
+    "thc_synth_gaussian_basis", "thc_isdf_half", "thc_qrcp", "thc_isdf_complex",
 ]
 
 
@@ -122,10 +122,11 @@ def load(build_if_missing: bool = False):
                              ctypes.POINTER(IsdfStats)]
     lib.thc_isdf_half.argtypes = [vp, vp, cll, ci, vp, ci, vp, ci, vp, vp, cd, vp, vp, vp,
                                   ctypes.POINTER(IsdfStats)]
+    lib.thc_isdf_complex.argtypes = lib.thc_isdf.argtypes
     lib.thc_qrcp.argtypes = [vp, vp, cll, ci, vp, ci, ci, vp, vp, vp, ctypes.POINTER(QrcpStats)]
     for f in ("thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
               "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_kmeans_noalloc",
-              "thc_isdf_half", "thc_qrcp"):
+              "thc_isdf_half", "thc_qrcp", "thc_isdf_complex"):
         getattr(lib, f).restype = ci
     _lib = lib
     return lib
@@ -279,6 +280,24 @@ class Context:
         if raise_on_error and st not in (THC_OK, THC_ERR_NOT_PD):
             self._check(st, "thc_isdf")
         return dict(M=out_M, L=out_L, orbitals=out_orbitals, stats=stats, status=st)
+
+    def isdf_complex(self, phi, idx, mesh, coulG, shift_rel=-1.0):
+        """thc_isdf_complex: ``phi`` complex128 (N_g, N_o) or float64 (N_g, N_o, 2)."""
+        if np.iscomplexobj(phi):
+            phi = np.ascontiguousarray(phi).view(np.float64).reshape(phi.shape + (2,))
+        ng, no = int(phi.shape[0]), int(phi.shape[1])
+        nmu = int(idx.shape[0])
+        mesh_a = np.ascontiguousarray(np.asarray(mesh, dtype=np.int32).reshape(3))
+        out_M = np.zeros((nmu, nmu, 2))
+        out_L = np.zeros((nmu, nmu, 2))
+        out_orb = np.zeros((no, nmu, 2))
+        stats = IsdfStats()
+        st = self.lib.thc_isdf_complex(self.h, _ptr(phi), ng, no, _ptr(idx), nmu, _ptr(mesh_a),
+                                       _ptr(coulG), float(shift_rel), _ptr(out_orb),
+                                       _ptr(out_M), _ptr(out_L), ctypes.byref(stats))
+        if st not in (THC_OK, THC_ERR_NOT_PD):
+            self._check(st, "thc_isdf_complex")
+        return dict(M=out_M, L=out_L, orbitals=out_orb, stats=stats, status=st)
 
     def qrcp(self, phi, npts, phi_occ=None):
         """thc_qrcp: QRCP interpolating points (sorted), pivot order and |R_kk|."""

@@ -353,6 +353,17 @@ int thc_isdf(thc_ctx* h, const double* phi, long long ng, int norb, const int* i
                        out_M, out_L, stats);
 }
 
+int thc_isdf_complex(thc_ctx* h, const double* phi, long long ng, int norb, const int* idx,
+                     int nmu, const int* mesh, const double* coulG, double shift_rel,
+                     double* out_orbitals, double* out_M, double* out_L, thc_isdf_stats* stats)
+{
+  if (!h) return THC_ERR_ARG;
+  if (cudaSetDevice(h->c.device) != cudaSuccess) return THC_ERR_CUDA;
+  if (stats) memset(stats, 0, sizeof(*stats));
+  return thc::isdf_run(&h->c, phi, ng, norb, idx, nmu, mesh, coulG, shift_rel, out_orbitals,
+                       out_M, out_L, stats, nullptr, 0, nullptr, true);
+}
+
 int thc_isdf_half(thc_ctx* h, const double* phi, long long ng, int norb, const double* phi_occ,
                   int nocc, const int* idx, int nmu, const int* mesh, const double* coulG,
                   double shift_rel, double* out_orbitals, double* out_occ_orbitals,

@@ -125,6 +125,40 @@ __global__ void set_scalar(double* p, double v) { *p = v; }
 
 __global__ void scale_scalar(const double* src, double f, double* dst) { *dst = f * *src; }
 
+// Complex orbitals stored as (re, im) pairs, K = 2 N_o real columns per point:
+// out[a, 2i] = Im phi_i(a), out[a, 2i + 1] = -Re phi_i(a), so that a real product of
+// the pair layout with this one is Im P = Im(Phi_mu^H Phi).
+__global__ void rotate_pairs(const double* __restrict__ in, long long n, double* __restrict__ out)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const double re = in[2 * e], im = in[2 * e + 1];
+  out[2 * e] = im;
+  out[2 * e + 1] = -re;
+}
+
+// a = a + b * b elementwise (|P|^2 = (Re P)^2 + (Im P)^2, with a = (Re P)^2 on entry).
+__global__ void add_square_k(double* a, long long lda, const double* __restrict__ b,
+                             long long ldb, long long rows, long long cols)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= rows * cols) return;
+  long long r = e / cols, c = e % cols;
+  const double v = b[r * ldb + c];
+  a[r * lda + c] = __dadd_rn(a[r * lda + c], __dmul_rn(v, v));
+}
+
+// /Hamiltonian/THC/Orbitals (N_o, N_mu, 2) from the gathered complex rows (N_mu x 2 N_o).
+__global__ void complex_orbitals_out(const double* __restrict__ phimu, int nmu, int no,
+                                     double* __restrict__ orbitals)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)nmu * no) return;
+  const int mu = (int)(e / no), i = (int)(e % no);
+  orbitals[2 * ((long long)i * nmu + mu)] = phimu[2 * e];
+  orbitals[2 * ((long long)i * nmu + mu) + 1] = phimu[2 * e + 1];
+}
+
 // a[r * lda + c] *= b[r * ldb + c] (the Hadamard products of the half-rotated path).
 __global__ void hadamard_k(double* a, long long lda, const double* __restrict__ b,
                            long long ldb, long long rows, long long cols)
@@ -204,12 +238,16 @@ int fft_forward(Ctx* c, int n0, int n1, int n2, int count, cufftType type, void*
 int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_in, int nmu,
              const int* mesh_in, const double* coul_in, double shift_rel, double* out_orb,
              double* out_M, double* out_L, thc_isdf_stats* stats, const double* phiocc_in,
-             int nocc, double* out_orb_occ)
+             int nocc, double* out_orb_occ, bool cplx)
 {
   if (!phi_in || !idx_in || !mesh_in || !coul_in || ng <= 0 || no <= 0 || nmu <= 0 ||
       nmu > ng || (phiocc_in && nocc <= 0))
     return set_error(c, THC_ERR_ARG, "thc_isdf: invalid arguments");
   const bool half = phiocc_in != nullptr;
+  if (half && cplx)
+    return set_error(c, THC_ERR_ARG, "thc_isdf: the half-rotated path takes real orbitals");
+  // Row width of phi in doubles: N_o real values, or N_o (re, im) pairs.
+  const int kw = cplx ? 2 * no : no;
   int mesh[3];
   if (is_device_ptr(mesh_in)) {
     THC_CUDA(c, cudaMemcpy(mesh, mesh_in, sizeof(mesh), cudaMemcpyDeviceToHost));
@@ -220,12 +258,12 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
       (long long)mesh[0] * mesh[1] * mesh[2] != ng)
     return set_error(c, THC_ERR_SHAPE, "thc_isdf: FFT mesh %dx%dx%d does not match N_g=%lld",
                      mesh[0], mesh[1], mesh[2], ng);
-  if (c->precision == THC_PREC_MIXED && !half) return isdf_run_mixed(c, phi_in, ng, no, idx_in, nmu, mesh,
+  if (c->precision == THC_PREC_MIXED && !half && !cplx) return isdf_run_mixed(c, phi_in, ng, no, idx_in, nmu, mesh,
                                                             coul_in, shift_rel, out_orb, out_M,
                                                             out_L, stats);
   cudaStream_t s = c->stream;
   int st = 0;
-  const double* phi = (const double*)to_device(c, phi_in, sizeof(double) * ng * no, WS_PHI, &st);
+  const double* phi = (const double*)to_device(c, phi_in, sizeof(double) * ng * kw, WS_PHI, &st);
   if (st) return st;
   const int* idx = (const int*)to_device(c, idx_in, sizeof(int) * nmu, WS_IDX, &st);
   if (st) return st;
@@ -253,7 +291,13 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
   const int n0 = mesh[0], n1 = mesh[1], n2 = mesh[2];
   const long long nc = (long long)n0 * n1 * (n2 / 2 + 1);
   const long long nn = (long long)nmu * nmu;
-  double* phimu = (double*)ws_get(c, WS_PHIMU, sizeof(double) * nmu * no);
+  // Complex orbitals: phimu holds the gathered pair rows and then their rotated copies.
+  double* phimu = (double*)ws_get(c, WS_PHIMU, sizeof(double) * nmu * kw * (cplx ? 2 : 1));
+  double* phij = nullptr;
+  if (cplx) {
+    phij = (double*)ws_get(c, WS_PHIOCC, sizeof(double) * ng * kw);
+    if (!phij) return set_error(c, THC_ERR_NOMEM, "thc_isdf: workspace allocation failed");
+  }
   double* C = (double*)ws_get(c, WS_C, sizeof(double) * 2 * nn);   // C and its factor
   double* Cinv = (double*)ws_get(c, WS_CINV, sizeof(double) * nn);
   double* zt = (double*)ws_get(c, WS_ZT, sizeof(double) * nmu * ng);
@@ -293,9 +337,22 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
   THC_CUDA(c, cudaMemsetAsync(scr + 512, 0, 64, s));
   THC_CUDA(c, cudaEventRecord(c->ev0, s));
 
-  gather_rows<<<(int)cdiv((long long)nmu * no, 256), 256, 0, s>>>(phi, ng, no, idx, nmu, phimu,
-                                                                  orb_dev, bad);
+  gather_rows<<<(int)cdiv((long long)nmu * kw, 256), 256, 0, s>>>(phi, ng, kw, idx, nmu, phimu,
+                                                                  cplx ? nullptr : orb_dev, bad);
   THC_LAUNCHED(c, "gather_rows");
+  double* phimu_j = phimu + (long long)nmu * kw;
+  if (cplx) {
+    if (orb_dev) {
+      complex_orbitals_out<<<(int)cdiv((long long)nmu * no, 256), 256, 0, s>>>(phimu, nmu, no,
+                                                                              orb_dev);
+      THC_LAUNCHED(c, "complex_orbitals_out");
+    }
+    rotate_pairs<<<(int)cdiv(ng * no, 256), 256, 0, s>>>(phi, ng * no, phij);
+    THC_LAUNCHED(c, "rotate_pairs");
+    rotate_pairs<<<(int)cdiv((long long)nmu * no, 256), 256, 0, s>>>(phimu, (long long)nmu * no,
+                                                                    phimu_j);
+    THC_LAUNCHED(c, "rotate_pairs");
+  }
   if (orb_host)
     THC_CUDA(c, cudaMemcpyAsync(out_orb, orb_dev, sizeof(double) * 2 * nmu * no,
                                 cudaMemcpyDeviceToHost, s));
@@ -310,20 +367,41 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
   // C = (Phi_mu Phi_mu^T)^2
   {
     GemmArgs g;
-    g.M = nmu; g.N = nmu; g.K = no;
-    g.A = phimu; g.sam = no; g.sak = 1;
-    g.B = phimu; g.sbn = no; g.sbk = 1;
+    g.M = nmu; g.N = nmu; g.K = kw;
+    g.A = phimu; g.sam = kw; g.sak = 1;
+    g.B = phimu; g.sbn = kw; g.sbk = 1;
     g.C = C; g.ldc = nmu; g.mode = half ? GEMM_STORE : GEMM_SQUARE;
     if ((st = dgemm(c, g))) return st;
   }
   // Z^T = (Phi_mu Phi^T)^2
   {
     GemmArgs g;
-    g.M = nmu; g.N = ng; g.K = no;
-    g.A = phimu; g.sam = no; g.sak = 1;
-    g.B = phi; g.sbn = no; g.sbk = 1;
+    g.M = nmu; g.N = ng; g.K = kw;
+    g.A = phimu; g.sam = kw; g.sak = 1;
+    g.B = phi; g.sbn = kw; g.sbk = 1;
     g.C = zt; g.ldc = ng; g.mode = half ? GEMM_STORE : GEMM_SQUARE;
     if ((st = dgemm(c, g))) return st;
+  }
+  if (cplx) {
+    // Z = P o conj(P) = (Re P)^2 + (Im P)^2 (setup_CZt, src/interpolating_vectors.cpp:127-141):
+    // the squared real parts are in C and zt; the imaginary parts go through Cinv and zeta,
+    // which are written later.
+    GemmArgs g;
+    g.M = nmu; g.N = nmu; g.K = kw;
+    g.A = phimu; g.sam = kw; g.sak = 1;
+    g.B = phimu_j; g.sbn = kw; g.sbk = 1;
+    g.C = Cinv; g.ldc = nmu; g.mode = GEMM_STORE;
+    if ((st = dgemm(c, g))) return st;
+    GemmArgs h;
+    h.M = nmu; h.N = ng; h.K = kw;
+    h.A = phimu; h.sam = kw; h.sak = 1;
+    h.B = phij; h.sbn = kw; h.sbk = 1;
+    h.C = zeta; h.ldc = ng; h.mode = GEMM_STORE;
+    if ((st = dgemm(c, h))) return st;
+    add_square_k<<<(int)cdiv(nn, 256), 256, 0, s>>>(C, nmu, Cinv, nmu, nmu, nmu);
+    THC_LAUNCHED(c, "add_square");
+    add_square_k<<<(int)cdiv((long long)nmu * ng, 256), 256, 0, s>>>(zt, ng, zeta, ng, nmu, ng);
+    THC_LAUNCHED(c, "add_square");
   }
   if (half) {
     // Half-rotated products: C = (Phi_mu Phi_mu^T) o (Phi_occ,mu Phi_occ,mu^T) and

@@ -16,11 +16,13 @@ int fft_forward(Ctx* c, int n0, int n1, int n2, int count, cufftType type, void*
 // With phi_occ (N_g x nocc) the half-rotated products replace P o P: Z = P_occ o P,
 // C = Z[:, idx]; M is returned without a Cholesky factor (out_L unused) and the occupied
 // orbitals at the interpolating points go to out_orb_occ.  This path runs in FP64 in both
-// precisions.
+// precisions.  With complex_orbitals, phi holds N_o (re, im) pairs per point and
+// Z = |Phi_mu^H Phi|^2 (real, so the rest of the path is unchanged); FP64 as well.
 int isdf_run(Ctx* c, const double* phi, long long ng, int no, const int* idx, int nmu,
              const int* mesh, const double* coul, double shift_rel, double* out_orb,
              double* out_M, double* out_L, thc_isdf_stats* stats,
-             const double* phi_occ = nullptr, int nocc = 0, double* out_orb_occ = nullptr);
+             const double* phi_occ = nullptr, int nocc = 0, double* out_orb_occ = nullptr,
+             bool complex_orbitals = false);
 
 // Mixed-precision variant (mesh already validated and copied to the host).
 int isdf_run_mixed(Ctx* c, const double* phi, long long ng, int no, const int* idx, int nmu,

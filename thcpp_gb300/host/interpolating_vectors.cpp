@@ -2,6 +2,7 @@
 //   constructor (:17-57)    reads aoR and fft_grid, truncates the output file when asked,
 //                           writes /Hamiltonian/THC/{Orbitals, InterpIndx} as
 //                           setup_pseudo_dm does (:75-90)
+//                           (complex aoR, k-point orbitals: thc_isdf_complex, Z = |P|^2)
 //   kernel (:406-455)       one GPU call (thc_isdf) for the least-squares vectors, the FFT
 //                           Coulomb matrix and its Cholesky factor; writes THC/Luv in the
 //                           layout of dump_thc_data (:307-315), printing the same warnings
@@ -39,28 +40,37 @@ IVecs::IVecs(nlohmann::json& input, ContextHandler::BlacsHandler& BH, std::vecto
   prefix = rotate ? "HalfTransformed" : "";
   thc_host::context(&input);
   h5lite::Reader f(input_file);
-  // Real parts of a complex (N_g, n) orbital dataset.
-  auto read_real = [&](const char* name, std::vector<double>& out, long long& rows, int& cols) {
+  // A complex (N_g, n) orbital dataset: its real parts, or (re, im) pairs when an
+  // imaginary part is non-zero and complex data are allowed.
+  auto read_orbitals = [&](const char* name, std::vector<double>& out, long long& rows,
+                           int& cols, bool allow_complex, bool* is_complex) {
     std::vector<uint64_t> dims;
     std::vector<double> aor = f.read_c128(name, &dims);
     rows = (long long)dims[0];
     cols = (int)dims[1];
-    out.resize((size_t)rows * cols);
     double max_im = 0.0;
-    for (size_t i = 0; i < out.size(); i++) {
-      out[i] = aor[2 * i];
+    for (size_t i = 0; i < (size_t)rows * cols; i++)
       max_im = std::max(max_im, std::fabs(aor[2 * i + 1]));
+    if (max_im != 0.0 && allow_complex) {
+      *is_complex = true;
+      out.swap(aor);
+      return;
     }
     if (max_im != 0.0) {
       std::cerr << " * ERROR: " << name << " has a non-zero imaginary part (max " << max_im
-                << "); complex orbitals are not part of the GPU build yet." << std::endl;
+                << "); the half-rotated pass takes real orbitals." << std::endl;
       exit(1);
     }
+    out.resize((size_t)rows * cols);
+    for (size_t i = 0; i < out.size(); i++) out[i] = aor[2 * i];
   };
-  read_real("aoR", phi, ngrid, nbasis);
+  bool unused = false;
+  read_orbitals("aoR", phi, ngrid, nbasis, !rotate, &complex_orbitals);
+  if (complex_orbitals)
+    std::cout << " * aoR is complex: Z = |P|^2 from complex pseudo-densities." << std::endl;
   if (rotate) {
     long long rows = 0;
-    read_real("aoR_half", phi_occ, rows, nocc);
+    read_orbitals("aoR_half", phi_occ, rows, nocc, false, &unused);
     if (rows != ngrid) {
       std::cerr << " * ERROR: aoR_half has " << rows << " grid points, aoR " << ngrid << std::endl;
       exit(1);
@@ -77,20 +87,29 @@ IVecs::IVecs(nlohmann::json& input, ContextHandler::BlacsHandler& BH, std::vecto
   // Orbitals at the interpolating points, (n, N_mu, 2), and the indices, under the names
   // setup_pseudo_dm gives them (:75-90).
   int nmu = (int)interp.size();
-  auto write_mu = [&](const std::vector<double>& src, int n, const std::string& prfx) {
+  auto write_mu = [&](const std::vector<double>& src, int n, const std::string& prfx,
+                      bool cplx) {
     std::vector<double> orb((size_t)n * nmu * 2, 0.0);
     for (int i = 0; i < n; i++)
-      for (int m = 0; m < nmu; m++) orb[2 * ((size_t)i * nmu + m)] = src[(size_t)interp[m] * n + i];
+      for (int m = 0; m < nmu; m++) {
+        const size_t o = 2 * ((size_t)i * nmu + m);
+        if (cplx) {
+          orb[o] = src[2 * ((size_t)interp[m] * n + i)];
+          orb[o + 1] = src[2 * ((size_t)interp[m] * n + i) + 1];
+        } else {
+          orb[o] = src[(size_t)interp[m] * n + i];
+        }
+      }
     std::cout << " * Writing aoR_mu to file" << std::endl;
     w.write_f64("/Hamiltonian/THC/" + prfx + "Orbitals", {(uint64_t)n, (uint64_t)nmu, 2}, orb.data());
     std::cout << " * Writing indices of interpolating points to file" << std::endl;
     w.write_i32("/Hamiltonian/THC/" + prfx + "InterpIndx", {(uint64_t)nmu}, interp.data());
   };
   if (rotate) {
-    write_mu(phi, nbasis, prefix + "Full");
-    write_mu(phi_occ, nocc, prefix + "Occ");
+    write_mu(phi, nbasis, prefix + "Full", false);
+    write_mu(phi_occ, nocc, prefix + "Occ", false);
   } else {
-    write_mu(phi, nbasis, prefix);
+    write_mu(phi, nbasis, prefix, complex_orbitals);
   }
 }
 
@@ -114,6 +133,9 @@ void IVecs::kernel(ContextHandler::BlacsHandler& BH)
     status = thc_isdf_half(thc_host::context(), phi.data(), ngrid, nbasis, phi_occ.data(), nocc,
                            interp.data(), nmu, fft_grid.data(), coul.data(), -1.0, nullptr,
                            nullptr, L.data(), &st);
+  else if (complex_orbitals)
+    status = thc_isdf_complex(thc_host::context(), phi.data(), ngrid, nbasis, interp.data(), nmu,
+                              fft_grid.data(), coul.data(), -1.0, nullptr, nullptr, L.data(), &st);
   else
     status = thc_isdf(thc_host::context(), phi.data(), ngrid, nbasis, interp.data(), nmu,
                       fft_grid.data(), coul.data(), -1.0, nullptr, nullptr, L.data(), &st);

@@ -24,7 +24,8 @@ class IVecs {
   bool half_rotate = false;
   std::vector<int> fft_grid;
   std::vector<int> interp;
-  std::vector<double> phi;   // N_g x N_o real orbitals
+  std::vector<double> phi;   // N_g x N_o real orbitals, or N_g x N_o (re, im) pairs
+  bool complex_orbitals = false;
   std::vector<double> phi_occ;  // N_g x N_occ (aoR_half), half-rotated runs only
   int nocc = 0;
   std::string prefix;           // "HalfTransformed" for half-rotated runs

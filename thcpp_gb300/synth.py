@@ -323,7 +323,7 @@ def write_orbital_file(system: System, path: str, half_rotate: bool = False) -> 
     """
     from . import h5
     nup = system.nocc
-    full = np.einsum("ij,ij->i", system.phi, system.phi)
+    full = np.einsum("ij,ij->i", np.conj(system.phi), system.phi).real
     with h5.Writer(path, truncate=True) as w:
         w.write("real_space_grid", system.grid)
         w.write("kmesh", np.ones(3, dtype=np.int32))
