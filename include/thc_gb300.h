@@ -20,6 +20,7 @@
  *                               setup_pseudo_dm/setup_CZt (:59-141), setup_CCt (:163-190),
  *                               least_squares (:416), fft_vectors (:331-404),
  *                               construct_muv (:247-281), dump_thc_data's Cholesky (:283-315)
+ *   thc_qrcp_complex            the same for complex aoR
  *   thc_qrcp                    QRCP::QRCPSolver::kernel (src/qrcp.cpp:100-173): setup_Z_matrix /
  *                               setup_Z_half_matrix (:34-67), pzgeqpf (matrix_operations.h:
  *                               757-790), the first thc_cfac * N_o pivots sorted (:149-160)
@@ -236,6 +237,13 @@ int thc_isdf_half(thc_ctx* ctx, const double* phi, long long ng, int norb, const
 int thc_qrcp(thc_ctx* ctx, const double* phi, long long ng, int norb, const double* phi_occ,
              int nocc, int npts, int* out_idx, int* out_order, double* out_diag,
              thc_qrcp_stats* stats);
+
+/*
+ * thc_qrcp for complex orbitals: phi is ng x norb x 2 doubles ((re, im) pairs, as `aoR` is
+ * stored); the rows of Z^T are conj(phi_i) phi_k and its Gram matrix is |Phi^H Phi|^2.
+ */
+int thc_qrcp_complex(thc_ctx* ctx, const double* phi, long long ng, int norb, int npts,
+                     int* out_idx, int* out_order, double* out_diag, thc_qrcp_stats* stats);
 
 /*
  * One system of a batch: the inputs of thc_kmeans (grid, rho, init_idx, max_it, threshold)

@@ -19,7 +19,7 @@ of Z^T, one row per orbital pair and one column per grid point:
     Same pivots as QRCP in exact arithmetic (d_k(a) = squared residual norm of column a);
     ties go to the lowest grid index.
 
-Real orbitals only (the reference's complex conj(phi_i) phi_k reduces to this).
+Complex orbitals: rows conj(phi_i) phi_k, Gram matrix |P|^2 with P = Phi^H Phi (real).
 """
 
 from __future__ import annotations
@@ -30,6 +30,11 @@ import scipy.linalg as sla
 
 def z_transpose(phi: np.ndarray, phi_occ=None) -> np.ndarray:
     """Z^T exactly as the reference fills it (rows x N_g)."""
+    if np.iscomplexobj(phi):
+        phi = np.asarray(phi, np.complex128)
+        ng, nb = phi.shape
+        return np.ascontiguousarray(
+            (phi.conj()[:, :, None] * phi[:, None, :]).reshape(ng, nb * nb).T)
     phi = np.asarray(phi, np.float64)
     ng, nb = phi.shape
     if phi_occ is None:
@@ -53,6 +58,9 @@ def qrcp_reference(phi: np.ndarray, npts: int, phi_occ=None):
 
 
 def _gram_column(phi, po, p, kmin):
+    if np.iscomplexobj(phi):
+        g = phi.conj() @ phi[p]                  # P(a, p) = sum_k conj(phi_k(a)) phi_k(p)
+        return g.real ** 2 + g.imag ** 2
     g3 = phi @ phi[p]
     if po is None:
         return g3 * g3
@@ -65,6 +73,8 @@ def _gram_column(phi, po, p, kmin):
 
 
 def _gram_diag(phi, po, kmin):
+    if np.iscomplexobj(phi):
+        return np.einsum("ij,ij->i", phi.conj(), phi).real ** 2
     g3 = np.einsum("ij,ij->i", phi, phi)
     if po is None:
         return g3 * g3
@@ -78,7 +88,7 @@ def _gram_diag(phi, po, kmin):
 
 def qrcp_gram(phi: np.ndarray, npts: int, phi_occ=None, all_pairs: bool = False):
     """Pivoted Cholesky of Z Z^T.  Returns dict(idx sorted, order, diag)."""
-    phi = np.asarray(phi, np.float64)
+    phi = np.asarray(phi, np.complex128 if np.iscomplexobj(phi) else np.float64)
     po = None if phi_occ is None else np.asarray(phi_occ, np.float64)
     ng, nb = phi.shape
     kmin = nb if po is None else (0 if all_pairs else min(po.shape[1], nb))

@@ -132,6 +132,31 @@ def test_driver_complex_orbitals(tmp_path, lib):
     assert np.linalg.norm(Lc @ Lc.conj().T - isd["M"]) / np.linalg.norm(isd["M"]) < 1e-6
 
 
+def test_driver_qrcp_complex(tmp_path, lib, gpu_ctx_fp64):
+    """QRCP points and the ISDF pass on a complex orbital file."""
+    from tests.test_oracle import complex_orbitals
+    build.build_host()
+    s = system("tiny")
+    pc = complex_orbitals(s.phi)
+    z = synth.System(**{**s.__dict__, "phi": pc})
+    orb = str(tmp_path / "orbitals.h5")
+    out = str(tmp_path / "thc.h5")
+    synth.write_orbital_file(z, orb)
+    inp = tmp_path / "input.json"
+    d = synth.input_json(z, orb, out)
+    d["interpolating_points"] = {"qrcp": {}}
+    inp.write_text(json.dumps(d))
+    r = subprocess.run([build.DRIVER, str(inp)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    f = h5.Reader(out)
+    idx = f.read("/Hamiltonian/THC/InterpIndx")
+    assert np.array_equal(idx, oracle.qrcp_gram(pc, s.nmu)["idx"])
+    L = f.read("/Hamiltonian/THC/Luv")
+    Lc = L[..., 0] + 1j * L[..., 1]
+    isd = oracle.isdf_real(pc, idx, s.mesh, s.coulG)
+    assert np.linalg.norm(Lc @ Lc.conj().T - isd["M"]) / np.linalg.norm(isd["M"]) < 1e-6
+
+
 def test_driver_empty_cluster_exits(tmp_path, lib):
     """Reference behaviour: CRITICAL ERROR message and exit(1) (src/kmeans.cpp:137-143)."""
     s = system("tiny")

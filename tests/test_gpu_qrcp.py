@@ -75,3 +75,17 @@ def test_qrcp_invalid_arguments(gpu_ctx_fp64):
     with pytest.raises(capi.ThcError) as e:
         gpu_ctx_fp64.qrcp(s.phi, s.ng + 1)
     assert e.value.status == capi.THC_ERR_ARG
+
+
+@pytest.mark.parametrize("name,npts", [("tiny", 48), ("c2", 256)])
+def test_qrcp_complex(gpu_ctx_fp64, name, npts):
+    """thc_qrcp_complex against the oracle's Gram form for complex orbitals Phi A: the same
+    pivots and |R_kk| (Phi A has no symmetry-equivalent points)."""
+    from tests.test_oracle import complex_orbitals
+    s = system(name)
+    pc = complex_orbitals(s.phi)
+    r = gpu_ctx_fp64.qrcp(pc, npts)
+    ref = oracle.qrcp_gram(pc, npts)
+    assert np.max(np.abs(r["diag"] - ref["diag"])) <= 1e-10 * ref["diag"][0]
+    assert np.array_equal(r["order"], ref["order"])
+    assert np.array_equal(r["idx"], ref["idx"])

@@ -294,3 +294,14 @@ def test_isdf_complex_forms_agree():
     x = oracle.isdf_real(s.phi @ u, km.idx, s.mesh, s.coulG)
     r = oracle.isdf_real(s.phi, km.idx, s.mesh, s.coulG)
     assert np.linalg.norm(x["M"] - r["M"]) / np.linalg.norm(r["M"]) < 1e-7
+
+
+def test_qrcp_complex_forms_agree():
+    """Complex orbitals: Householder QRCP of the rows conj(phi_i) phi_k against the pivoted
+    Cholesky of |Phi^H Phi|^2."""
+    s = synth.config("tiny")
+    pc = complex_orbitals(s.phi)
+    a = oracle.qrcp_reference(pc, 48)
+    b = oracle.qrcp_gram(pc, 48)
+    assert np.array_equal(a["order"], b["order"])
+    assert np.max(np.abs(a["diag"] - b["diag"])) <= 1e-10 * a["diag"][0]

@@ -35,6 +35,7 @@ EXPORTS = [
     "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
     "thc_kmeans_history", "thc_factorize_batched", "thc_kmeans_noalloc",
     "thc_synth_gaussian_basis", "thc_isdf_half", "thc_qrcp", "thc_isdf_complex",
+    "thc_qrcp_complex",
 ]
 
 
@@ -123,10 +124,11 @@ def load(build_if_missing: bool = False):
     lib.thc_isdf_half.argtypes = [vp, vp, cll, ci, vp, ci, vp, ci, vp, vp, cd, vp, vp, vp,
                                   ctypes.POINTER(IsdfStats)]
     lib.thc_isdf_complex.argtypes = lib.thc_isdf.argtypes
+    lib.thc_qrcp_complex.argtypes = [vp, vp, cll, ci, ci, vp, vp, vp, ctypes.POINTER(QrcpStats)]
     lib.thc_qrcp.argtypes = [vp, vp, cll, ci, vp, ci, ci, vp, vp, vp, ctypes.POINTER(QrcpStats)]
     for f in ("thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
               "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_kmeans_noalloc",
-              "thc_isdf_half", "thc_qrcp", "thc_isdf_complex"):
+              "thc_isdf_half", "thc_qrcp", "thc_isdf_complex", "thc_qrcp_complex"):
         getattr(lib, f).restype = ci
     _lib = lib
     return lib
@@ -307,8 +309,15 @@ class Context:
         order = np.zeros(npts, np.int32)
         diag = np.zeros(npts)
         stats = QrcpStats()
-        st = self.lib.thc_qrcp(self.h, _ptr(phi), ng, no, _ptr(phi_occ), nocc, int(npts),
-                               _ptr(idx), _ptr(order), _ptr(diag), ctypes.byref(stats))
+        if np.iscomplexobj(phi):
+            if phi_occ is not None:
+                raise ValueError("the half-rotated QRCP takes real orbitals")
+            pr = np.ascontiguousarray(phi).view(np.float64)
+            st = self.lib.thc_qrcp_complex(self.h, _ptr(pr), ng, no, int(npts), _ptr(idx),
+                                           _ptr(order), _ptr(diag), ctypes.byref(stats))
+        else:
+            st = self.lib.thc_qrcp(self.h, _ptr(phi), ng, no, _ptr(phi_occ), nocc, int(npts),
+                                   _ptr(idx), _ptr(order), _ptr(diag), ctypes.byref(stats))
         self._check(st, "thc_qrcp")
         return dict(idx=idx, order=order, diag=diag, stats=stats)
 

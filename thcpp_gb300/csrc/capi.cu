@@ -387,6 +387,16 @@ int thc_qrcp(thc_ctx* h, const double* phi, long long ng, int norb, const double
                        stats);
 }
 
+int thc_qrcp_complex(thc_ctx* h, const double* phi, long long ng, int norb, int npts,
+                     int* out_idx, int* out_order, double* out_diag, thc_qrcp_stats* stats)
+{
+  if (!h) return THC_ERR_ARG;
+  if (cudaSetDevice(h->c.device) != cudaSuccess) return THC_ERR_CUDA;
+  if (stats) memset(stats, 0, sizeof(*stats));
+  return thc::qrcp_run(&h->c, phi, ng, norb, nullptr, 0, npts, out_idx, out_order, out_diag,
+                       stats, true);
+}
+
 namespace {
 std::mutex g_pool_mu;
 std::map<std::pair<int, int>, std::vector<thc_ctx*>> g_pool;

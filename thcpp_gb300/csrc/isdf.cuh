@@ -55,6 +55,7 @@ int kmeans_run(Ctx* c, const double* grid, const double* rho, long long ng, int 
 int kmeans_history(Ctx* c, double* diff, double* pct, int n);
 
 int qrcp_run(Ctx* c, const double* phi, long long ng, int no, const double* phi_occ, int nocc,
-             int npts, int* out_idx, int* out_order, double* out_diag, thc_qrcp_stats* stats);
+             int npts, int* out_idx, int* out_order, double* out_diag, thc_qrcp_stats* stats,
+             bool complex_orbitals = false);
 
 }  // namespace thc

@@ -49,6 +49,7 @@ struct QrGeom {
   long long ng;
   int no, nocc, kmin;    // kmin: orbitals in the P_min factor; 0 = every pair
   int ppb;               // points per block (the grid is a multiple of the SM count)
+  int cplx;              // complex orbitals: rows 2k / 2k + 1 of phi hold Re / Im phi_k
 };
 
 // dst[i * n + a] = src[a * m + i] for a < n, i < m.
@@ -135,6 +136,18 @@ __device__ __forceinline__ double gram(const QrGeom& g, long long a, const doubl
                                        const double* op, long long ps)
 {
   const double* ra = g.phi + a;
+  if (g.cplx) {
+    // Complex Z^T rows conj(phi_i) phi_k: G(a, b) = |P(a, b)|^2, P(a, b) = sum_k
+    // conj(phi_k(a)) phi_k(b) (real and imaginary parts accumulated separately).
+    double re = 0.0, im = 0.0;
+    for (int k = 0; k < g.no; k++) {
+      const double xr = ra[(2 * k) * g.ng], xi = ra[(2 * k + 1) * g.ng];
+      const double yr = pp[(2 * k) * ps], yi = pp[(2 * k + 1) * ps];
+      re = fma(xr, yr, fma(xi, yi, re));
+      im = fma(xr, yi, fma(-xi, yr, im));
+    }
+    return fma(re, re, im * im);
+  }
   double g3 = 0.0, gmin = 0.0;
   for (int k = 0; k < g.no; k++) {
     if (k == g.kmin) gmin = g3;
@@ -172,13 +185,14 @@ qrcp_step_kernel(QrGeom g, double* __restrict__ L, double* __restrict__ d, int k
                  QrPiv* blk, unsigned* ticket, int* piv, double* dpiv)
 {
   extern __shared__ double sh[];
+  const int kw = g.cplx ? 2 * g.no : g.no;
   double* pp = sh;
-  double* op = pp + g.no;
+  double* op = pp + kw;
   double* lp = op + g.nocc;
   const int p = piv[k];
   const double dp = dpiv[k];
   const long long ng = g.ng;
-  for (int i = threadIdx.x; i < g.no; i += kQrThreads) pp[i] = g.phi[(long long)i * ng + p];
+  for (int i = threadIdx.x; i < kw; i += kQrThreads) pp[i] = g.phi[(long long)i * ng + p];
   if (g.occ)
     for (int i = threadIdx.x; i < g.nocc; i += kQrThreads)
       op[i] = g.occ[(long long)i * ng + p];
@@ -234,20 +248,22 @@ qrcp_step_kernel(QrGeom g, double* __restrict__ L, double* __restrict__ d, int k
 }  // namespace
 
 int qrcp_run(Ctx* c, const double* phi_in, long long ng, int no, const double* occ_in, int nocc,
-             int npts, int* out_idx, int* out_order, double* out_diag, thc_qrcp_stats* stats)
+             int npts, int* out_idx, int* out_order, double* out_diag, thc_qrcp_stats* stats,
+             bool cplx)
 {
   if (!phi_in || !out_idx || ng <= 0 || no <= 0 || npts <= 0 || npts > ng ||
-      (occ_in && nocc <= 0))
+      (occ_in && nocc <= 0) || (occ_in && cplx))
     return set_error(c, THC_ERR_ARG, "thc_qrcp: invalid arguments");
+  const int kw = cplx ? 2 * no : no;   // doubles per point
   if (ng > 0x7ffffffeLL)
     return set_error(c, THC_ERR_SHAPE, "thc_qrcp: N_g %lld exceeds the 32-bit index range", ng);
-  const size_t shmem = sizeof(double) * ((size_t)no + (occ_in ? nocc : 0) + npts);
+  const size_t shmem = sizeof(double) * ((size_t)kw + (occ_in ? nocc : 0) + npts);
   if (shmem > 200 * 1024)
     return set_error(c, THC_ERR_SHAPE, "thc_qrcp: N_o + N_occ + points = %zu values exceed the "
                      "200 KB pivot buffer", shmem / sizeof(double));
   cudaStream_t s = c->stream;
   int st = 0;
-  const double* phi = (const double*)to_device(c, phi_in, sizeof(double) * ng * no, WS_PHI, &st);
+  const double* phi = (const double*)to_device(c, phi_in, sizeof(double) * ng * kw, WS_PHI, &st);
   if (st) return st;
   const double* occ = nullptr;
   if (occ_in) {
@@ -264,14 +280,14 @@ int qrcp_run(Ctx* c, const double* phi_in, long long ng, int no, const double* o
   // L (npts x N_g), the transposed orbitals ((N_o + N_occ) x N_g), d (N_g), block
   // candidates, pivots and their residuals, ticket.
   const size_t l_bytes = sizeof(double) * (size_t)npts * ng;
-  const size_t t_bytes = sizeof(double) * (size_t)(no + nt) * ng;
+  const size_t t_bytes = sizeof(double) * (size_t)(kw + nt) * ng;
   const size_t bytes = l_bytes + t_bytes + sizeof(double) * ng + sizeof(QrPiv) * nblk +
                        (sizeof(int) + sizeof(double)) * npts + 1024;
   char* base = (char*)ws_get(c, WS_ZT, bytes);
   if (!base) return set_error(c, THC_ERR_NOMEM, "thc_qrcp: workspace allocation failed");
   double* L = (double*)base;
   double* phit = L + (size_t)npts * ng;
-  double* occt = phit + (size_t)no * ng;
+  double* occt = phit + (size_t)kw * ng;
   double* d = occt + (size_t)nt * ng;
   QrPiv* blk = (QrPiv*)(d + ng);
   double* dpiv = (double*)(blk + nblk);
@@ -284,6 +300,7 @@ int qrcp_run(Ctx* c, const double* phi_in, long long ng, int no, const double* o
   g.no = no;
   g.nocc = nt;
   g.ppb = ppb;
+  g.cplx = cplx ? 1 : 0;
   g.kmin = occ ? (c->qrcp_all_pairs ? 0 : std::min(nocc, no)) : no;
   THC_CUDA(c, cudaFuncSetAttribute(qrcp_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)shmem));
@@ -292,7 +309,7 @@ int qrcp_run(Ctx* c, const double* phi_in, long long ng, int no, const double* o
   {
     ProfScope ps(c, "qrcp_init");
     const dim3 tb(32, 8);
-    transpose_rows<<<dim3((unsigned)cdiv(ng, 32), (unsigned)cdiv(no, 32)), tb, 0, s>>>(phi, ng, no,
+    transpose_rows<<<dim3((unsigned)cdiv(ng, 32), (unsigned)cdiv(kw, 32)), tb, 0, s>>>(phi, ng, kw,
                                                                                      phit);
     if (occ)
       transpose_rows<<<dim3((unsigned)cdiv(ng, 32), (unsigned)cdiv(nt, 32)), tb, 0, s>>>(

@@ -37,24 +37,28 @@ QRCPSolver::QRCPSolver(nlohmann::json& input, ContextHandler::BlacsHandler& BH)
 QRCPSolver::~QRCPSolver() {}
 
 namespace {
-// Real parts of a complex (N_g, n) orbital dataset.
-std::vector<double> read_real(h5lite::Reader& f, const char* name, long long& rows, int& cols)
+// A complex (N_g, n) orbital dataset: its real parts, or its (re, im) pairs when an
+// imaginary part is non-zero and complex data are allowed (*is_complex set).
+std::vector<double> read_orbitals(h5lite::Reader& f, const char* name, long long& rows,
+                                  int& cols, bool allow_complex, bool* is_complex)
 {
   std::vector<uint64_t> dims;
   std::vector<double> c = f.read_c128(name, &dims);
   rows = (long long)dims[0];
   cols = (int)dims[1];
-  std::vector<double> out((size_t)rows * cols);
   double max_im = 0.0;
-  for (size_t i = 0; i < out.size(); i++) {
-    out[i] = c[2 * i];
-    max_im = std::max(max_im, std::fabs(c[2 * i + 1]));
+  for (size_t i = 0; i < (size_t)rows * cols; i++) max_im = std::max(max_im, std::fabs(c[2 * i + 1]));
+  if (max_im != 0.0 && allow_complex) {
+    *is_complex = true;
+    return c;
   }
   if (max_im != 0.0) {
     std::cerr << " * ERROR: " << name << " has a non-zero imaginary part (max " << max_im
-              << "); complex orbitals are not part of the GPU build yet." << std::endl;
+              << "); the half-rotated QRCP takes real orbitals." << std::endl;
     exit(1);
   }
+  std::vector<double> out((size_t)rows * cols);
+  for (size_t i = 0; i < out.size(); i++) out[i] = c[2 * i];
   return out;
 }
 }  // namespace
@@ -67,11 +71,12 @@ void QRCPSolver::kernel(ContextHandler::BlacsHandler& BH, std::vector<int>& inte
   h5lite::Reader f(input_file);
   long long ng = 0, ng_occ = 0;
   int nbasis = 0, nelec = 0;
-  std::vector<double> phi = read_real(f, "aoR", ng, nbasis);
+  bool cplx = false, unused = false;
+  std::vector<double> phi = read_orbitals(f, "aoR", ng, nbasis, !half_rotate, &cplx);
   std::vector<double> occ;
   std::cout << " * Constructing Z matrix." << std::endl;
   if (half_rotate) {
-    occ = read_real(f, "aoR_half", ng_occ, nelec);
+    occ = read_orbitals(f, "aoR_half", ng_occ, nelec, false, &unused);
     if (ng_occ != ng) {
       std::cerr << " * ERROR: aoR_half has " << ng_occ << " grid points, aoR " << ng << std::endl;
       exit(1);
@@ -87,9 +92,12 @@ void QRCPSolver::kernel(ContextHandler::BlacsHandler& BH, std::vector<int>& inte
   interp_indxs.resize(num_interp_pts);
   std::vector<double> diag(num_interp_pts);
   thc_qrcp_stats st;
-  int status = thc_qrcp(thc_host::context(), phi.data(), ng, nbasis,
-                        half_rotate ? occ.data() : nullptr, nelec, num_interp_pts,
-                        interp_indxs.data(), nullptr, diag.data(), &st);
+  int status = cplx ? thc_qrcp_complex(thc_host::context(), phi.data(), ng, nbasis,
+                                        num_interp_pts, interp_indxs.data(), nullptr,
+                                        diag.data(), &st)
+                    : thc_qrcp(thc_host::context(), phi.data(), ng, nbasis,
+                               half_rotate ? occ.data() : nullptr, nelec, num_interp_pts,
+                               interp_indxs.data(), nullptr, diag.data(), &st);
   thc_host::check(status, "QRCP");
   double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   std::cout << "  * Time for QRCP: " << secs << " seconds (numerical rank " << st.numerical_rank
