@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "common.cuh"
@@ -192,6 +193,15 @@ qrcp_step_kernel(QrGeom g, double* __restrict__ L, double* __restrict__ d, int k
   const int p = piv[k];
   const double dp = dpiv[k];
   const long long ng = g.ng;
+  if (p < 0 || p >= ng) {
+    // No valid pivot (every candidate residual was NaN): pass the marker on without
+    // touching memory; the host reports the step.
+    if (k + 1 < npts && blockIdx.x == 0 && threadIdx.x == 0) {
+      piv[k + 1] = p;
+      dpiv[k + 1] = -INFINITY;
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < kw; i += kQrThreads) pp[i] = g.phi[(long long)i * ng + p];
   if (g.occ)
     for (int i = threadIdx.x; i < g.nocc; i += kQrThreads)
@@ -336,15 +346,26 @@ int qrcp_run(Ctx* c, const double* phi_in, long long ng, int no, const double* o
   int rank = npts;
   for (int k = 0; k < npts; k++) {
     if (order[k] < 0 || order[k] >= ng)
-      return set_error(c, THC_ERR_CUDA, "thc_qrcp: pivot %d out of range at step %d", order[k], k);
+      return set_error(c, THC_ERR_ARG, "thc_qrcp: no finite residual at step %d (NaN or "
+                       "infinite orbital values?)", k);
     dv[k] = std::sqrt(std::max(dv[k], 0.0));
     if (rank == npts && !(dv[k] > 1e-7 * dv[0])) rank = k;
   }
-  if (out_order) std::copy(order.begin(), order.end(), out_order);
-  if (out_diag) std::copy(dv.begin(), dv.end(), out_diag);
   std::vector<int> idx(order);
   std::sort(idx.begin(), idx.end());
-  std::copy(idx.begin(), idx.end(), out_idx);
+  // Outputs may live on the host or on the device.
+  auto put = [&](void* dst, const void* src, size_t bytes) -> int {
+    if (!dst) return 0;
+    if (is_device_ptr(dst)) {
+      THC_CUDA(c, cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    } else {
+      std::memcpy(dst, src, bytes);
+    }
+    return 0;
+  };
+  if ((st = put(out_order, order.data(), sizeof(int) * npts))) return st;
+  if ((st = put(out_diag, dv.data(), sizeof(double) * npts))) return st;
+  if ((st = put(out_idx, idx.data(), sizeof(int) * npts))) return st;
   if (stats) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
