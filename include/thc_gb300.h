@@ -20,10 +20,10 @@
  *                               setup_pseudo_dm/setup_CZt (:59-141), setup_CCt (:163-190),
  *                               least_squares (:416), fft_vectors (:331-404),
  *                               construct_muv (:247-281), dump_thc_data's Cholesky (:283-315)
- *   thc_qrcp_complex            the same for complex aoR
  *   thc_qrcp                    QRCP::QRCPSolver::kernel (src/qrcp.cpp:100-173): setup_Z_matrix /
  *                               setup_Z_half_matrix (:34-67), pzgeqpf (matrix_operations.h:
  *                               757-790), the first thc_cfac * N_o pivots sorted (:149-160)
+ *   thc_qrcp_complex            thc_qrcp for complex aoR
  *   thc_isdf_complex            the same for complex aoR (P = Phi_mu^H Phi, :117; Z = P o conj(P))
  *   thc_isdf_half               IVecs with rotate = true (src/interpolating_vectors.cpp:45-49):
  *                               setup_CZt_half (:143-161), the IVMG product of

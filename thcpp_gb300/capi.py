@@ -146,6 +146,28 @@ def _ptr(a):
     raise TypeError(f"unsupported array type {type(a)}")
 
 
+def _is_complex(a) -> bool:
+    """Whether ``a`` holds complex values, without converting it (device tensors stay put)."""
+    if hasattr(a, "is_complex"):
+        return bool(a.is_complex())
+    return bool(np.iscomplexobj(a))
+
+
+def _complex_pairs(a):
+    """A complex array as its (re, im) float64 pairs, shape ``a.shape + (2,)``.
+
+    Tensors (any device) go through ``torch.view_as_real`` and keep their device; numpy
+    arrays through a float64 view.
+    """
+    if hasattr(a, "is_complex"):
+        import torch
+        if a.dtype != torch.complex128:
+            raise TypeError(f"complex orbitals must be complex128, not {a.dtype}")
+        return torch.view_as_real(a.contiguous())
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    return a.view(np.float64).reshape(a.shape + (2,))
+
+
 def factorize_batched(systems, device=0, precision=THC_PREC_MIXED, nstreams=8):
     """Run thc_factorize_batched on a list of dicts with the thc_system fields.
 
@@ -285,8 +307,8 @@ class Context:
 
     def isdf_complex(self, phi, idx, mesh, coulG, shift_rel=-1.0):
         """thc_isdf_complex: ``phi`` complex128 (N_g, N_o) or float64 (N_g, N_o, 2)."""
-        if np.iscomplexobj(phi):
-            phi = np.ascontiguousarray(phi).view(np.float64).reshape(phi.shape + (2,))
+        if _is_complex(phi):
+            phi = _complex_pairs(phi)
         ng, no = int(phi.shape[0]), int(phi.shape[1])
         nmu = int(idx.shape[0])
         mesh_a = np.ascontiguousarray(np.asarray(mesh, dtype=np.int32).reshape(3))
@@ -309,10 +331,10 @@ class Context:
         order = np.zeros(npts, np.int32)
         diag = np.zeros(npts)
         stats = QrcpStats()
-        if np.iscomplexobj(phi):
+        if _is_complex(phi):
             if phi_occ is not None:
                 raise ValueError("the half-rotated QRCP takes real orbitals")
-            pr = np.ascontiguousarray(phi).view(np.float64)
+            pr = _complex_pairs(phi)
             st = self.lib.thc_qrcp_complex(self.h, _ptr(pr), ng, no, int(npts), _ptr(idx),
                                            _ptr(order), _ptr(diag), ctypes.byref(stats))
         else:

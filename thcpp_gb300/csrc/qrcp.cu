@@ -353,19 +353,30 @@ int qrcp_run(Ctx* c, const double* phi_in, long long ng, int no, const double* o
   }
   std::vector<int> idx(order);
   std::sort(idx.begin(), idx.end());
-  // Outputs may live on the host or on the device.
+  // Outputs may live on the host or on the device.  Device outputs are written on the
+  // context's stream (work the caller queues there afterwards sees them), and the stream
+  // is drained before the pageable host vectors go out of scope.
+  bool any_dev = false;
   auto put = [&](void* dst, const void* src, size_t bytes) -> int {
     if (!dst) return 0;
     if (is_device_ptr(dst)) {
-      THC_CUDA(c, cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+      THC_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+      any_dev = true;
     } else {
       std::memcpy(dst, src, bytes);
     }
     return 0;
   };
-  if ((st = put(out_order, order.data(), sizeof(int) * npts))) return st;
-  if ((st = put(out_diag, dv.data(), sizeof(double) * npts))) return st;
-  if ((st = put(out_idx, idx.data(), sizeof(int) * npts))) return st;
+  st = put(out_order, order.data(), sizeof(int) * npts);
+  if (!st) st = put(out_diag, dv.data(), sizeof(double) * npts);
+  if (!st) st = put(out_idx, idx.data(), sizeof(int) * npts);
+  if (any_dev) {
+    // Also after a failed copy: an earlier one may still read the host vectors.
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (!st && e != cudaSuccess)
+      st = set_error(c, THC_ERR_CUDA, "thc_qrcp: output copy: %s", cudaGetErrorString(e));
+  }
+  if (st) return st;
   if (stats) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
