@@ -25,6 +25,8 @@
  *                               757-790), the first thc_cfac * N_o pivots sorted (:149-160)
  *   thc_qrcp_complex            thc_qrcp for complex aoR
  *   thc_isdf_complex            the same for complex aoR (P = Phi_mu^H Phi, :117; Z = P o conj(P))
+ *   thc_isdf_interpolating_vectors  the least-squares solution zeta of the last ISDF call
+ *                               (interpolating_vectors.cpp:416)
  *   thc_isdf_half               IVecs with rotate = true (src/interpolating_vectors.cpp:45-49):
  *                               setup_CZt_half (:143-161), the IVMG product of
  *                               construct_muv (:271-273), dump_thc_data's Muv (:317-328)
@@ -218,6 +220,18 @@ int thc_isdf_half(thc_ctx* ctx, const double* phi, long long ng, int norb, const
                   int nocc, const int* idx, int nmu, const int* mesh, const double* coulG,
                   double shift_rel, double* out_orbitals, double* out_occ_orbitals,
                   double* out_M, thc_isdf_stats* stats);
+
+/*
+ * The interpolating vectors of the last thc_isdf / thc_isdf_complex / thc_isdf_half call on
+ * this context: out_zeta (nmu x ng doubles, host or device; row mu is zeta_mu on the grid,
+ * in grid order) receives the solution of the least-squares problem C zeta^T = Z^T
+ * (IVecs::kernel's least_squares, src/interpolating_vectors.cpp:416, whose result the
+ * reference keeps in CZt before fft_vectors, :331-404).  The mixed path keeps them in FP32
+ * (its FFT input); they are widened to FP64.  ng / nmu must be the last call's sizes
+ * (THC_ERR_SHAPE otherwise); THC_ERR_ARG when the context holds no such result (no ISDF call
+ * yet, or a later QRCP or failed ISDF call reused the workspace).
+ */
+int thc_isdf_interpolating_vectors(thc_ctx* ctx, long long ng, int nmu, double* out_zeta);
 
 /*
  * Interpolating points by QR with column pivoting of Z^T (the reference's "qrcp" point

@@ -16,14 +16,19 @@ Contents
                        literal Z^T + pivoted Householder QR, and the pivoted Cholesky of
                        Z Z^T that the CUDA path implements.
 
+``reference.py``       runs the reference's OWN ``src/kmeans.cpp``, compiled unmodified by
+                       ``ref/Makefile`` into ``_ref/kmeans_ref`` (one-rank MPI stand-in,
+                       in-memory datasets in place of the HDF5 file).
+
 Parity pinning
 --------------
-The reference's own tests hold no golden vector for this path (its Catch2 tests cover
-only real ``d``-routines and the molecular LS-THC path), and the reference cannot be
-built here (MPI, BLACS/ScaLAPACK, FFTW3 and the HDF5 C++ API are absent), so parity is
-pinned by known-answer tests written for this project (constructed k-means ties,
-delta/plane-wave FFTs, analytic Gaussian Coulomb integrals, L L^T = M) and by
-cross-checking the two oracle formulations against each other.
+k-means is pinned to the reference itself: ``reference.py`` runs its ``KMeansSolver`` and
+the tests compare the restatement (and the GPU) with it, live where the reference tree is
+present and through fixtures it generated (``tests/golden/ref_kmeans.npz``) elsewhere.
+The ISDF half needs MPI, BLACS/ScaLAPACK, FFTW3 and the HDF5 C++ API, none of which is
+installed, so it cannot be built; its restatement is pinned by known-answer tests written
+for this project (delta/plane-wave FFTs, analytic Gaussian Coulomb integrals, L L^T = M)
+and by cross-checking the two oracle formulations against each other.
 """
 
 from __future__ import annotations
@@ -64,7 +69,8 @@ def _load():
         lib.orc_initial_indices.restype = ci
         lib.orc_classify.argtypes = [vp, i64, vp, ci, vp, ci]
         lib.orc_classify.restype = None
-        lib.orc_kmeans.argtypes = [vp, vp, i64, ci, vp, ci, cd, ci, vp, vp, vp, vp, vp]
+        lib.orc_kmeans.argtypes = [vp, vp, i64, ci, vp, ci, cd, ci, vp, vp, vp, vp, vp, vp,
+                                   vp]
         lib.orc_kmeans.restype = ci
         lib.orc_num_threads.argtypes = []
         lib.orc_num_threads.restype = ci
@@ -96,13 +102,15 @@ def classify(grid: np.ndarray, centroids: np.ndarray, nthreads: int = 0) -> np.n
 
 
 class KMeansResult:
-    def __init__(self, status, idx, iters, diff, centroids, labels):
+    def __init__(self, status, idx, iters, diff, centroids, labels, diffs=None, pct=None):
         self.status = status
         self.idx = idx
         self.iters = iters
         self.diff = diff
         self.centroids = centroids
         self.labels = labels
+        self.diffs = diffs      # normed difference of every completed iteration
+        self.pct = pct          # percentage_change of every completed iteration
 
 
 def kmeans(grid, rho, nmu, init_idx, max_it, threshold, nthreads: int = 0) -> KMeansResult:
@@ -116,10 +124,13 @@ def kmeans(grid, rho, nmu, init_idx, max_it, threshold, nthreads: int = 0) -> KM
     labels = np.zeros(ng, np.int32)
     iters = ctypes.c_int()
     diff = ctypes.c_double()
+    diffs = np.zeros(max_it)
+    pct = np.zeros(max_it)
     st = _load().orc_kmeans(_p(g), _p(r), ng, nmu, _p(init), max_it, threshold,
                             nthreads or os.cpu_count() or 1, _p(idx), ctypes.byref(iters),
-                            ctypes.byref(diff), _p(cen), _p(labels))
-    return KMeansResult(st, idx, iters.value, diff.value, cen, labels)
+                            ctypes.byref(diff), _p(cen), _p(labels), _p(diffs), _p(pct))
+    n = iters.value
+    return KMeansResult(st, idx, n, diff.value, cen, labels, diffs[:n], pct[:n])
 
 
 def kmeans_system(system, nthreads: int = 0) -> KMeansResult:

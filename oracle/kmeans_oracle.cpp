@@ -101,11 +101,13 @@ void orc_classify(const double* grid, int64_t ng, const double* cen, int nmu, in
 //   status: 0 ok, 2 empty cluster (the reference exits), 3 bad argument.
 //   out_idx receives the sorted interpolating indices; out_iters the number of
 //   completed iterations; out_diff the last normed difference; out_centroids (nmu x 3)
-//   the centroids handed to map_to_grid; out_labels (optional) the last labels.
+//   the centroids handed to map_to_grid; out_labels (optional) the last labels;
+//   out_diffs / out_pct (optional, max_it each) every iteration's normed difference and
+//   percentage_change (src/kmeans.cpp:177-185, :236-237).
 int orc_kmeans(const double* grid, const double* rho, int64_t ng, int nmu,
                const int* init_idx, int max_it, double threshold, int nthreads,
                int* out_idx, int* out_iters, double* out_diff, double* out_centroids,
-               int* out_labels)
+               int* out_labels, double* out_diffs, double* out_pct)
 {
   if (ng <= 0 || nmu <= 0 || nmu > ng || max_it < 1) return 3;
   std::vector<double> cur(3 * (size_t)nmu), nxt(3 * (size_t)nmu);
@@ -142,6 +144,13 @@ int orc_kmeans(const double* grid, const double* rho, int64_t ng, int nmu,
       return 2;
     }
     diff = normed_difference(nxt, cur);
+    if (out_diffs) out_diffs[it] = diff;
+    if (out_pct) {
+      // percentage_change: labels of this iteration against the previous one's.
+      int64_t changed = 0;
+      for (int64_t i = 0; i < ng; i++) changed += map[i] != old_map[i];
+      out_pct[it] = 100 * ((double)changed) / ng;
+    }
     if (diff < threshold) {
       converged = true;
       break;

@@ -66,3 +66,40 @@ def rounding_stress_grid(seed: int = 11):
     grid = grid + rng.integers(-3, 4, size=grid.shape) * 2.0 ** -4
     rho = 1.0 + rng.integers(0, 2 ** 40, size=grid.shape[0]).astype(np.float64) * 2.0 ** -40
     return np.ascontiguousarray(grid), rho
+
+
+def limit_case():
+    """k-means at the size limits of thc_kmeans_noalloc: N_g = 65,536 (a 64 x 32 x 32 mesh
+    of the 8-atom diamond cell), N_mu = 1,024, max_it = 1,000, threshold 1e-6.
+
+    The weight is a sum of Gaussians exp(-0.6 |r - R|^2) over the atoms and their nearest
+    periodic images, so every region of the cell carries weight and no cluster empties.
+    Returns (grid, rho, nmu, max_it, threshold, rng_seed).
+    """
+    from thcpp_gb300 import synth
+    a = synth.A_DIAMOND
+    lattice = np.eye(3) * a
+    grid = synth.uniform_grid(lattice, (64, 32, 32))
+    atoms = synth._DIAMOND_FRAC @ lattice
+    shifts = np.array([[i, j, k] for i in (-1, 0, 1) for j in (-1, 0, 1) for k in (-1, 0, 1)],
+                      dtype=np.float64) @ lattice
+    rho = np.zeros(grid.shape[0])
+    for at in atoms:
+        for sh in shifts:
+            d = grid - (at + sh)
+            rho += np.exp(-0.6 * np.einsum("ij,ij->i", d, d))
+    return np.ascontiguousarray(grid), rho, 1024, 1000, 1e-6, 29
+
+
+def ref_case_inputs(name):
+    """(grid, rho, norb, thc_cfac, max_it, threshold, rng_seed) of a case of the reference
+    k-means fixtures (tests/golden/make_ref_golden.py): a synthetic system by name, c4_<s>
+    for system s of the batch, ``limit`` (:func:`limit_case`) and ``limit_full`` (the same
+    with a negative threshold, so that every one of the 1,000 iterations runs)."""
+    from thcpp_gb300 import synth
+    from tests.conftest import system
+    if name.startswith("limit"):
+        g, r, nmu, mi, th, seed = limit_case()
+        return g, r, nmu // 8, 8, mi, (th if name == "limit" else -1.0), seed
+    s = synth.c4_system(int(name[3:])) if name.startswith("c4_") else system(name)
+    return s.grid, s.density, s.norb, s.thc_cfac, s.max_it, s.threshold, s.rng_seed

@@ -64,7 +64,17 @@ def test_orbital_file_contract(tmp_path):
     assert r.info("aoR_half")[1] == (s.ng, s.nocc)
 
 
-REF_FIXTURE = "/root/reference/tests/data/eri_thc.h5"
+def _reference_fixture():
+    """The reference tree's HDF5 fixture (tests/data/eri_thc.h5), where the tree is present;
+    its location is the one the reference build recipe (oracle/ref/Makefile) compiles from."""
+    from oracle import reference
+    try:
+        return os.path.join(reference.reference_dir(), "tests", "data", "eri_thc.h5")
+    except Exception:
+        return ""
+
+
+REF_FIXTURE = _reference_fixture()
 
 
 @pytest.mark.skipif(not os.path.exists(REF_FIXTURE), reason="reference fixture not present")

@@ -35,7 +35,7 @@ EXPORTS = [
     "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
     "thc_kmeans_history", "thc_factorize_batched", "thc_kmeans_noalloc",
     "thc_synth_gaussian_basis", "thc_isdf_half", "thc_qrcp", "thc_isdf_complex",
-    "thc_qrcp_complex",
+    "thc_qrcp_complex", "thc_isdf_interpolating_vectors",
 ]
 
 
@@ -126,9 +126,11 @@ def load(build_if_missing: bool = False):
     lib.thc_isdf_complex.argtypes = lib.thc_isdf.argtypes
     lib.thc_qrcp_complex.argtypes = [vp, vp, cll, ci, ci, vp, vp, vp, ctypes.POINTER(QrcpStats)]
     lib.thc_qrcp.argtypes = [vp, vp, cll, ci, vp, ci, ci, vp, vp, vp, ctypes.POINTER(QrcpStats)]
+    lib.thc_isdf_interpolating_vectors.argtypes = [vp, cll, ci, vp]
     for f in ("thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
               "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_kmeans_noalloc",
-              "thc_isdf_half", "thc_qrcp", "thc_isdf_complex", "thc_qrcp_complex"):
+              "thc_isdf_half", "thc_qrcp", "thc_isdf_complex", "thc_qrcp_complex",
+              "thc_isdf_interpolating_vectors"):
         getattr(lib, f).restype = ci
     _lib = lib
     return lib
@@ -304,6 +306,16 @@ class Context:
         if raise_on_error and st not in (THC_OK, THC_ERR_NOT_PD):
             self._check(st, "thc_isdf")
         return dict(M=out_M, L=out_L, orbitals=out_orbitals, stats=stats, status=st)
+
+    def interpolating_vectors(self, ng, nmu, out=None):
+        """thc_isdf_interpolating_vectors: zeta^T (N_mu x N_g float64) of the last ISDF call;
+        into ``out`` (host array or device tensor) when given."""
+        if out is None:
+            out = np.zeros((nmu, ng))
+        self._check(self.lib.thc_isdf_interpolating_vectors(self.h, int(ng), int(nmu),
+                                                            _ptr(out)),
+                    "thc_isdf_interpolating_vectors")
+        return out
 
     def isdf_complex(self, phi, idx, mesh, coulG, shift_rel=-1.0):
         """thc_isdf_complex: ``phi`` complex128 (N_g, N_o) or float64 (N_g, N_o, 2)."""

@@ -140,6 +140,16 @@ static void clear_profile(Ctx* c)
 
 }  // namespace thc
 
+namespace {
+// out[i] = in[i] for FP32 interpolating vectors (grid-stride).
+__global__ void widen_f32(const float* __restrict__ in, long long n, double* __restrict__ out)
+{
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = (double)in[i];
+}
+}  // namespace
+
 extern "C" {
 
 const char* thc_status_string(int status)
@@ -374,6 +384,45 @@ int thc_isdf_half(thc_ctx* h, const double* phi, long long ng, int norb, const d
   if (stats) memset(stats, 0, sizeof(*stats));
   return thc::isdf_run(&h->c, phi, ng, norb, idx, nmu, mesh, coulG, shift_rel, out_orbitals,
                        out_M, nullptr, stats, phi_occ, nocc, out_occ_orbitals);
+}
+
+int thc_isdf_interpolating_vectors(thc_ctx* h, long long ng, int nmu, double* out_zeta)
+{
+  if (!h || !out_zeta) return THC_ERR_ARG;
+  thc::Ctx* c = &h->c;
+  if (cudaSetDevice(c->device) != cudaSuccess) return THC_ERR_CUDA;
+  if (!c->zeta_elem || !c->zeta_last)
+    return thc::set_error(c, THC_ERR_ARG, "thc_isdf_interpolating_vectors: no ISDF result on "
+                          "this context (none yet, or a later call reused its workspace)");
+  if (ng != c->zeta_ng || nmu != c->zeta_nmu)
+    return thc::set_error(c, THC_ERR_SHAPE, "thc_isdf_interpolating_vectors: the last ISDF "
+                          "call had N_g %lld, N_mu %d", c->zeta_ng, c->zeta_nmu);
+  const long long n = (long long)nmu * ng;
+  cudaStream_t s = c->stream;
+  if (c->zeta_elem == (int)sizeof(double)) {
+    THC_CUDA(c, cudaMemcpyAsync(out_zeta, c->zeta_last, sizeof(double) * n, cudaMemcpyDefault, s));
+  } else if (thc::is_device_ptr(out_zeta)) {
+    widen_f32<<<(unsigned)std::min<long long>(thc::cdiv(n, 256), 1 << 20), 256, 0, s>>>(
+        (const float*)c->zeta_last, n, out_zeta);
+    THC_LAUNCHED(c, "widen_f32");
+  } else {
+    // Host output: widen 32 Mi values at a time in a staging slot, then copy each chunk.
+    const long long chunk = 1LL << 25;
+    double* stage = (double*)thc::ws_get(c, thc::WS_OUT, sizeof(double) * std::min(n, chunk));
+    if (!stage) return thc::set_error(c, THC_ERR_NOMEM, "thc_isdf_interpolating_vectors: staging");
+    for (long long o = 0; o < n; o += chunk) {
+      const long long m = std::min(chunk, n - o);
+      widen_f32<<<(unsigned)std::min<long long>(thc::cdiv(m, 256), 1 << 20), 256, 0, s>>>(
+          (const float*)c->zeta_last + o, m, stage);
+      THC_LAUNCHED(c, "widen_f32");
+      THC_CUDA(c, cudaMemcpyAsync(out_zeta + o, stage, sizeof(double) * m,
+                                  cudaMemcpyDeviceToHost, s));
+      // The next chunk reuses the staging slot: wait for this copy.
+      THC_CUDA(c, cudaStreamSynchronize(s));
+    }
+  }
+  THC_CUDA(c, cudaStreamSynchronize(s));
+  return THC_OK;
 }
 
 int thc_qrcp(thc_ctx* h, const double* phi, long long ng, int norb, const double* phi_occ,

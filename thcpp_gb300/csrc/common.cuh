@@ -99,6 +99,13 @@ struct Ctx {
   // Instantiated k-means iteration graphs, most recently used last, keyed by every kernel
   // argument they bake in.
   std::vector<std::pair<std::vector<long long>, cudaGraphExec_t>> km_graphs;
+  // Interpolating vectors zeta^T (N_mu x N_g, row mu = zeta_mu on the grid) of the last
+  // ISDF call, where they stay in the workspace until the next call: element size 8 (FP64)
+  // or 4 (FP32, the mixed path's R2C input); zeta_elem = 0 when there are none.
+  const void* zeta_last = nullptr;
+  int zeta_elem = 0;
+  long long zeta_ng = 0;
+  int zeta_nmu = 0;
   std::string last_error;
   // History of the last k-means run (device buffer WS_KM_LOG: diff[max_it], pct[max_it]).
   int km_last_iters = 0;

@@ -240,6 +240,7 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
              double* out_M, double* out_L, thc_isdf_stats* stats, const double* phiocc_in,
              int nocc, double* out_orb_occ, bool cplx)
 {
+  c->zeta_elem = 0;   // the workspace is about to be rewritten
   if (!phi_in || !idx_in || !mesh_in || !coul_in || ng <= 0 || no <= 0 || nmu <= 0 ||
       nmu > ng || (phiocc_in && nocc <= 0))
     return set_error(c, THC_ERR_ARG, "thc_isdf: invalid arguments");
@@ -543,6 +544,10 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
   THC_CUDA(c, cudaMemcpyAsync(&hshift, shift_dev, sizeof(double), cudaMemcpyDeviceToHost, s));
   THC_CUDA(c, cudaStreamSynchronize(s));
   if (hbad) return set_error(c, THC_ERR_ARG, "thc_isdf: interpolating index out of range");
+  c->zeta_last = zeta;
+  c->zeta_elem = sizeof(double);
+  c->zeta_ng = ng;
+  c->zeta_nmu = nmu;
   if (stats) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);

@@ -143,6 +143,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
                    int nmu, const int* mesh, const double* coul_in, double shift_rel,
                    double* out_orb, double* out_M, double* out_L, thc_isdf_stats* stats)
 {
+  c->zeta_elem = 0;   // the workspace is about to be rewritten
   cudaStream_t s = c->stream;
   int st = 0;
   const double* phi = (const double*)to_device(c, phi_in, sizeof(double) * ng * no, WS_PHI, &st);
@@ -425,6 +426,10 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   THC_CUDA(c, cudaStreamSynchronize(s));
   if (hbad) return set_error(c, THC_ERR_ARG, "thc_isdf: interpolating index out of range");
   if (herr) return set_error(c, THC_ERR_TIMEOUT, "thc_isdf: tensor-core GEMM wait timed out");
+  c->zeta_last = zeta;
+  c->zeta_elem = (int)real_sz;
+  c->zeta_ng = ng;
+  c->zeta_nmu = nmu;
   if (stats) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);

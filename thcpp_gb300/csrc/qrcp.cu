@@ -261,6 +261,7 @@ int qrcp_run(Ctx* c, const double* phi_in, long long ng, int no, const double* o
              int npts, int* out_idx, int* out_order, double* out_diag, thc_qrcp_stats* stats,
              bool cplx)
 {
+  c->zeta_elem = 0;   // L shares the workspace slot of Z and zeta
   if (!phi_in || !out_idx || ng <= 0 || no <= 0 || npts <= 0 || npts > ng ||
       (occ_in && nocc <= 0) || (occ_in && cplx))
     return set_error(c, THC_ERR_ARG, "thc_qrcp: invalid arguments");

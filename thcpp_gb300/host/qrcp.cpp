@@ -3,9 +3,9 @@
 // prints the reference's messages and |R_kk| lines (:100-173).  Differences: the pivots
 // come from a pivoted Cholesky factorisation of Z Z^T rather than Householder QR of Z^T
 // (the same pivots in exact arithmetic), |R_kk| is printed for the thc_cfac * N_o steps
-// taken rather than for all min(rows, N_g), and the indices are 0-based grid indices (the
-// reference passes pzgeqpf's 1-based IPIV values on unchanged, qrcp.cpp:137-157, and
-// IVecs then indexes the grid with them, matrix_operations.h:418-420).
+// taken rather than for all min(rows, N_g).  The indices are 0-based grid indices, as in
+// the reference (MatrixOperations::qrcp converts pzgeqpf's 1-based IPIV values with
+// add_constant(perm, -1), matrix_operations.h:785-786, before map_perm orders them).
 #include "qrcp.h"
 
 #include <chrono>
