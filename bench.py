@@ -252,6 +252,8 @@ def main():
                     help="c2 is the benchmark workload; c3 and c4 (batch) are reported separately")
     ap.add_argument("--c4-systems", type=int, default=48)
     ap.add_argument("--c4-streams", type=int, default=8)
+    ap.add_argument("--refine", type=int, default=None,
+                    help="refinement steps of the shifted solve (default: 1 for c5, else 0)")
     args = ap.parse_args()
     if args.workload == "c4" and args.impl != "reference":
         return run_c4(args)
@@ -281,6 +283,10 @@ def main():
         s = synth.config(WORKLOAD)
     nmu, ng, no = s.nmu, s.ng, s.norb
     init = capi.initial_indices(ng, nmu, s.rng_seed)
+    # The 216-atom cell's C is near rank-deficient by construction: its FP64 Cholesky always
+    # runs with the diagonal shift 1e-10 tr(C)/N_mu, followed by refinement of zeta.
+    shift_rel = 1e-10 if WORKLOAD == "c5" else -1.0
+    refine = args.refine if args.refine is not None else (1 if WORKLOAD == "c5" else 0)
 
     # Device-resident inputs.
     as_dev = (lambda a: a) if on_device else (lambda a: torch.from_numpy(a).to(dev))
@@ -301,12 +307,13 @@ def main():
         _, kst, st = ctx.kmeans(d_grid, d_rho, nmu, d_init, s.max_it, s.threshold, out_idx=d_idx)
         if st:
             raise RuntimeError(f"thc_kmeans status {st}")
-        r = ctx.isdf(d_phi, d_idx, s.mesh, d_coul, -1.0, out_orbitals=d_orb, out_M=d_M,
+        r = ctx.isdf(d_phi, d_idx, s.mesh, d_coul, shift_rel, out_orbitals=d_orb, out_M=d_M,
                      out_L=d_L)
         return kst, r
 
     def timed(ctx, steps, warmup):
         ctx.set_stream(stream.cuda_stream)
+        ctx.set_option("refine", refine)
         for _ in range(warmup):
             device_step(ctx)
         torch.cuda.synchronize()
@@ -340,7 +347,11 @@ def main():
     ms_mixed, launches, kst, r_mx = timed(ctx, args.steps, args.warmup)
     torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
+    torch.cuda.synchronize()
+    free_b, total_b = torch.cuda.mem_get_info()
+    mem_gb = (total_b - free_b) / 1e9      # inputs + the library's grow-only workspace
     M_mixed = d_M.cpu().numpy().copy()
+    isdf_st = r_mx["stats"]
     oz_ms, oz_n = ctx.kernel_time("ozgemm")
     km_ms, km_n = ctx.kernel_time("km_assign")
     # Device time per system of each stage of the timed steps (CUDA events the library
@@ -434,7 +445,8 @@ def main():
 
     def host_step():
         ctx.kmeans(h_grid, h_rho, nmu, h_init, s.max_it, s.threshold, out_idx=h_idx)
-        ctx.isdf(h_phi, h_idx, s.mesh, h_coul, -1.0, out_orbitals=h_orb, out_M=h_M, out_L=h_L)
+        ctx.isdf(h_phi, h_idx, s.mesh, h_coul, shift_rel, out_orbitals=h_orb, out_M=h_M,
+                 out_L=h_L)
 
     e2e = float("nan")
     if "e2e" in paths:
@@ -511,6 +523,14 @@ def main():
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "stage_ms_per_system": stage_ms,
         }
+        # Conditioning of C at the k-means points (side computation, after the timing).
+        pm = d_phi[d_idx.long()]
+        ev = torch.linalg.eigvalsh((pm @ pm.T) ** 2)
+        line["solve"] = {"cond_C": float(ev[-1] / ev[0]) if float(ev[0]) > 0 else None,
+                         "shift_rel": shift_rel if shift_rel > 0 else None,
+                         "shift_used": isdf_st.shift_used, "refine_steps": refine,
+                         "rank_deficient": int(isdf_st.rank_deficient)}
+        line["device_memory_gb"] = round(mem_gb, 2)
         if qrcp:
             line["qrcp"] = qrcp
         if leg_errors:

@@ -82,10 +82,11 @@ def half_spectrum_weights(coulG: np.ndarray, mesh):
 
 
 def isdf_real(phi: np.ndarray, idx: np.ndarray, mesh, coulG: np.ndarray, shift: float = 0.0,
-              workers=-1, fft_dtype=np.float64, phi_occ=None):
+              workers=-1, fft_dtype=np.float64, phi_occ=None, refine: int = 0):
     """Real-arithmetic formulation (the CUDA path's).  Returns dict(M, L, info, zeta, ...).
 
-    ``shift`` is added to the diagonal of C before the Cholesky factorisation.  Complex
+    ``shift`` is added to the diagonal of C before the Cholesky factorisation; ``refine``
+    steps of iterative refinement zeta <- zeta + (C + sI)^{-1} (Z^T - C zeta) follow.  Complex
     ``phi`` (k-point orbitals) gives Z = |Phi_mu^H Phi|^2, still real.  With
     ``phi_occ`` (N_g x N_occ) the half-rotated products Z = P_occ o P, C = Z[:, idx] replace
     P o P (C stays symmetric positive semi-definite: a Schur product of two Gram matrices).
@@ -121,6 +122,8 @@ def isdf_real(phi: np.ndarray, idx: np.ndarray, mesh, coulG: np.ndarray, shift: 
     Lc = np.linalg.cholesky(Cs)
     Cinv = sla.cho_solve((Lc, True), np.eye(C.shape[0]))
     zt = Cinv @ Zt                                      # zeta^T (N_mu, N_g)
+    for _ in range(refine):
+        zt = zt + Cinv @ (Zt - C @ zt)
     n0, n1, n2 = mesh
     zh = sfft.rfftn(zt.reshape(-1, n0, n1, n2).astype(fft_dtype), axes=(1, 2, 3),
                     workers=workers)

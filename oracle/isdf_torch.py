@@ -8,12 +8,13 @@ Cholesky, cuFFT D2Z through torch.fft) so that it reaches the sizes the CPU orac
 
 * C = (Phi_mu Phi_mu^T)^2 + shift I, its Cholesky factor L (one N_mu x N_mu FP64 solve);
 * zeta^T = C^{-1} Z^T by triangular solves with L, one block of grid points at a time,
-  Z^T of the block formed on the fly as (Phi_mu Phi_blk^T)^2: Z is never held whole;
+  Z^T of the block formed on the fly as (Phi_mu Phi_blk^T)^2: Z is never held whole; with a
+  shift, optional steps of literal iterative refinement zeta += (C + sI)^{-1}(Z^T - C zeta);
 * zeta_hat = D2Z FFT of the interpolating vectors, ``mu_block`` vectors at a time;
 * M = sum_half w [v_sym Re(a) + i v_anti Im(a)], a = conj(zeta_hat_mu) zeta_hat_nu, as one
   FP64 product over the scaled half spectra.
 
-It is checked against the CPU oracle on the smaller cells (``tests/test_gpu_oracle.py``).
+It is checked against the CPU oracle on the smaller cells (``tests/test_gpu_accuracy.py``).
 Only tests and the accuracy report under ``tests/`` use it.
 """
 
@@ -50,8 +51,11 @@ def half_spectrum_weights(coulG, mesh, device):
 
 
 def isdf_real(phi, idx, mesh, coulG, shift: float = 0.0, device="cuda:0",
-              grid_block: int = 1 << 16, mu_block: int = 256, keep_zeta: bool = True):
-    """FP64 ISDF on the GPU.  ``shift`` is added to C's diagonal (absolute).
+              grid_block: int = 1 << 16, mu_block: int = 256, keep_zeta: bool = True,
+              refine: int = 0, shift_rel: float | None = None):
+    """FP64 ISDF on the GPU.  ``shift`` is added to C's diagonal (absolute; or
+    ``shift_rel`` tr(C)/N_mu).  ``refine`` steps of iterative refinement follow the shifted
+    solve, literally: zeta <- zeta + (C + sI)^{-1} (Z^T - C zeta), per block of grid points.
 
     Returns dict(M (N_mu x N_mu complex128, host), L (host), C (device), zeta_t (device
     N_mu x N_g float64, when keep_zeta), cond_C, n_anti).
@@ -67,14 +71,19 @@ def isdf_real(phi, idx, mesh, coulG, shift: float = 0.0, device="cuda:0",
     C = (phimu @ phimu.T) ** 2
     ev = torch.linalg.eigvalsh(C)
     cond = float(ev[-1] / ev[0]) if float(ev[0]) > 0 else float("inf")
+    if shift_rel is not None:
+        shift = shift_rel * float(torch.trace(C)) / nmu
     Cs = C + shift * torch.eye(nmu, dtype=torch.float64, device=device)
     L = torch.linalg.cholesky(Cs)
     zt = torch.empty((nmu, ng), dtype=torch.float64, device=device)
     for g0 in range(0, ng, grid_block):
         g1 = min(ng, g0 + grid_block)
         zb = (phimu @ phi[g0:g1].T) ** 2                 # Z^T of the block (N_mu x b)
-        zt[:, g0:g1] = torch.cholesky_solve(zb, L)
-        del zb
+        x = torch.cholesky_solve(zb, L)
+        for _ in range(refine):
+            x = x + torch.cholesky_solve(zb - C @ x, L)
+        zt[:, g0:g1] = x
+        del zb, x
     dsym, danti = half_spectrum_weights(coulG, mesh, device)
     nc = dsym.numel()
     sq = torch.sqrt(torch.clamp(dsym, min=0.0))

@@ -51,9 +51,9 @@ def test_gpu_oracle_matches_cpu_oracle(name):
     idx = ref_idx(name)
     cpu = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG)
     gpu = torch_oracle(name)
-    assert _rel(gpu["M"], cpu["M"]) < 1e-10
+    # Two FP64 solves of the same system agree to ~cond(C) u (tiny: cond 3e10).
+    assert _rel(gpu["M"], cpu["M"]) < max(1e-10, gpu["cond_C"] * 2.2e-16)
     zt = gpu["zeta_t"].cpu().numpy()
-    # Two FP64 solves of the same system agree to ~cond(C) u.
     assert _rel(zt, cpu["zeta_t"]) < max(1e-10, 100 * gpu["cond_C"] * 2.2e-16)
 
 
@@ -104,3 +104,34 @@ def test_interpolating_vectors_host_output_and_errors(gpu_ctx_mixed):
     with pytest.raises(capi.ThcError) as e:
         gpu_ctx_mixed.interpolating_vectors(s.ng, s.nmu)
     assert e.value.status == capi.THC_ERR_ARG
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_refined_shifted_solve_matches_oracle(gpu_ctx_fp64, gpu_ctx_mixed, prec):
+    """A forced diagonal shift of 1e-6 tr(C)/N_mu on C2 (cond 2.3e6, so the shift biases the
+    smallest eigen-directions by up to ~30 %), then 0, 1 and 2 refinement steps: each M
+    matches the oracle's literal refinement, and every step moves M toward the unshifted
+    solution."""
+    ctx = gpu_ctx_fp64 if prec == "fp64" else gpu_ctx_mixed
+    s = system("c2")
+    idx = ref_idx("c2")
+    exact = torch_oracle("c2")["M"]
+    prev = None
+    try:
+        for k in range(3):
+            ctx.set_option("refine", k)
+            r = ctx.isdf(s.phi, idx, s.mesh, s.coulG, 1e-6)
+            assert r["status"] == 0 and r["stats"].rank_deficient == 1
+            ref = isdf_torch.isdf_real(s.phi, idx, s.mesh, s.coulG, shift_rel=1e-6, refine=k,
+                                       keep_zeta=False)
+            M = _cplx(r["M"])
+            err = _rel(M, ref["M"])
+            to_exact = _rel(M, exact)
+            print(f"{prec} refine {k}: |dM|/|M| vs refined oracle {err:.2e}, vs unshifted "
+                  f"{to_exact:.2e}")
+            assert err < (1e-9 if prec == "fp64" else 1e-6)
+            if prev is not None:
+                assert to_exact < 0.5 * prev
+            prev = to_exact
+    finally:
+        ctx.set_option("refine", 0)

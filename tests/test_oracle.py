@@ -305,3 +305,29 @@ def test_qrcp_complex_forms_agree():
     b = oracle.qrcp_gram(pc, 48)
     assert np.array_equal(a["order"], b["order"])
     assert np.max(np.abs(a["diag"] - b["diag"])) <= 1e-10 * a["diag"][0]
+
+
+def test_refinement_closed_form():
+    """k steps of iterative refinement of a shifted solve, zeta += (C + sI)^{-1}(Z - C zeta)
+    from zeta_0 = (C + sI)^{-1} Z, equal X^T P X Z with X = L^{-1} (L L^T = C + sI) and
+    P = sum_{j<=k} (s X X^T)^j -- the form the library evaluates (refine_polynomial)."""
+    rng = np.random.default_rng(3)
+    n = 40
+    q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    lam = np.logspace(0, -9, n)
+    C = (q * lam) @ q.T
+    Z = rng.standard_normal((n, 7))
+    s = 1e-6
+    L = np.linalg.cholesky(C + s * np.eye(n))
+    X = np.linalg.inv(L)
+    zeta = np.linalg.solve(C + s * np.eye(n), Z)
+    for k in range(4):
+        if k:
+            zeta = zeta + np.linalg.solve(C + s * np.eye(n), Z - C @ zeta)
+        G = s * X @ X.T
+        P = sum(np.linalg.matrix_power(G, j) for j in range(k + 1))
+        closed = X.T @ (P @ X) @ Z
+        assert np.linalg.norm(closed - zeta) <= 1e-8 * np.linalg.norm(zeta)
+        # Eigen form: filter 1 - (s / (lam + s))^(k+1) on 1 / lam.
+        filt = (1 - (s / (lam + s)) ** (k + 1)) / lam
+        assert np.allclose(q.T @ closed, filt[:, None] * (q.T @ Z), rtol=1e-6, atol=0)

@@ -65,6 +65,7 @@ enum Slot : int {
   WS_KM_WIN,        // k-means windows, cluster window offsets, segment tables
   WS_PHIOCC,        // half-rotated path: ng x nocc occupied orbitals, then nmu x nocc rows
   WS_ORB,           // (N_o + N_occ) x N_mu x 2 orbital outputs staged for a host copy
+  WS_REFINE,        // 2 x nmu x nmu doubles: the refinement polynomial applied to L^{-1}
   WS_NSLOTS
 };
 
@@ -96,6 +97,9 @@ struct Ctx {
   int tc_hi_stages = 8; // drain period of the level >= 3 accumulator, in 16-k MMA steps
   int fft64 = 0;        // mixed path: zeta in FP64 and a D2Z FFT (else FP32 and R2C)
   int qrcp_all_pairs = 0;  // half-rotated QRCP: every (occupied, orbital) pair as a row
+  // Iterative-refinement steps of zeta when C is solved with a diagonal shift s: step j
+  // adds (C + sI)^{-1} (Z^T - C zeta_j) (see isdf.cu, refine_polynomial).
+  int refine = 0;
   // Instantiated k-means iteration graphs, most recently used last, keyed by every kernel
   // argument they bake in.
   std::vector<std::pair<std::vector<long long>, cudaGraphExec_t>> km_graphs;

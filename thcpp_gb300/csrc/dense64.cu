@@ -464,6 +464,40 @@ int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* din
   return dgemm(c, g);
 }
 
+int refine_polynomial(Ctx* c, const double* X, int n, double s, int k, double* G, double* T,
+                      double* Xt)
+{
+  cudaStream_t st = c->stream;
+  const size_t bytes = sizeof(double) * (size_t)n * n;
+  int r;
+  {
+    GemmArgs g;                                   // G = s X X^T
+    g.M = n; g.N = n; g.K = n;
+    g.A = X; g.sam = n; g.sak = 1;
+    g.B = X; g.sbn = n; g.sbk = 1;
+    g.alpha = s;
+    g.C = G; g.ldc = n;
+    if ((r = dgemm(c, g))) return r;
+  }
+  // Horner: Xt = X + G (X + G (... X)); the last step lands in Xt.
+  const double* cur = X;
+  double* buf[2] = {Xt, T};
+  if (k <= 0) THC_CUDA(c, cudaMemcpyAsync(Xt, X, bytes, cudaMemcpyDeviceToDevice, st));
+  for (int j = 1; j <= k; j++) {
+    double* dst = buf[(k - j) % 2];
+    THC_CUDA(c, cudaMemcpyAsync(dst, X, bytes, cudaMemcpyDeviceToDevice, st));
+    GemmArgs g;                                   // dst = X + G cur
+    g.M = n; g.N = n; g.K = n;
+    g.A = G; g.sam = n; g.sak = 1;
+    g.B = cur; g.sbn = 1; g.sbk = n;
+    g.beta = 1.0;
+    g.C = dst; g.ldc = n;
+    if ((r = dgemm(c, g))) return r;
+    cur = dst;
+  }
+  return THC_OK;
+}
+
 int set_identity(Ctx* c, double* A, long long ld, int n)
 {
   set_identity_k<<<(int)cdiv((long long)n * n, 256), 256, 0, c->stream>>>(A, ld, n);

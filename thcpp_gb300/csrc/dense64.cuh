@@ -50,6 +50,13 @@ int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholSta
 // With Cinv == nullptr only X = L^{-1} is formed.
 int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* dinv, double* X,
                  double* T, double* Cinv, const CholStatus* cs);
+// Iterative refinement of a shifted solve, in closed form.  With L L^T = C + sI and
+// X = L^{-1} (n x n, ld n), k steps zeta_{j+1} = zeta_j + (C + sI)^{-1} (Z^T - C zeta_j)
+// from zeta_0 = (C + sI)^{-1} Z^T give zeta_k = X^T P X Z^T, P = sum_{j<=k} (s X X^T)^j
+// (eigenvalue lambda of C: filter 1 - (s / (lambda + s))^{k+1} on 1 / lambda).  Writes
+// Xt = P X by Horner's rule in FP64 (k + 1 GEMMs of n^3); G and T are n x n scratch.
+int refine_polynomial(Ctx* c, const double* X, int n, double s, int k, double* G, double* T,
+                      double* Xt);
 int set_identity(Ctx* c, double* A, long long ld, int n);
 int add_diag_shift(Ctx* c, double* A, long long ld, int n, double rel, double* shift_out);
 int diag_mean(Ctx* c, const double* A, long long ld, int n, double* out);

@@ -461,8 +461,26 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
     if (hcs.flag)
       return set_error(c, THC_ERR_NOT_PD, "thc_isdf: Cholesky of C failed at pivot %d", hcs.info);
   }
-  // C^{-1} and zeta^T = C^{-1} Z^T.
-  if ((st = chol_inverse(c, Lc, nmu, nmu, dinv, Xinv, Tinv, Cinv, cs))) return st;
+  // C^{-1} and zeta^T = C^{-1} Z^T.  With a shift and refinement steps, C^{-1} becomes
+  // X^T P X (X = L^{-1}, P the refinement polynomial; refine_polynomial).
+  const bool refining = shifted && c->refine > 0;
+  if ((st = chol_inverse(c, Lc, nmu, nmu, dinv, Xinv, Tinv, refining ? nullptr : Cinv, cs)))
+    return st;
+  if (refining) {
+    double hs = 0.0;
+    THC_CUDA(c, cudaMemcpyAsync(&hs, shift_dev, sizeof(double), cudaMemcpyDeviceToHost, s));
+    THC_CUDA(c, cudaStreamSynchronize(s));
+    double* rb = (double*)ws_get(c, WS_REFINE, sizeof(double) * 2 * nn);
+    if (!rb) return set_error(c, THC_ERR_NOMEM, "thc_isdf: refinement workspace");
+    double* xt = rb + nn;
+    if ((st = refine_polynomial(c, Xinv, nmu, hs, c->refine, Cinv, rb, xt))) return st;
+    GemmArgs g;                                   // C^{-1}_k = X^T (P X)
+    g.M = nmu; g.N = nmu; g.K = nmu;
+    g.A = Xinv; g.sam = 1; g.sak = nmu;
+    g.B = xt; g.sbn = 1; g.sbk = nmu;
+    g.C = Cinv; g.ldc = nmu;
+    if ((st = dgemm(c, g))) return st;
+  }
   {
     GemmArgs g;
     g.M = nmu; g.N = ng; g.K = nmu;

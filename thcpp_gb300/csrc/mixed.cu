@@ -122,6 +122,13 @@ __global__ void zero_upper_complex_m(double* A, int n)
   if (c > r) { A[2 * e] = 0.0; A[2 * e + 1] = 0.0; }
 }
 
+// y[i] = x[i] + a y[i]
+__global__ void axpy_from(const double* __restrict__ x, double a, long long n, double* y)
+{
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = x[i] + a * y[i];
+}
+
 __global__ void mixed_scalars(double* dmean, double* thr, double* shift, double* zero)
 {
   *thr = 1e-13 * *dmean;
@@ -322,8 +329,49 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     // zeta^T = X^T Y.  (Emulated on the C1 cell this is also more accurate than the FP64
     // C^{-1} product: pair-Coulomb invariant 1.7e-8 against 2.2e-6.)
     const SliceBuf zs = slices(sb, eb, ng_pad, mu_kpad, sz), xs = slices(sa, ea, mu_pad, mu_kpad, sz);
+    // Iterative refinement of the shifted solve: the first product takes P X in place of X
+    // (refine_polynomial in dense64.cuh), formed here with the sliced GEMM: G = X X^T once,
+    // then k Horner steps T <- X + s G T.
+    const double* xfirst = Xinv;
+    if (c->refine > 0) {
+      double hs = 0.0;
+      THC_CUDA(c, cudaMemcpyAsync(&hs, shift_dev, sizeof(double), cudaMemcpyDeviceToHost, s));
+      THC_CUDA(c, cudaStreamSynchronize(s));
+      double* rb = (double*)ws_get(c, WS_REFINE, sizeof(double) * 2 * nn);
+      if (!rb) return set_error(c, THC_ERR_NOMEM, "thc_isdf: refinement workspace");
+      double* G = Cinv;                          // unused by the shifted solve
+      double* tb[2] = {rb, rb + nn};
+      const SliceBuf ts = slices(sb, eb, mu_pad, mu_kpad, sz);
+      auto product = [&](const SliceBuf& a, const SliceBuf& b, double* out, const char* tag) {
+        OzArgs g;
+        g.M = nmu; g.N = nmu; g.K = nmu;
+        g.a = a.operand();
+        g.b = b.operand();
+        g.levels = sz; g.epilogue = OZ_STORE_F64; g.C = out; g.ldc = nmu;
+        g.tag = tag;
+        g.ksplit = oz_choose_split(nmu, nmu, nmu, false);
+        if (g.ksplit > 1) {
+          g.part = (double*)ws_get(c, WS_PART, sizeof(double) * g.ksplit * nn);
+          if (!g.part) return set_error(c, THC_ERR_NOMEM, "thc_isdf: split-K partials");
+        }
+        return gemm(g);
+      };
+      if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, nmu, 1, nullptr, 0, xs))) return st;
+      if ((st = product(xs, xs, G, "oz_refine"))) return st;                   // G = X X^T
+      if ((st = oz_slice_rows_f64(c, G, nmu, nmu, nmu, 1, nullptr, 0, xs))) return st;
+      const double* cur = Xinv;
+      for (int j = 1; j <= c->refine; j++) {
+        double* dst = tb[j & 1];
+        if ((st = oz_slice_rows_f64(c, cur, nmu, nmu, 1, nmu, nullptr, 0, ts))) return st;
+        if ((st = product(xs, ts, dst, "oz_refine"))) return st;              // G cur
+        axpy_from<<<(int)cdiv(nn, 256), 256, 0, s>>>(Xinv, hs, nn, dst);     // X + s G cur
+        THC_LAUNCHED(c, "axpy_from");
+        cur = dst;
+      }
+      xfirst = cur;
+    }
     if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs))) return st;
-    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, nmu, 1, nullptr, 0, xs))) return st;   // rows of X
+    if ((st = oz_slice_rows_f64(c, xfirst, nmu, nmu, nmu, 1, nullptr, 0, xs))) return st; // rows of P X
     {
       OzArgs g;                                  // Y^T (N_g x N_mu) = Z X^T, into zg
       g.M = ng; g.N = nmu; g.K = nmu;

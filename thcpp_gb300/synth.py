@@ -24,7 +24,8 @@ Cells, basis and seeds (the workload definitions used by the tests and the bench
   atoms at 0 and a/4 (1,1,1); mesh 24^3; N_o = 8; N_mu = 8 N_o = 64.
 * ``c2``: 8-atom cubic conventional diamond cell, a = 6.74; mesh 48^3; N_o = 32; N_mu = 256.
 * ``c3``: 2x2x2 repeat of c2 (64 atoms); mesh 72^3; N_o = 256; N_mu = 2048.
-* ``c5``: 3x3x3 repeat of c2 (216 atoms); mesh 108^3; N_o = 864; N_mu = 5184.
+* ``c5``: 3x3x3 repeat of c2 (216 atoms); mesh 108^3; N_o = 864; N_mu = 5184; half of
+  the exponents redrawn from U[3, 6] so that C is near rank-deficient (cond 2.8e11).
 * ``c4``: 48 random cubic cells (see :func:`c4_system`).
 
 Per atom four functions s = exp(-a|r-R|^2) and p_x,y,z = (x-X) exp(-a|r-R|^2), each with
@@ -175,11 +176,30 @@ def loewdin(phi: np.ndarray, volume: float) -> np.ndarray:
     return phi @ (u * (1.0 / np.sqrt(w))) @ u.T
 
 
-def draw_parameters(atoms, norb, seed):
-    """The seeded exponents (one per function, atom-major s, px, py, pz) and mixing matrix."""
+# Cells whose interpolation matrix C is made near rank-deficient on purpose: a fraction of
+# the basis functions gets tight exponents.  The 216-atom cell with every exponent in
+# [0.3, 1.5] gives cond(C) 2.6e6; with half of them redrawn from [3, 6] cond(C) = 2.8e11
+# (129 eigenvalues below 1e-8 tr(C)/N_mu), measured on the k-means points of the GPU path.
+# (Broader functions do the opposite: [0.3, 0.5] for every function gives 3.9e3.)
+_TIGHT = {"c5": (0.5, 3.0, 6.0)}
+
+
+def draw_parameters(atoms, norb, seed, tight=None):
+    """The seeded exponents (one per function, atom-major s, px, py, pz) and mixing matrix.
+
+    ``tight`` = (fraction, lo, hi): that fraction of the exponents, chosen by
+    ``default_rng(seed + 777)``, is redrawn from U[lo, hi] by the same generator."""
     rng = np.random.default_rng(seed)
     alphas = rng.uniform(0.3, 1.5, size=4 * atoms.shape[0])
     mix = rng.standard_normal((norb, norb))
+    if tight is not None:
+        frac, lo, hi = tight
+        r2 = np.random.default_rng(seed + 777)
+        n = alphas.size
+        k = int(round(frac * n))
+        sel = np.sort(r2.choice(n, k, replace=False))
+        alphas = alphas.copy()
+        alphas[sel] = r2.uniform(lo, hi, size=k)
     return alphas, mix
 
 
@@ -206,7 +226,7 @@ def image_centres(lattice, atoms, alphas, nfunc):
 
 def make_system(name, lattice, atoms, mesh, norb, cfac, seed, kmeans_seed,
                 max_it=100, threshold=1e-6) -> System:
-    alphas, mix = draw_parameters(atoms, norb, seed)
+    alphas, mix = draw_parameters(atoms, norb, seed, _TIGHT.get(name))
     grid = uniform_grid(lattice, mesh)
     raw = gaussian_sp_basis(grid, lattice, atoms, alphas, norb)
     vol = abs(np.linalg.det(lattice))
@@ -388,7 +408,7 @@ def make_system_gpu(name, lattice, atoms, mesh, norb, cfac, seed, kmeans_seed, c
     mixing, Loewdin orthonormalisation and density formed there (FP64).  Same draws as
     make_system; orbitals agree with it to ~1e-6 relative (FP32 Gaussians)."""
     import torch
-    alphas, mix = draw_parameters(atoms, norb, seed)
+    alphas, mix = draw_parameters(atoms, norb, seed, _TIGHT.get(name))
     grid = uniform_grid(lattice, mesh)
     ng = grid.shape[0]
     cen, cat, rcut = image_centres(lattice, atoms, alphas, norb)
