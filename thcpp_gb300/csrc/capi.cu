@@ -282,6 +282,10 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
     h->c.qrcp_all_pairs = value != 0.0;
     return THC_OK;
   }
+  if (!strcmp(key, "equilibrate")) {
+    h->c.equilibrate = value != 0.0;
+    return THC_OK;
+  }
   if (!strcmp(key, "refine")) {
     if (value < 0 || value > 8) return THC_ERR_ARG;
     h->c.refine = (int)value;

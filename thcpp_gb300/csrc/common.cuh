@@ -65,7 +65,8 @@ enum Slot : int {
   WS_KM_WIN,        // k-means windows, cluster window offsets, segment tables
   WS_PHIOCC,        // half-rotated path: ng x nocc occupied orbitals, then nmu x nocc rows
   WS_ORB,           // (N_o + N_occ) x N_mu x 2 orbital outputs staged for a host copy
-  WS_REFINE,        // 2 x nmu x nmu doubles: the refinement polynomial applied to L^{-1}
+  WS_REFINE,        // 3 x nmu x nmu doubles: refinement polynomial, L^{-1} T (mixed)
+  WS_EQUIL,         // nmu doubles + nmu ints: power-of-two equilibration of C (mixed)
   WS_NSLOTS
 };
 
@@ -100,6 +101,11 @@ struct Ctx {
   // Iterative-refinement steps of zeta when C is solved with a diagonal shift s: step j
   // adds (C + sI)^{-1} (Z^T - C zeta_j) (see isdf.cu, refine_polynomial).
   int refine = 0;
+  // Mixed path: solve with C scaled to a unit-range diagonal by powers of two, T C T
+  // (T = 2^{-round(log2 sqrt(C_ii))}), so that the rows sliced for the solve products are
+  // balanced (an ill-conditioned C with a wide diagonal otherwise loses most of the 42 bits
+  // of its small entries).
+  int equilibrate = 1;
   // Instantiated k-means iteration graphs, most recently used last, keyed by every kernel
   // argument they bake in.
   std::vector<std::pair<std::vector<long long>, cudaGraphExec_t>> km_graphs;

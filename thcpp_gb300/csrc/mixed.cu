@@ -122,6 +122,49 @@ __global__ void zero_upper_complex_m(double* A, int n)
   if (c > r) { A[2 * e] = 0.0; A[2 * e + 1] = 0.0; }
 }
 
+// Power-of-two equilibration of a symmetric positive semi-definite C: t_i = 2^{-k_i},
+// k_i = round(log2 sqrt(C_ii)) (k_i = 0 for a non-positive diagonal, or when off).
+__global__ void equil_scales(const double* __restrict__ C, int n, int on, double* t, int* k)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double d = C[(long long)i * n + i];
+  int e = 0;
+  if (on && d > 0.0) e = (int)rint(0.5 * log2(d));
+  k[i] = e;
+  t[i] = ldexp(1.0, -e);
+}
+
+// dst = diag(t) src diag(t) (exact: powers of two)
+__global__ void scale_sym(const double* __restrict__ src, const double* __restrict__ t, int n,
+                          double* dst)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)n * n) return;
+  dst[e] = src[e] * t[e / n] * t[e % n];
+}
+
+// A[i][j] *= t[i] (rows) or t[j] (columns), into dst.
+__global__ void scale_rows_cols(const double* __restrict__ A, const double* __restrict__ t, int n,
+                                int cols, double* dst)
+{
+  long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= (long long)n * n) return;
+  dst[e] = A[e] * t[cols ? e % n : e / n];
+}
+
+// shift = rel * mean diag(C) (of the unscaled C); A_ii += shift t_i^2.
+__global__ void add_shift_scaled(double* A, int n, const double* dmean, double rel,
+                                 const double* __restrict__ t, double* shift_out)
+{
+  const double sh = rel * *dmean;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *shift_out = sh;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    A[(long long)i * n + i] += sh * t[i] * t[i];
+}
+
+__global__ void scaled_threshold(const double* dmean_s, double* thr) { *thr = 1e-13 * *dmean_s; }
+
 // y[i] = x[i] + a y[i]
 __global__ void axpy_from(const double* __restrict__ x, double a, long long n, double* y)
 {
@@ -249,14 +292,29 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     if ((st = dgemm(c, g))) return st;
   }
   double* Lc = C + nn;
+  // The solve runs on T C T (equilibration by powers of two, the context option
+  // "equilibrate"): C^{-1} = T (T C T)^{-1} T, and the shift s I becomes s T^2.
+  double* teq = (double*)ws_get(c, WS_EQUIL, (sizeof(double) + sizeof(int)) * nmu + 256);
+  if (!teq) return set_error(c, THC_ERR_NOMEM, "thc_isdf (mixed): equilibration scales");
+  int* keq = (int*)(teq + nmu);
+  double* dmean_s = dmean + 4;
+  equil_scales<<<(int)cdiv(nmu, 256), 256, 0, s>>>(C, nmu, c->equilibrate, teq, keq);
+  THC_LAUNCHED(c, "equil_scales");
+  const int nbe = (int)cdiv(nn, 256);
   if ((st = diag_mean(c, C, nmu, nmu, dmean))) return st;
   mixed_scalars<<<1, 1, 0, s>>>(dmean, thr, shift_dev, zero);
   THC_LAUNCHED(c, "mixed_scalars");
+  scale_sym<<<nbe, 256, 0, s>>>(C, teq, nmu, Lc);
+  THC_LAUNCHED(c, "scale_sym");
+  if ((st = diag_mean(c, Lc, nmu, nmu, dmean_s))) return st;
+  scaled_threshold<<<1, 1, 0, s>>>(dmean_s, thr);   // pivot threshold on the scaled matrix
+  THC_LAUNCHED(c, "scaled_threshold");
   auto factor = [&](double rel) -> int {
-    THC_CUDA(c, cudaMemcpyAsync(Lc, C, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
+    scale_sym<<<nbe, 256, 0, s>>>(C, teq, nmu, Lc);
+    THC_LAUNCHED(c, "scale_sym");
     if (rel > 0.0) {
-      int r = add_diag_shift(c, Lc, nmu, nmu, rel, shift_dev);
-      if (r) return r;
+      add_shift_scaled<<<(int)cdiv(nmu, 256), 256, 0, s>>>(Lc, nmu, dmean, rel, teq, shift_dev);
+      THC_LAUNCHED(c, "add_shift_scaled");
     }
     init_cs<<<1, 1, 0, s>>>(cs);
     THC_LAUNCHED(c, "init_cs");
@@ -319,6 +377,12 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     }
     if ((st = gemm(g))) return st;
   }
+  if (!shifted) {
+    // (T C T)^{-1} -> T (T C T)^{-1}: the left factor T (row scaling; the right one scales Z's
+    // columns while they are sliced).
+    scale_rows_cols<<<nbe, 256, 0, s>>>(Cinv, teq, nmu, 0, Cinv);
+    THC_LAUNCHED(c, "scale_rows_cols");
+  }
   // zeta^T = C^{-1} Z^T: A = C^{-1} sliced by rows, B = Z sliced by rows (grid points).
   // A rank-deficient C (shifted) has an inverse whose null-space entries are ~1/shift, so
   // the product cancels by far more than any slice depth resolves: it runs in FP64 then.
@@ -329,16 +393,21 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     // zeta^T = X^T Y.  (Emulated on the C1 cell this is also more accurate than the FP64
     // C^{-1} product: pair-Coulomb invariant 1.7e-8 against 2.2e-6.)
     const SliceBuf zs = slices(sb, eb, ng_pad, mu_kpad, sz), xs = slices(sa, ea, mu_pad, mu_kpad, sz);
-    // Iterative refinement of the shifted solve: the first product takes P X in place of X
-    // (refine_polynomial in dense64.cuh), formed here with the sliced GEMM: G = X X^T once,
-    // then k Horner steps T <- X + s G T.
+    // Here X = L^{-1} of the equilibrated T (C + sI) T = L L^T, so (C + sI)^{-1} =
+    // T X^T X T and zeta^T = (X T)^T (X (T Z^T)): the first product slices Z's columns scaled
+    // by T.  Iterative refinement of the shifted solve (refine_polynomial in dense64.cuh)
+    // puts P X in place of X in the first product, P = sum_j (s G)^j with G = X T^2 X^T,
+    // formed with the sliced GEMM: G once, then k Horner steps W <- X + s G W.
+    double* rb = (double*)ws_get(c, WS_REFINE, sizeof(double) * 3 * nn);
+    if (!rb) return set_error(c, THC_ERR_NOMEM, "thc_isdf: refinement workspace");
+    double* xsc = rb + 2 * nn;                   // X T
+    scale_rows_cols<<<nbe, 256, 0, s>>>(Xinv, teq, nmu, 1, xsc);
+    THC_LAUNCHED(c, "scale_rows_cols");
     const double* xfirst = Xinv;
     if (c->refine > 0) {
       double hs = 0.0;
       THC_CUDA(c, cudaMemcpyAsync(&hs, shift_dev, sizeof(double), cudaMemcpyDeviceToHost, s));
       THC_CUDA(c, cudaStreamSynchronize(s));
-      double* rb = (double*)ws_get(c, WS_REFINE, sizeof(double) * 2 * nn);
-      if (!rb) return set_error(c, THC_ERR_NOMEM, "thc_isdf: refinement workspace");
       double* G = Cinv;                          // unused by the shifted solve
       double* tb[2] = {rb, rb + nn};
       const SliceBuf ts = slices(sb, eb, mu_pad, mu_kpad, sz);
@@ -356,8 +425,8 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
         }
         return gemm(g);
       };
-      if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, nmu, 1, nullptr, 0, xs))) return st;
-      if ((st = product(xs, xs, G, "oz_refine"))) return st;                   // G = X X^T
+      if ((st = oz_slice_rows_f64(c, xsc, nmu, nmu, nmu, 1, nullptr, 0, xs))) return st;
+      if ((st = product(xs, xs, G, "oz_refine"))) return st;           // G = X T^2 X^T
       if ((st = oz_slice_rows_f64(c, G, nmu, nmu, nmu, 1, nullptr, 0, xs))) return st;
       const double* cur = Xinv;
       for (int j = 1; j <= c->refine; j++) {
@@ -370,7 +439,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
       }
       xfirst = cur;
     }
-    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs))) return st;
+    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs, keq))) return st;              // Z T
     if ((st = oz_slice_rows_f64(c, xfirst, nmu, nmu, nmu, 1, nullptr, 0, xs))) return st; // rows of P X
     {
       OzArgs g;                                  // Y^T (N_g x N_mu) = Z X^T, into zg
@@ -381,7 +450,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
       g.tag = "oz_Y";
       if ((st = gemm(g))) return st;
     }
-    if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, 1, nmu, nullptr, 0, xs))) return st;   // rows of X^T
+    if ((st = oz_slice_rows_f64(c, xsc, nmu, nmu, 1, nmu, nullptr, 0, xs))) return st;   // rows of (X T)^T
     if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs))) return st;                    // rows of Y^T
     OzArgs g;                                    // zeta^T = X^T Y
     g.M = nmu; g.N = ng; g.K = nmu;
@@ -393,7 +462,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   } else {
     const SliceBuf ci = slices(sa, ea, mu_pad, mu_kpad, sz), zs = slices(sb, eb, ng_pad, mu_kpad, sz);
     if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, ci))) return st;
-    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs))) return st;
+    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs, keq))) return st;             // Z T
     OzArgs g;
     g.M = nmu; g.N = ng; g.K = nmu;
     g.a = ci.operand();

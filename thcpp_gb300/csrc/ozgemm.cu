@@ -364,10 +364,11 @@ __device__ __forceinline__ long long fixed_point_f32(float x, int shift_total)
 // Slices of a double-word (hi, lo) matrix, one warp per row, as slice_rows_kernel: the row
 // exponent comes from max |hi| (|hi + lo| < 2^e whenever |hi| < 2^e), and the fixed-point
 // integer is the sum of the two parts' roundings (within one unit of the exact value).
+// With kexp, column k is scaled by 2^{-kexp[k]}: a shift of the fixed-point cut, exact.
 __global__ void slice_rows_dw_kernel(const float2* __restrict__ X, long long rows, long long cols,
                                      long long ldx, int ns, __nv_bfloat16* out, long long ldo,
                                      long long sstride, long long kts, int* exps,
-                                     long long rows_pad)
+                                     long long rows_pad, const int* __restrict__ kexp)
 {
   long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
@@ -375,7 +376,9 @@ __global__ void slice_rows_dw_kernel(const float2* __restrict__ X, long long row
   unsigned mx = 0;
   if (r < rows)
     for (long long cc = lane; cc < cols; cc += 32) {
-      unsigned a = __float_as_uint(X[r * ldx + cc].x) & 0x7fffffffu;
+      float h = X[r * ldx + cc].x;
+      if (kexp) h = ldexpf(h, -kexp[cc]);
+      unsigned a = __float_as_uint(h) & 0x7fffffffu;
       mx = a > mx ? a : mx;
     }
   for (int off = 16; off; off >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
@@ -388,7 +391,8 @@ __global__ void slice_rows_dw_kernel(const float2* __restrict__ X, long long row
     long long R = 0;
     if (r < rows && cc < cols && Em > 0) {
       float2 v = X[r * ldx + cc];
-      R = fixed_point_f32(v.x, total) + fixed_point_f32(v.y, total);
+      const int t = kexp ? total - kexp[cc] : total;
+      R = fixed_point_f32(v.x, t) + fixed_point_f32(v.y, t);
     }
     for (int s2 = 0; s2 < ns; s2++) {
       int sh = 7 * (ns - 1 - s2);
@@ -491,13 +495,13 @@ int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, l
 }
 
 int oz_slice_rows_dw(Ctx* c, const float2* X, long long rows, long long cols, long long ldx,
-                     const SliceBuf& out)
+                     const SliceBuf& out, const int* kexp)
 {
   ProfScope prof(c, "slice");
   long long threads = out.rows_pad * 32;
   slice_rows_dw_kernel<<<(unsigned)cdiv(threads, 256), 256, 0, c->stream>>>(
       X, rows, cols, ldx, out.ns, out.s, out.kpad, out.slice_stride(), out.kt_stride(), out.e,
-      out.rows_pad);
+      out.rows_pad, kexp);
   THC_LAUNCHED(c, "slice_rows_dw");
   return THC_OK;
 }

@@ -89,8 +89,9 @@ struct SliceBuf {
 int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
                       long long sc, const double* scale, int scale_shift, const SliceBuf& out);
 // Slices of a double-word matrix (float2 {hi, lo} entries, row-major, ld = ldx).
+// kexp (optional, one per column): column k is scaled by 2^{-kexp[k]} first (exact).
 int oz_slice_rows_dw(Ctx* c, const float2* X, long long rows, long long cols, long long ldx,
-                     const SliceBuf& out);
+                     const SliceBuf& out, const int* kexp = nullptr);
 int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, long long ldx,
                       const float* scale, int scale_shift, const SliceBuf& out);
 // Warp-level mma.sync implementation (reference for the tensor-core kernel below).
