@@ -185,6 +185,9 @@ int thc_ctx_create(int device, int precision, thc_ctx** out)
   c->device = device;
   c->precision = precision;
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       cudaMallocHost(&c->pinned, 4096) != cudaSuccess) {
     cudaGetLastError();
@@ -222,6 +225,12 @@ int thc_ctx_destroy(thc_ctx* h)
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->aux_stream) {
+    cudaStreamSynchronize(c->aux_stream);
+    cudaStreamDestroy(c->aux_stream);
+  }
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete h;
   return THC_OK;

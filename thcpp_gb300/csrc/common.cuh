@@ -75,6 +75,10 @@ struct Ctx {
   int precision = THC_PREC_FP64;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  // Second stream for work that overlaps the main one (C's factorisation beside the P
+  // product), forked and joined with these events.
+  cudaStream_t aux_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void* ws[WS_NSLOTS] = {};
   size_t ws_bytes[WS_NSLOTS] = {};
   std::map<std::tuple<int, int, int, int, int>, cufftHandle> plans;  // (n0,n1,n2,batch,type)
@@ -125,6 +129,15 @@ struct Ctx {
   struct Rec { std::string name; cudaEvent_t a, b; };
   std::vector<Rec> recs;
   std::vector<cudaEvent_t> event_pool;
+};
+
+// Runs the enclosing scope's launches on another stream (the context's current stream is
+// what every helper launches on), restoring the previous one on exit.
+struct StreamSwap {
+  Ctx* c;
+  cudaStream_t prev;
+  StreamSwap(Ctx* ctx, cudaStream_t s) : c(ctx), prev(ctx->stream) { c->stream = s; }
+  ~StreamSwap() { c->stream = prev; }
 };
 
 // RAII event pair around one launch when profiling is on.

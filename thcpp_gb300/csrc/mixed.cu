@@ -238,12 +238,12 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   double* Tinv = Xinv + nn;
   // Slices: A holds Phi's, then C^{-1}'s / X's; B holds Phi_mu's, Z's (or Y's), then,
   // once the solve is done, zeta_hat's for the Coulomb contraction.
-  size_t a_elems = std::max((size_t)sp * ng_pad * no_kpad, (size_t)sz * mu_pad * mu_kpad);
+  size_t a_elems = std::max((size_t)sp * ng_pad * no_kpad, 2 * (size_t)sz * mu_pad * mu_kpad);
   size_t b_elems = std::max({(size_t)sp * mu_pad * no_kpad, (size_t)sz * ng_pad * mu_kpad,
                              (size_t)sm * mu_pad * k2_pad});
   __nv_bfloat16* sa = (__nv_bfloat16*)ws_get(c, WS_SLICE_A, sizeof(__nv_bfloat16) * a_elems);
   __nv_bfloat16* sb = (__nv_bfloat16*)ws_get(c, WS_SLICE_B, sizeof(__nv_bfloat16) * b_elems);
-  int* ex = (int*)ws_get(c, WS_SLICE_E, sizeof(int) * (mu_pad + ng_pad + 64));
+  int* ex = (int*)ws_get(c, WS_SLICE_E, sizeof(int) * (2 * mu_pad + ng_pad + 64));
   if (!phimu || !C || !Cinv || !zg || !zeta || !zhat || !dsym || !danti || !Mw || !Lw || !scr || !dinv ||
       !sa || !sb || !ex)
     return set_error(c, THC_ERR_NOMEM, "thc_isdf (mixed): workspace allocation failed");
@@ -251,6 +251,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   float* sq = (float*)(dsym + 2 * nc);
   int* ea = ex;
   int* eb = ex + mu_pad;
+  int* et = eb + ng_pad + 64;       // exponents of the refinement's W slices
   CholStatus* cs = (CholStatus*)scr;
   CholStatus* csm = cs + 1;
   double* dmean = (double*)(scr + 256);
@@ -309,17 +310,39 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   if ((st = diag_mean(c, Lc, nmu, nmu, dmean_s))) return st;
   scaled_threshold<<<1, 1, 0, s>>>(dmean_s, thr);   // pivot threshold on the scaled matrix
   THC_LAUNCHED(c, "scaled_threshold");
+  // Factorisation of T C T (+ shift) on the context's current stream.
   auto factor = [&](double rel) -> int {
-    scale_sym<<<nbe, 256, 0, s>>>(C, teq, nmu, Lc);
+    cudaStream_t fs = c->stream;
+    scale_sym<<<nbe, 256, 0, fs>>>(C, teq, nmu, Lc);
     THC_LAUNCHED(c, "scale_sym");
     if (rel > 0.0) {
-      add_shift_scaled<<<(int)cdiv(nmu, 256), 256, 0, s>>>(Lc, nmu, dmean, rel, teq, shift_dev);
+      add_shift_scaled<<<(int)cdiv(nmu, 256), 256, 0, fs>>>(Lc, nmu, dmean, rel, teq, shift_dev);
       THC_LAUNCHED(c, "add_shift_scaled");
     }
-    init_cs<<<1, 1, 0, s>>>(cs);
+    init_cs<<<1, 1, 0, fs>>>(cs);
     THC_LAUNCHED(c, "init_cs");
     return potrf_inv(c, Lc, nmu, nmu, thr, cs, dinv);
   };
+  // C's factorisation and inverse depend on Phi_mu only: they run on the context's second
+  // stream while the P product and Z's slicing run on the main one (the Cholesky's diagonal
+  // blocks occupy one SM at a time).  The expected case is taken ahead: the shift as given,
+  // X = L^{-1}, and C^{-1} = X^T X in FP64 when N_mu < 512 without a shift; a breakdown of
+  // the unshifted factorisation is retried on the main stream after the join.
+  bool shifted = shift_rel > 0.0;
+  bool cinv_tc = !shifted && nmu >= 512;
+  CholStatus* hcs_p = (CholStatus*)c->pinned;      // pinned: the copy stays asynchronous
+  {
+    THC_CUDA(c, cudaEventRecord(c->ev_fork, s));
+    THC_CUDA(c, cudaStreamWaitEvent(c->aux_stream, c->ev_fork, 0));
+    StreamSwap on_aux(c, c->aux_stream);
+    if ((st = factor(shifted ? shift_rel : 0.0))) return st;
+    if ((st = chol_inverse(c, Lc, nmu, nmu, dinv, Xinv, Tinv, (shifted || cinv_tc) ? nullptr : Cinv,
+                           cs)))
+      return st;
+    THC_CUDA(c, cudaMemcpyAsync(hcs_p, cs, sizeof(CholStatus), cudaMemcpyDeviceToHost,
+                                c->aux_stream));
+    THC_CUDA(c, cudaEventRecord(c->ev_join, c->aux_stream));
+  }
   // Z = (Phi Phi_mu^T)^2 (N_g x N_mu) via the sliced GEMM: A = Phi sliced by grid point,
   // B = Phi_mu sliced by interpolating point; Z's rows are then K-contiguous for the solve.
   // Z is kept as double-word FP32 (~46 bits; the solve slices it to 42), so the epilogue
@@ -336,19 +359,25 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     g.tag = "oz_P";
     if ((st = gemm(g))) return st;
   }
-  CholStatus hcs{};
+  // Z T sliced by rows (grid points) for the solve: the B operand of zeta^T = C^{-1} Z^T, or
+  // the A operand of Y^T = Z X^T with a shift (the columns scaled by T, exactly).
+  const SliceBuf zs = slices(sb, eb, ng_pad, mu_kpad, sz);
+  if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs, keq))) return st;
+  // Join C's factorisation.
+  THC_CUDA(c, cudaStreamSynchronize(c->aux_stream));
+  THC_CUDA(c, cudaStreamWaitEvent(s, c->ev_join, 0));
+  CholStatus hcs = *hcs_p;
   int chol_c_info = 0;
-  bool shifted = shift_rel > 0.0;
-  if ((st = factor(shift_rel > 0.0 ? shift_rel : 0.0))) return st;
-  THC_CUDA(c, cudaMemcpyAsync(&hcs, cs, sizeof(CholStatus), cudaMemcpyDeviceToHost, s));
-  THC_CUDA(c, cudaStreamSynchronize(s));
   if (hcs.flag) {
     chol_c_info = hcs.info;
     if (shift_rel < 0.0 && !shifted) {
       if ((st = factor(1e-10))) return st;
       shifted = true;
+      cinv_tc = false;
       THC_CUDA(c, cudaMemcpyAsync(&hcs, cs, sizeof(CholStatus), cudaMemcpyDeviceToHost, s));
       THC_CUDA(c, cudaStreamSynchronize(s));
+      if (!hcs.flag && (st = chol_inverse(c, Lc, nmu, nmu, dinv, Xinv, Tinv, nullptr, cs)))
+        return st;
     }
     if (hcs.flag)
       return set_error(c, THC_ERR_NOT_PD, "thc_isdf: Cholesky of C failed at pivot %d", hcs.info);
@@ -356,10 +385,6 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   // X = L^{-1}; C^{-1} = X^T X is needed by the full-rank solve only.  From N_mu = 512 on,
   // that product runs as a sliced tensor GEMM (A = B = the slices of X^T): on C2 its M
   // error is 4e-9, while the FP64 product would cost 2 N_mu^3 on the narrow FP64 pipe.
-  const bool cinv_tc = !shifted && nmu >= 512;
-  if ((st = chol_inverse(c, Lc, nmu, nmu, dinv, Xinv, Tinv, (shifted || cinv_tc) ? nullptr : Cinv,
-                         cs)))
-    return st;
   if (cinv_tc) {
     const SliceBuf xt = slices(sa, ea, mu_pad, mu_kpad, sz);
     if ((st = oz_slice_rows_f64(c, Xinv, nmu, nmu, 1, nmu, nullptr, 0, xt)))   // rows of X^T
@@ -392,7 +417,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     // X instead, each amplifying by ~1/sqrt(shift) only: Y^T = Z X^T, then
     // zeta^T = X^T Y.  (Emulated on the C1 cell this is also more accurate than the FP64
     // C^{-1} product: pair-Coulomb invariant 1.7e-8 against 2.2e-6.)
-    const SliceBuf zs = slices(sb, eb, ng_pad, mu_kpad, sz), xs = slices(sa, ea, mu_pad, mu_kpad, sz);
+    const SliceBuf xs = slices(sa, ea, mu_pad, mu_kpad, sz);
     // Here X = L^{-1} of the equilibrated T (C + sI) T = L L^T, so (C + sI)^{-1} =
     // T X^T X T and zeta^T = (X T)^T (X (T Z^T)): the first product slices Z's columns scaled
     // by T.  Iterative refinement of the shifted solve (refine_polynomial in dense64.cuh)
@@ -410,7 +435,8 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
       THC_CUDA(c, cudaStreamSynchronize(s));
       double* G = Cinv;                          // unused by the shifted solve
       double* tb[2] = {rb, rb + nn};
-      const SliceBuf ts = slices(sb, eb, mu_pad, mu_kpad, sz);
+      // W's slices behind X's in the A buffer (B holds Z's slices).
+      const SliceBuf ts = slices(sa + (size_t)sz * mu_pad * mu_kpad, et, mu_pad, mu_kpad, sz);
       auto product = [&](const SliceBuf& a, const SliceBuf& b, double* out, const char* tag) {
         OzArgs g;
         g.M = nmu; g.N = nmu; g.K = nmu;
@@ -439,7 +465,6 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
       }
       xfirst = cur;
     }
-    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs, keq))) return st;              // Z T
     if ((st = oz_slice_rows_f64(c, xfirst, nmu, nmu, nmu, 1, nullptr, 0, xs))) return st; // rows of P X
     {
       OzArgs g;                                  // Y^T (N_g x N_mu) = Z X^T, into zg
@@ -460,9 +485,8 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     g.tag = "oz_zeta";
     if ((st = gemm(g))) return st;
   } else {
-    const SliceBuf ci = slices(sa, ea, mu_pad, mu_kpad, sz), zs = slices(sb, eb, ng_pad, mu_kpad, sz);
+    const SliceBuf ci = slices(sa, ea, mu_pad, mu_kpad, sz);
     if ((st = oz_slice_rows_f64(c, Cinv, nmu, nmu, nmu, 1, nullptr, 0, ci))) return st;
-    if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs, keq))) return st;             // Z T
     OzArgs g;
     g.M = nmu; g.N = ng; g.K = nmu;
     g.a = ci.operand();
