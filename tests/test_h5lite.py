@@ -87,3 +87,54 @@ def test_reads_libhdf5_fixture():
     assert r.read("nelec").ravel().tolist()[0] == 5
     for name, shape in [("etaPm", (140, 10)), ("eri_df", (140, 100)), ("T", (140, 140))]:
         assert r.info(name)[1] == shape
+
+
+_READ_ALL = r"""
+import sys
+sys.path.insert(0, {root!r})
+from thcpp_gb300 import h5
+try:
+    r = h5.Reader({path!r})
+    for name in ("real_space_grid", "aoR", "fft_coulomb", "fft_grid", "density_occ"):
+        r.read(name)
+    print("READ_OK")
+except (OSError, KeyError) as e:
+    print("READ_ERROR", e)
+"""
+
+
+def _read_in_child(path):
+    """Read every dataset in a child process: a corrupt file must give an error, not a
+    crash (a crash would end the child with a signal)."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    p = subprocess.run([sys.executable, "-c", _READ_ALL.format(root=root, path=path)],
+                       capture_output=True, text=True, timeout=120)
+    assert p.returncode == 0, (p.returncode, p.stderr[-500:])
+    return p.stdout
+
+
+def test_truncated_and_corrupt_orbital_files_raise(tmp_path):
+    """Orbital files cut short at several offsets, or with bytes of the metadata overwritten,
+    raise OSError/KeyError from the reader (the drop-in's THC_ERR_IO) instead of crashing."""
+    s = synth.config("tiny")
+    good = str(tmp_path / "orb.h5")
+    synth.write_orbital_file(s, good)
+    assert "READ_OK" in _read_in_child(good)
+    data = open(good, "rb").read()
+    rng = np.random.default_rng(5)
+    cases = [data[:n] for n in (0, 7, 100, 600, len(data) // 3, len(data) - 9)]
+    for _ in range(12):
+        b = bytearray(data)
+        off = int(rng.integers(0, 2048))               # superblock, object headers, B-trees
+        b[off:off + 8] = bytes(rng.integers(0, 256, 8, dtype=np.uint8))
+        cases.append(bytes(b))
+    n_err = 0
+    for k, blob in enumerate(cases):
+        p = str(tmp_path / f"bad{k}.h5")
+        open(p, "wb").write(blob)
+        out = _read_in_child(p)
+        assert "READ_OK" in out or "READ_ERROR" in out
+        n_err += "READ_ERROR" in out
+    assert n_err >= 6            # every truncation is an error; some flips hit only data

@@ -331,3 +331,33 @@ def test_refinement_closed_form():
         # Eigen form: filter 1 - (s / (lam + s))^(k+1) on 1 / lam.
         filt = (1 - (s / (lam + s)) ** (k + 1)) / lam
         assert np.allclose(q.T @ closed, filt[:, None] * (q.T @ Z), rtol=1e-6, atol=0)
+
+
+def test_rsqrt_refinement_reaches_fp64():
+    """The reciprocal square root of the diagonal Cholesky pivots (dense64.cu rsqrt_fast):
+    an FP32 seed y0 refined once by the second-order binomial step
+    y = y0 + y0 e (1/2 + 3/8 e), e = 1 - d y0^2 (FMAs as in the kernel), stays within 2 ulp
+    of 1/sqrt(d) for seeds up to 8 FP32 ulps off, over the pivot range (d spans 1e-30..1e30,
+    the kernel's FP32 seed range)."""
+    import math
+    from fractions import Fraction as F
+
+    def fma(a, b, c):
+        return float(F(a) * F(b) + F(c))
+
+    rng = np.random.default_rng(9)
+    worst = 0.0
+    for d in np.concatenate([10.0 ** rng.uniform(-30, 30, 400), [1.0, 2.0, 0.5, 3.0]]):
+        d = float(d)
+        ref = 1.0 / math.sqrt(d)
+        s32 = float(np.float32(ref))
+        for k in (-8, -3, 0, 3, 8):
+            y = float(np.float32(s32) + np.float32(k) * np.spacing(np.float32(s32)))
+            e = fma(-(d * y), y, 1.0)
+            out = fma(y * e, fma(0.375, e, 0.5), y)
+            # exact 1/sqrt(d) to ~1e-30 through a Newton step in rationals
+            r = F(ref)
+            r = r * (F(3) - F(d) * r * r) / 2
+            err = abs(F(out) - r) / r
+            worst = max(worst, float(err))
+    assert worst < 2 * 2.0 ** -52

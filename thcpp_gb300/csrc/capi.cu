@@ -291,6 +291,11 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
     h->c.qrcp_all_pairs = value != 0.0;
     return THC_OK;
   }
+  if (!strcmp(key, "spin_limit")) {
+    if (value < 0 || value > 1e12) return THC_ERR_ARG;
+    h->c.spin_limit = (long long)value;
+    return THC_OK;
+  }
   if (!strcmp(key, "equilibrate")) {
     h->c.equilibrate = value != 0.0;
     return THC_OK;

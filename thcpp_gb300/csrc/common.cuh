@@ -110,6 +110,8 @@ struct Ctx {
   // balanced (an ill-conditioned C with a wide diagonal otherwise loses most of the 42 bits
   // of its small entries).
   int equilibrate = 1;
+  // Polls of an mbarrier before a bounded device wait gives up (THC_ERR_TIMEOUT).
+  long long spin_limit = 1LL << 24;
   // Instantiated k-means iteration graphs, most recently used last, keyed by every kernel
   // argument they bake in.
   std::vector<std::pair<std::vector<long long>, cudaGraphExec_t>> km_graphs;

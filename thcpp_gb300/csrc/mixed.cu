@@ -43,9 +43,11 @@ __global__ void gather_rows_m(const double* __restrict__ phi, long long ng, int 
   }
 }
 
+// With a Coulomb kernel that is negative somewhere, sq / sqd carry sqrt(max(w v_sym, 0))
+// and sqn / sqdn sqrt(max(-w v_sym, 0)): M = A+ A+^T - A- A-^T.
 __global__ void coulomb_weights_m(const double* __restrict__ v, int n0, int n1, int n2,
                                   double* dsym, double* danti, float* sq, double* sqd,
-                                  int* n_anti)
+                                  int* n_anti, float* sqn, double* sqdn, int* n_neg)
 {
   int nc = n2 / 2 + 1;
   long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -63,6 +65,10 @@ __global__ void coulomb_weights_m(const double* __restrict__ v, int n0, int n1, 
   const double rt = sqrt(fmax(ds, 0.0));
   sq[e] = (float)rt;
   if (sqd) sqd[e] = rt;
+  const double rn = sqrt(fmax(-ds, 0.0));
+  sqn[e] = (float)rn;
+  if (sqdn) sqdn[e] = rn;
+  if (ds < 0.0) atomicAdd(n_neg, 1);
   double a = w * 0.5 * (vp - vn);
   danti[e] = a;
   if (a != 0.0) atomicAdd(n_anti, 1);
@@ -165,6 +171,13 @@ __global__ void add_shift_scaled(double* A, int n, const double* dmean, double r
 
 __global__ void scaled_threshold(const double* dmean_s, double* thr) { *thr = 1e-13 * *dmean_s; }
 
+// y[i] -= x[i]
+__global__ void sub_from(const double* __restrict__ x, long long n, double* y)
+{
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) y[i] -= x[i];
+}
+
 // y[i] = x[i] + a y[i]
 __global__ void axpy_from(const double* __restrict__ x, double a, long long n, double* y)
 {
@@ -226,8 +239,8 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   float2* zg = (float2*)zreg;                      // Z: N_g x N_mu, double-word
   void* zeta = zreg;                               // zeta^T: N_mu x N_g (after Z is sliced)
   void* zhat = zreg + zeta_bytes;                  // N_mu x N_c complex
-  // dsym (FP64), sqrt(dsym) in FP64, then sqrt(dsym) in FP32.
-  double* dsym = (double*)ws_get(c, WS_DSYM, (2 * sizeof(double) + sizeof(float)) * nc + 64);
+  // dsym (FP64), sqrt(dsym) and sqrt(-dsym) in FP64, then both in FP32.
+  double* dsym = (double*)ws_get(c, WS_DSYM, (3 * sizeof(double) + 2 * sizeof(float)) * nc + 64);
   double* danti = (double*)ws_get(c, WS_DANTI, sizeof(double) * nc);
   double* Mw = (double*)ws_get(c, WS_M, sizeof(double) * 4 * nn);
   double* Lw = (double*)ws_get(c, WS_L, sizeof(double) * 2 * nn);
@@ -248,7 +261,9 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
       !sa || !sb || !ex)
     return set_error(c, THC_ERR_NOMEM, "thc_isdf (mixed): workspace allocation failed");
   double* sqd = dsym + nc;
-  float* sq = (float*)(dsym + 2 * nc);
+  double* sqdn = dsym + 2 * nc;
+  float* sq = (float*)(dsym + 3 * nc);
+  float* sqn = sq + nc;
   int* ea = ex;
   int* eb = ex + mu_pad;
   int* et = eb + ng_pad + 64;       // exponents of the refinement's W slices
@@ -261,6 +276,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   int* bad = (int*)(scr + 512);
   int* n_anti = bad + 1;
   int* gemm_err = bad + 2;
+  int* n_neg = bad + 3;
   double* orb_dev = nullptr;
   if (out_orb) {
     orb_dev = is_device_ptr(out_orb) ? out_orb
@@ -499,26 +515,27 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   if ((st = fft_forward(c, n0, n1, n2, nmu, f64fft ? CUFFT_D2Z : CUFFT_R2C, zeta, zhat)))
     return st;
   coulomb_weights_m<<<(int)cdiv(nc, 256), 256, 0, s>>>(coul, n0, n1, n2, dsym, danti, sq,
-                                                       f64fft ? sqd : nullptr, n_anti);
+                                                       f64fft ? sqd : nullptr, n_anti, sqn,
+                                                       f64fft ? sqdn : nullptr, n_neg);
   THC_LAUNCHED(c, "coulomb_weights");
-  int h_anti = 0;
+  int h_anti = 0, h_neg = 0;
   THC_CUDA(c, cudaMemcpyAsync(&h_anti, n_anti, sizeof(int), cudaMemcpyDeviceToHost, s));
-  // Re M (lower) = A A^T with A = zeta_hat (interleaved re, im) scaled by sqrt(w v_sym).
-  const SliceBuf zh = slices(sb, ea, mu_pad, k2_pad, sm);
-  if (f64fft)
-    st = oz_slice_rows_f64(c, (const double*)zhat, nmu, 2 * nc, 2 * nc, 1, sqd, 1, zh);
-  else
-    st = oz_slice_rows_f32(c, (const float*)zhat, nmu, 2 * nc, 2 * nc, sq, 1, zh);
-  if (st) return st;
+  THC_CUDA(c, cudaMemcpyAsync(&h_neg, n_neg, sizeof(int), cudaMemcpyDeviceToHost, s));
   double* mre = Mw;
   double* xim = Mw + nn;
   double* mcx = Mw + 2 * nn;
-  {
+  // Re M (lower) = A A^T with A = zeta_hat (interleaved re, im) scaled by sqrt(w v_sym)
+  // (by sqrt(max(+-w v_sym, 0)) for the two parts of a kernel with negative values).
+  auto coulomb_product = [&](const float* scale32, const double* scale64, double* out) -> int {
+    const SliceBuf zh = slices(sb, ea, mu_pad, k2_pad, sm);
+    int r = f64fft ? oz_slice_rows_f64(c, (const double*)zhat, nmu, 2 * nc, 2 * nc, 1, scale64, 1, zh)
+                   : oz_slice_rows_f32(c, (const float*)zhat, nmu, 2 * nc, 2 * nc, scale32, 1, zh);
+    if (r) return r;
     OzArgs g;
     g.M = nmu; g.N = nmu; g.K = 2 * nc;
     g.a = zh.operand();
     g.b = g.a;
-    g.levels = sm; g.epilogue = OZ_STORE_F64; g.C = mre; g.ldc = nmu; g.lower_only = 1;
+    g.levels = sm; g.epilogue = OZ_STORE_F64; g.C = out; g.ldc = nmu; g.lower_only = 1;
     g.tag = "oz_M";
     // Long K (2 N_c) and a small N_mu x N_mu output: split K over CTAs.
     g.ksplit = oz_choose_split(nmu, nmu, 2 * nc, true);
@@ -526,10 +543,17 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
       g.part = (double*)ws_get(c, WS_PART, sizeof(double) * g.ksplit * nn);
       if (!g.part) return set_error(c, THC_ERR_NOMEM, "thc_isdf: split-K buffer");
     }
-    if ((st = gemm(g))) return st;
-  }
+    return gemm(g);
+  };
+  if ((st = coulomb_product(sq, sqd, mre))) return st;
   THC_CUDA(c, cudaStreamSynchronize(s));
   int nb2 = (int)cdiv(nn, 256);
+  if (h_neg > 0) {
+    double* mneg = Cinv;                          // free once zeta is formed
+    if ((st = coulomb_product(sqn, sqdn, mneg))) return st;
+    sub_from<<<nb2, 256, 0, s>>>(mneg, nn, mre);
+    THC_LAUNCHED(c, "sub_from");
+  }
   if (h_anti > 0) {
     if (f64fft)
       imag_part_c64<<<nb2, 256, 0, s>>>((const double2*)zhat, nc, nmu, danti, xim);

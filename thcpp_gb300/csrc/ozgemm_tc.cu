@@ -40,7 +40,7 @@ constexpr int kSmemGuard = 16 * 1024;   // slack after the buffers (descriptor r
 constexpr int TEPI_WARPS = 8;
 constexpr int kGroupM = 8;    // m-tiles per group of the tile order
 constexpr int TTHREADS = 32 * (2 + TEPI_WARPS);
-constexpr long long kSpinLimit = 1LL << 24;
+constexpr long long kDrainLimit = 1LL << 22;   // teardown waits after an abort
 
 __device__ __forceinline__ uint32_t su32(const void* p)
 {
@@ -75,15 +75,24 @@ __device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity)
   return ok != 0;
 }
 
-// Bounded wait: false (and *abort set) when the barrier phase never completes.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort)
+// Bounded wait: false (and *abort set) when the barrier phase does not complete within
+// `limit` polls (the context option "spin_limit"; 0 gives up at once).
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort,
+                                          long long limit)
 {
-  for (long long i = 0; i < kSpinLimit; i++) {
+  for (long long i = 0; i < limit; i++) {
     if (mbar_try(b, parity)) return true;
     if (*abort) return false;
   }
   *abort = 1;
   return false;
+}
+
+// Teardown wait after an abort: polls a phase a bounded number of times, whatever *abort.
+__device__ __forceinline__ void mbar_drain(uint64_t* b, uint32_t parity)
+{
+  for (long long i = 0; i < kDrainLimit; i++)
+    if (mbar_try(b, parity)) return;
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
@@ -219,6 +228,7 @@ struct TcArgs {
   int epilogue;
   int lower_only;
   int* error;                         // set to 1 when a bounded wait gave up
+  long long spin_limit;               // polls before a wait gives up
   int ksplit;
   double* part;
 };
@@ -274,8 +284,11 @@ __global__ void __launch_bounds__(TTHREADS, 1)
   uint64_t* acc_empty = acc_full + 1;      // exact levels drained
   uint64_t* acc_empty_hi = acc_empty + 1;  // the level >= 3 accumulator drained
   uint64_t* acc_full_hi = acc_empty_hi + 1;  // the level >= 3 accumulator ready
-  uint32_t* tmem_slot = (uint32_t*)(acc_full_hi + 1);
+  uint64_t* mma_done = acc_full_hi + 1;      // every issued MMA has completed (teardown)
+  uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
   volatile int* abort = (volatile int*)(tmem_slot + 1);
+  volatile int* issued = abort + 1;          // stages whose loads the producer issued
+  volatile int* consumed = issued + 1;       // stages the MMA issuer saw land
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   long long kbeg = 0, kend = g.K;
@@ -301,7 +314,10 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     mbar_init(acc_empty, TEPI_WARPS);
     mbar_init(acc_empty_hi, TEPI_WARPS);
     mbar_init(acc_full_hi, 1);
+    mbar_init(mma_done, 1);
     *abort = 0;
+    *issued = 0;
+    *consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 1) {
@@ -320,8 +336,9 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       for (int it = 0; it < nstages; it++) {
         int s = it % NST;
         uint32_t ph = (uint32_t)((it / NST) & 1);
-        if (!mbar_wait(&empty[s], ph ^ 1, abort)) break;
+        if (!mbar_wait(&empty[s], ph ^ 1, abort, g.spin_limit)) break;
         unsigned char* st = smem + s * STAGE_BYTES;
+        *issued = it + 1;
         mbar_expect_tx(&full[s], STAGE_BYTES);
         const long long k = kbeg + (long long)it * BK;
         // Plain maps: x = k, y = slice row.  Tiled maps (64-byte rows): x = k % 32 and y
@@ -347,7 +364,8 @@ __global__ void __launch_bounds__(TTHREADS, 1)
         int chunk = it / Cfg::CHUNK_STAGES;
         bool chunk_first = (it % Cfg::CHUNK_STAGES) == 0;
         bool chunk_last = ((it + 1) % Cfg::CHUNK_STAGES) == 0 || it + 1 == nstages;
-        if (!mbar_wait(&full[s], ph, abort)) break;
+        if (!mbar_wait(&full[s], ph, abort, g.spin_limit)) break;
+        *consumed = it + 1;
         asm volatile("tcgen05.fence::after_thread_sync;\n");
         unsigned char* st = smem + s * STAGE_BYTES;
         uint32_t a0 = su32(st), b0 = su32(st + LV * A_BYTES);
@@ -400,18 +418,18 @@ __global__ void __launch_bounds__(TTHREADS, 1)
           // Both drains pending: the epilogue empties the level >= 3 accumulator first, so
           // those pairs go first and cover the drain of the exact levels.
           if (wait_hi) {
-            if (!mbar_wait(acc_empty_hi, (uint32_t)((hp - 1) & 1), abort)) break;
+            if (!mbar_wait(acc_empty_hi, (uint32_t)((hp - 1) & 1), abort, g.spin_limit)) break;
             asm volatile("tcgen05.fence::after_thread_sync;\n");
           }
           issue_hi();
-          if (!mbar_wait(acc_empty, (uint32_t)((chunk - 1) & 1), abort)) break;
+          if (!mbar_wait(acc_empty, (uint32_t)((chunk - 1) & 1), abort, g.spin_limit)) break;
           asm volatile("tcgen05.fence::after_thread_sync;\n");
           issue_ex();
         } else {
           // At most the level >= 3 drain pending: the exact pairs cover it.
           issue_ex();
           if (wait_hi) {
-            if (!mbar_wait(acc_empty_hi, (uint32_t)((hp - 1) & 1), abort)) break;
+            if (!mbar_wait(acc_empty_hi, (uint32_t)((hp - 1) & 1), abort, g.spin_limit)) break;
             asm volatile("tcgen05.fence::after_thread_sync;\n");
           }
           issue_hi();
@@ -420,6 +438,8 @@ __global__ void __launch_bounds__(TTHREADS, 1)
         if (LV > 3 && hp_last) umma_commit(acc_full_hi);
         if (chunk_last) umma_commit(acc_full);
       }
+      // Completion of every MMA this thread issued, for the teardown.
+      umma_commit(mma_done);
     }
   } else {
     // ------------------------------------------------------------------ epilogue
@@ -450,7 +470,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       // The level >= 3 periods of this chunk first (the MMA waits for each).
       const int hp_end = min(nhp, (ch + 1) * (Cfg::CHUNK_STAGES / HS));
       for (; LV > 3 && hpd < hp_end; hpd++) {
-        if (!mbar_wait(acc_full_hi, (uint32_t)(hpd & 1), abort)) { ok = false; break; }
+        if (!mbar_wait(acc_full_hi, (uint32_t)(hpd & 1), abort, g.spin_limit)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
         for (int b = 0; b < 8; b++) {
@@ -465,7 +485,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
         if (lane == 0) mbar_arrive(acc_empty_hi);
       }
       if (!ok) break;
-      if (!mbar_wait(acc_full, (uint32_t)(ch & 1), abort)) { ok = false; break; }
+      if (!mbar_wait(acc_full, (uint32_t)(ch & 1), abort, g.spin_limit)) { ok = false; break; }
       asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
       for (int b = 0; b < 8; b++) {   // 8 columns at a time (register pressure)
@@ -496,7 +516,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     }
     // The level >= 3 period that ends with the last stage.
     for (; ok && LV > 3 && hpd < nhp; hpd++) {
-      if (!mbar_wait(acc_full_hi, (uint32_t)(hpd & 1), abort)) { ok = false; break; }
+      if (!mbar_wait(acc_full_hi, (uint32_t)(hpd & 1), abort, g.spin_limit)) { ok = false; break; }
       asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
       for (int b = 0; b < 8; b++) {
@@ -595,7 +615,18 @@ __global__ void __launch_bounds__(TTHREADS, 1)
   // ---------------------------------------------------------------------- teardown
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
-  if (*abort && threadIdx.x == 0) atomicExch(g.error, 1);
+  if (threadIdx.x == 0) {
+    // Before shared memory and TMEM are released, bounded: after an abort the loads issued
+    // but never consumed land (each stage's phase completes); in every case the MMAs issued
+    // so far have completed (mma_done; at once on the normal path).
+    if (*abort) {
+      atomicExch(g.error, 1);
+      for (int it = *consumed; it < *issued; it++)
+        mbar_drain(&full[it % NST], (uint32_t)((it / NST) & 1));
+    }
+    mbar_drain(mma_done, 0);
+  }
+  __syncthreads();
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;\n");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
@@ -662,6 +693,7 @@ int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
   t.hi_stages = std::max(1, std::min(Cfg::CHUNK_STAGES, c->tc_hi_stages / (BK / 16)));
   t.ea = g.a.e; t.eb = g.b.e; t.C = g.C; t.ldc = g.ldc;
   t.epilogue = g.epilogue; t.lower_only = g.lower_only; t.error = err_flag;
+  t.spin_limit = c->spin_limit;
   t.ksplit = std::max(1, g.ksplit); t.part = g.part;
   const size_t smem = Cfg::SMEM;
   THC_CUDA(c, cudaFuncSetAttribute(ozgemm_tc_kernel<LV, BK>,
