@@ -25,6 +25,7 @@
  *                               757-790), the first thc_cfac * N_o pivots sorted (:149-160)
  *   thc_qrcp_complex            thc_qrcp for complex aoR
  *   thc_isdf_complex            the same for complex aoR (P = Phi_mu^H Phi, :117; Z = P o conj(P))
+ *   thc_isdf_half_complex       the same for complex aoR / aoR_half
  *   thc_isdf_interpolating_vectors  the least-squares solution zeta of the last ISDF call
  *                               (interpolating_vectors.cpp:416)
  *   thc_isdf_half               IVecs with rotate = true (src/interpolating_vectors.cpp:45-49):
@@ -232,6 +233,23 @@ int thc_isdf_half(thc_ctx* ctx, const double* phi, long long ng, int norb, const
  * yet, or a later QRCP or failed ISDF call reused the workspace).
  */
 int thc_isdf_interpolating_vectors(thc_ctx* ctx, long long ng, int nmu, double* out_zeta);
+
+/*
+ * thc_isdf_half for complex orbitals (k-point data): phi (ng x norb x 2) and phi_occ
+ * (ng x nocc x 2) are `aoR` and `aoR_half` as stored ((re, im) pairs, C order).  As the
+ * reference forms them (src/interpolating_vectors.cpp:143-161, :384-391, :261-273):
+ * P = Phi_mu^H Phi, P_occ = Phi_occ,mu^H Phi_occ, Z = P_occ o conj(P), C = Z[:, idx] (complex,
+ * not Hermitian), zeta = conj(C^{-1} Z), IVG / IVMG its forward / backward unnormalised FFTs
+ * and M = IVMG^T diag(v) IVG (HalfTransformedMuv, no Cholesky factor).  C is inverted by
+ * Gauss-Jordan elimination with partial pivoting in place of the reference's QR
+ * (thc_isdf_stats.c_min_pivot = min / max |pivot|^2); THC_ERR_NOT_PD if a column has no
+ * non-zero pivot.  out_orbitals / out_occ_orbitals receive the complex orbitals at the
+ * points (HalfTransformedFullOrbitals / HalfTransformedOccOrbitals).  FP64 in both precisions.
+ */
+int thc_isdf_half_complex(thc_ctx* ctx, const double* phi, long long ng, int norb,
+                          const double* phi_occ, int nocc, const int* idx, int nmu,
+                          const int* mesh, const double* coulG, double* out_orbitals,
+                          double* out_occ_orbitals, double* out_M, thc_isdf_stats* stats);
 
 /*
  * Interpolating points by QR with column pivoting of Z^T (the reference's "qrcp" point

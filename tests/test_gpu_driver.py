@@ -170,3 +170,35 @@ def test_driver_empty_cluster_exits(tmp_path, lib):
     r = subprocess.run([build.DRIVER, str(inp)], capture_output=True, text=True, timeout=600)
     assert r.returncode == 1
     assert "CRITICAL ERROR: Found centroid with weight ~ 0" in r.stdout
+
+
+def test_driver_half_rotated_complex(tmp_path, lib):
+    """half_rotated on a complex orbital file: the half pass runs thc_isdf_half_complex and
+    HalfTransformedMuv matches the oracle's literal complex half-rotated form."""
+    from tests.test_oracle import complex_orbitals
+    build.build_host()
+    s = system("tiny")
+    pc = complex_orbitals(s.phi)
+    z = synth.System(**{**s.__dict__, "phi": pc})
+    orb = str(tmp_path / "orbitals.h5")
+    out = str(tmp_path / "thc.h5")
+    synth.write_orbital_file(z, orb, half_rotate=True)
+    inp = tmp_path / "input.json"
+    d = synth.input_json(z, orb, out)
+    d["half_rotated"] = True
+    d["thc_half_cfac"] = 2
+    inp.write_text(json.dumps(d))
+    r = subprocess.run([build.DRIVER, str(inp)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    f = h5.Reader(out)
+    hs = synth.System(**{**s.__dict__, "thc_cfac": 2})
+    href = oracle.kmeans_system(hs)
+    po = pc[:, : s.nocc]
+    for part, src in (("Full", pc), ("Occ", po)):
+        assert np.array_equal(f.read(f"/Hamiltonian/THC/HalfTransformed{part}InterpIndx"), href.idx)
+        o = f.read(f"/Hamiltonian/THC/HalfTransformed{part}Orbitals")
+        assert np.array_equal(o[..., 0] + 1j * o[..., 1], src[href.idx].T)
+    M = f.read("/Hamiltonian/THC/HalfTransformedMuv")
+    M = M[..., 0] + 1j * M[..., 1]
+    ref = oracle.isdf_half_reference(pc, po, href.idx, s.mesh, s.coulG)
+    assert np.linalg.norm(M - ref) / np.linalg.norm(ref) < 1e-6

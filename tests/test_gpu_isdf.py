@@ -226,3 +226,30 @@ def test_isdf_complex_matches_oracle(gpu_ctx_fp64, gpu_ctx_mixed, prec, name, to
     assert np.allclose(np.triu(L, 1), 0)
     assert _rel(L @ L.conj().T, M) < 1e-12
     assert np.array_equal(_cplx(r["orbitals"]), pc[idx].T)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("name,npts,tol", [("tiny", None, 1e-6), ("c2", 128, 1e-9)])
+def test_isdf_half_complex_matches_reference_form(gpu_ctx_fp64, gpu_ctx_mixed, prec, name, npts,
+                                                  tol):
+    """thc_isdf_half_complex (FP64 in both precisions) against the oracle's literal
+    half-rotated form with complex orbitals (complex P and P_occ, Z = P_occ o conj(P), QR
+    least squares, forward and backward C2C FFTs, IVMG^T IVG).  tiny: cond(C) 1.7e10; C2 with
+    the first 128 k-means points: cond 8e5."""
+    from tests.test_oracle import complex_orbitals
+    ctx = gpu_ctx_fp64 if prec == "fp64" else gpu_ctx_mixed
+    s = system(name)
+    idx = kmeans_idx(name)
+    if npts:
+        idx = np.ascontiguousarray(idx[:npts])
+    pc = complex_orbitals(s.phi)
+    po = np.ascontiguousarray(pc[:, : s.norb // 2])
+    r = ctx.isdf_half_complex(pc, po, idx, s.mesh, s.coulG)
+    assert r["status"] == 0
+    ref = oracle.isdf_half_reference(pc, po, idx, s.mesh, s.coulG)
+    err = _rel(_cplx(r["M"]), ref)
+    print(f"{name} {prec}: half complex ||dM||/||M|| = {err:.3e}")
+    assert err < tol
+    assert np.array_equal(_cplx(r["orbitals"]), pc[idx].T)
+    assert np.array_equal(_cplx(r["occ_orbitals"]), po[idx].T)
+    assert 0 < r["stats"].c_min_pivot <= 1

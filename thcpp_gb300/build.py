@@ -21,7 +21,7 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libthc_gb300.so")
 
 CUDA_SOURCES = ["capi.cu", "kmeans.cu", "dense64.cu", "isdf.cu", "mixed.cu", "ozgemm.cu",
-                "ozgemm_tc.cu", "noalloc.cu", "synthgen.cu", "qrcp.cu"]
+                "ozgemm_tc.cu", "noalloc.cu", "synthgen.cu", "qrcp.cu", "halfc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST = os.path.join(PKG, "host")
 HOST_SOURCES = ["h5lite.cpp", "h5lite_capi.cpp", "gpu_context.cpp", "kmeans.cpp", "qrcp.cpp", "interpolating_points.cpp",

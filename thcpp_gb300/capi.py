@@ -35,7 +35,7 @@ EXPORTS = [
     "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_ctx_kernel_time",
     "thc_kmeans_history", "thc_factorize_batched", "thc_kmeans_noalloc",
     "thc_synth_gaussian_basis", "thc_isdf_half", "thc_qrcp", "thc_isdf_complex",
-    "thc_qrcp_complex", "thc_isdf_interpolating_vectors",
+    "thc_qrcp_complex", "thc_isdf_interpolating_vectors", "thc_isdf_half_complex",
 ]
 
 
@@ -127,10 +127,12 @@ def load(build_if_missing: bool = False):
     lib.thc_qrcp_complex.argtypes = [vp, vp, cll, ci, ci, vp, vp, vp, ctypes.POINTER(QrcpStats)]
     lib.thc_qrcp.argtypes = [vp, vp, cll, ci, vp, ci, ci, vp, vp, vp, ctypes.POINTER(QrcpStats)]
     lib.thc_isdf_interpolating_vectors.argtypes = [vp, cll, ci, vp]
+    lib.thc_isdf_half_complex.argtypes = [vp, vp, cll, ci, vp, ci, vp, ci, vp, vp, vp, vp, vp,
+                                          ctypes.POINTER(IsdfStats)]
     for f in ("thc_ctx_create", "thc_ctx_destroy", "thc_ctx_set_stream", "thc_ctx_set_option",
               "thc_kmeans_initial_indices", "thc_kmeans", "thc_isdf", "thc_kmeans_noalloc",
               "thc_isdf_half", "thc_qrcp", "thc_isdf_complex", "thc_qrcp_complex",
-              "thc_isdf_interpolating_vectors"):
+              "thc_isdf_interpolating_vectors", "thc_isdf_half_complex"):
         getattr(lib, f).restype = ci
     _lib = lib
     return lib
@@ -354,6 +356,27 @@ class Context:
                                    _ptr(idx), _ptr(order), _ptr(diag), ctypes.byref(stats))
         self._check(st, "thc_qrcp")
         return dict(idx=idx, order=order, diag=diag, stats=stats)
+
+    def isdf_half_complex(self, phi, phi_occ, idx, mesh, coulG):
+        """thc_isdf_half_complex: complex128 (N_g, N_o) / (N_g, N_occ) orbitals, or their
+        float64 (..., 2) pairs; returns M, the complex orbitals at the points and stats."""
+        if _is_complex(phi):
+            phi = _complex_pairs(phi)
+        if _is_complex(phi_occ):
+            phi_occ = _complex_pairs(phi_occ)
+        ng, no, nocc = int(phi.shape[0]), int(phi.shape[1]), int(phi_occ.shape[1])
+        nmu = int(idx.shape[0])
+        mesh_a = np.ascontiguousarray(np.asarray(mesh, dtype=np.int32).reshape(3))
+        out_M = np.zeros((nmu, nmu, 2))
+        out_orb = np.zeros((no, nmu, 2))
+        out_occ = np.zeros((nocc, nmu, 2))
+        stats = IsdfStats()
+        st = self.lib.thc_isdf_half_complex(self.h, _ptr(phi), ng, no, _ptr(phi_occ), nocc,
+                                            _ptr(idx), nmu, _ptr(mesh_a), _ptr(coulG),
+                                            _ptr(out_orb), _ptr(out_occ), _ptr(out_M),
+                                            ctypes.byref(stats))
+        self._check(st, "thc_isdf_half_complex")
+        return dict(M=out_M, orbitals=out_orb, occ_orbitals=out_occ, stats=stats, status=st)
 
     def isdf_half(self, phi, phi_occ, idx, mesh, coulG, shift_rel=-1.0):
         """thc_isdf_half: half-rotated interpolating vectors and M (no Cholesky factor)."""

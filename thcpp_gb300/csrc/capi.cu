@@ -409,6 +409,18 @@ int thc_isdf_half(thc_ctx* h, const double* phi, long long ng, int norb, const d
                        out_M, nullptr, stats, phi_occ, nocc, out_occ_orbitals);
 }
 
+int thc_isdf_half_complex(thc_ctx* h, const double* phi, long long ng, int norb,
+                          const double* phi_occ, int nocc, const int* idx, int nmu,
+                          const int* mesh, const double* coulG, double* out_orbitals,
+                          double* out_occ_orbitals, double* out_M, thc_isdf_stats* stats)
+{
+  if (!h) return THC_ERR_ARG;
+  if (cudaSetDevice(h->c.device) != cudaSuccess) return THC_ERR_CUDA;
+  if (stats) memset(stats, 0, sizeof(*stats));
+  return thc::isdf_half_complex_run(&h->c, phi, ng, norb, phi_occ, nocc, idx, nmu, mesh, coulG,
+                                    out_orbitals, out_occ_orbitals, out_M, stats);
+}
+
 int thc_isdf_interpolating_vectors(thc_ctx* h, long long ng, int nmu, double* out_zeta)
 {
   if (!h || !out_zeta) return THC_ERR_ARG;

@@ -195,7 +195,10 @@ int get_plan(Ctx* c, int n0, int n1, int n2, int batch, cufftType type, cufftHan
     long long ng = (long long)n0 * n1 * n2;
     long long nc = (long long)n0 * n1 * (n2 / 2 + 1);
     size_t work = 0;
-    cufftResult r = cufftMakePlanMany64(p, 3, n, nullptr, 1, ng, nullptr, 1, nc, type, batch, &work);
+    // Real-to-complex outputs are half spectra; complex-to-complex ones full grids.
+    const long long odist = type == CUFFT_Z2Z ? ng : nc;
+    cufftResult r = cufftMakePlanMany64(p, 3, n, nullptr, 1, ng, nullptr, 1, odist, type, batch,
+                                        &work);
     if (r != CUFFT_SUCCESS) {
       cufftDestroy(p);
       return set_error(c, THC_ERR_CUFFT, "cufftMakePlanMany64 failed (%d)", (int)r);

@@ -54,6 +54,13 @@ int kmeans_run(Ctx* c, const double* grid, const double* rho, long long ng, int 
 
 int kmeans_history(Ctx* c, double* diff, double* pct, int n);
 
+// Half-rotated ISDF with complex orbitals (halfc.cu): phi (N_g x N_o) and phi_occ
+// (N_g x N_occ) as (re, im) pairs; FP64 in both precisions.
+int isdf_half_complex_run(Ctx* c, const double* phi, long long ng, int no, const double* phi_occ,
+                          int nocc, const int* idx, int nmu, const int* mesh, const double* coul,
+                          double* out_orb, double* out_orb_occ, double* out_M,
+                          thc_isdf_stats* stats);
+
 int qrcp_run(Ctx* c, const double* phi, long long ng, int no, const double* phi_occ, int nocc,
              int npts, int* out_idx, int* out_order, double* out_diag, thc_qrcp_stats* stats,
              bool complex_orbitals = false);

@@ -1257,28 +1257,42 @@ __global__ void km_tile_boxes(KmBufs b, float* box)
   }
 }
 
-// map_to_grid with exact pruning: one warp per centroid (two per block, so that every SM
-// takes part).  U = min over tiles of the largest squared distance from the centroid to the
-// tile box bounds the nearest squared distance; only tiles whose smallest squared distance
-// is <= U (1 + 1e-4) + slack32 are scanned.  The bounds are FP32 (the FP64 pipe runs two
-// lanes per clock here); the margins are those of the pruned FP32 assign, far above the FP32
-// rounding of the boxes and distances, so the FP64 nearest point and every sqrt tie survive.
-// Tiles are not in grid-index order, so candidates merge on (sqrt distance, grid index),
-// which keeps the reference's first-index rule (classify with the roles swapped,
-// src/kmeans.cpp:146-150).
-constexpr int kMapThreads = 64;
+// map_to_grid with exact pruning: one block of kMapWarps warps per centroid, the warps
+// taking every kMapWarps-th 32-tile stretch.  U = min over tiles of the largest squared
+// distance from the centroid to the tile box bounds the nearest squared distance; only
+// tiles whose smallest squared distance is <= U (1 + 1e-4) + slack32 are scanned.  The
+// bounds are FP32 (the FP64 pipe runs two lanes per clock here); the margins are those of
+// the pruned FP32 assign, far above the FP32 rounding of the boxes and distances, so the
+// FP64 nearest point and every sqrt tie survive.  Tiles are not in grid-index order, so
+// candidates merge on (sqrt distance, grid index), which keeps the reference's first-index
+// rule (classify with the roles swapped, src/kmeans.cpp:146-150).
+constexpr int kMapWarps = 8;
+constexpr int kMapThreads = 32 * kMapWarps;
 __global__ void __launch_bounds__(kMapThreads) km_map_pruned(KmBufs b, const float* __restrict__ box,
                                                              int ntiles, int* idx)
 {
   const double* cen = b.cen + (size_t)b.st->final_buf * 3 * b.nmu;
-  int lane = threadIdx.x & 31;
-  long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long k = blockIdx.x;
   if (k >= b.nmu) return;
+  __shared__ float redf[kMapWarps];
+  __shared__ double reds[kMapWarps];
+  __shared__ int redk[kMapWarps];
   double c3[3] = {cen[k], cen[b.nmu + k], cen[2 * b.nmu + k]};
   const float* cf = b.cen32 + (size_t)b.st->final_buf * 3 * b.nmu;
   const float f3[3] = {cf[k], cf[b.nmu + k], cf[2 * b.nmu + k]};
+  // Block minimum of one float per thread (every thread gets it).
+  auto block_min = [&](float v) {
+    for (int off = 16; off; off >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, off));
+    __syncthreads();
+    if (lane == 0) redf[warp] = v;
+    __syncthreads();
+    float m = redf[0];
+    for (int w = 1; w < kMapWarps; w++) m = fminf(m, redf[w]);
+    return m;
+  };
   float u = INFINITY;
-  for (int t = lane; t < ntiles; t += 32) {
+  for (int t = threadIdx.x; t < ntiles; t += kMapThreads) {
     float ub = 0.f;
     for (int d = 0; d < 3; d++) {
       float a = f3[d] - box[t * 6 + d], e = f3[d] - box[t * 6 + 3 + d];
@@ -1286,7 +1300,7 @@ __global__ void __launch_bounds__(kMapThreads) km_map_pruned(KmBufs b, const flo
     }
     u = fminf(u, ub);
   }
-  for (int off = 16; off; off >>= 1) u = fminf(u, __shfl_xor_sync(0xffffffffu, u, off));
+  u = block_min(u);
   const float cut = u * (1.0f + 1e-4f) + (float)b.st->slack32;
   // The candidate tiles' points are scanned twice: first in FP32 for the smallest squared
   // distance m, then in FP64 only for points whose FP32 squared distance is within
@@ -1298,7 +1312,7 @@ __global__ void __launch_bounds__(kMapThreads) km_map_pruned(KmBufs b, const flo
     const float thr32 = pass ? m32 * (1.0f + 1e-4f) + (float)b.st->slack32 : 0.f;
     double bs = CUDART_INF, bm = CUDART_INF;
     int bk = 0x7fffffff;
-    for (int t0 = 0; t0 < ntiles; t0 += 32) {
+    for (int t0 = warp * 32; t0 < ntiles; t0 += 32 * kMapWarps) {
       int t = t0 + lane;
       bool cand = false;
       if (t < ntiles) {
@@ -1334,7 +1348,7 @@ __global__ void __launch_bounds__(kMapThreads) km_map_pruned(KmBufs b, const flo
       }
     }
     if (!pass) {
-      for (int off = 16; off; off >>= 1) m32 = fminf(m32, __shfl_xor_sync(0xffffffffu, m32, off));
+      m32 = block_min(m32);
       continue;
     }
     for (int off = 16; off; off >>= 1) {
@@ -1342,7 +1356,13 @@ __global__ void __launch_bounds__(kMapThreads) km_map_pruned(KmBufs b, const flo
       int k2 = __shfl_xor_sync(0xffffffffu, bk, off);
       if (s2 < bs || (s2 == bs && k2 < bk)) { bs = s2; bk = k2; }
     }
-    if (lane == 0) idx[k] = bk;
+    if (lane == 0) { reds[warp] = bs; redk[warp] = bk; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < kMapWarps; w++)
+        if (reds[w] < bs || (reds[w] == bs && redk[w] < bk)) { bs = reds[w]; bk = redk[w]; }
+      idx[k] = bk;
+    }
   }
 }
 
@@ -1668,7 +1688,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
     float* box = (float*)part_s;   // 6 floats per tile fit in the partials buffer
     km_tile_boxes<<<ntiles, 256, 0, s>>>(b, box);
     THC_LAUNCHED(c, "km_tile_boxes");
-    km_map_pruned<<<(int)cdiv((long long)nmu * 32, kMapThreads), kMapThreads, 0, s>>>(b, box, ntiles, didx);
+    km_map_pruned<<<nmu, kMapThreads, 0, s>>>(b, box, ntiles, didx);
     THC_LAUNCHED(c, "km_map_pruned");
   } else {
     dim3 mg((unsigned)nch, (unsigned)cdiv(nmu, 256));

@@ -9,8 +9,9 @@
 //   dump_qmcpack_data       hcore, Energies, occups, dims, THC/dims (:210-245)
 //   rotate = true           the half-rotated variant (:45-49, setup_CZt_half :143-161): reads
 //                           aoR_half as well, writes HalfTransformed{Full,Occ}{Orbitals,
-//                           InterpIndx}, and kernel writes HalfTransformedMuv (thc_isdf_half)
-//                           instead of Luv, as dump_thc_data does (:317-328)
+//                           InterpIndx}, and kernel writes HalfTransformedMuv (thc_isdf_half;
+//                           thc_isdf_half_complex when aoR or aoR_half is complex) instead of
+//                           Luv, as dump_thc_data does (:317-328)
 // Datasets are written contiguous rather than gzip-chunked (h5helper.cpp:28-35); values and
 // shapes are identical.
 #include "interpolating_vectors.h"
@@ -64,17 +65,28 @@ IVecs::IVecs(nlohmann::json& input, ContextHandler::BlacsHandler& BH, std::vecto
     out.resize((size_t)rows * cols);
     for (size_t i = 0; i < out.size(); i++) out[i] = aor[2 * i];
   };
-  bool unused = false;
-  read_orbitals("aoR", phi, ngrid, nbasis, !rotate, &complex_orbitals);
-  if (complex_orbitals)
+  read_orbitals("aoR", phi, ngrid, nbasis, true, &complex_orbitals);
+  if (complex_orbitals && !rotate)
     std::cout << " * aoR is complex: Z = |P|^2 from complex pseudo-densities." << std::endl;
   if (rotate) {
     long long rows = 0;
-    read_orbitals("aoR_half", phi_occ, rows, nocc, false, &unused);
+    bool occ_complex = false;
+    read_orbitals("aoR_half", phi_occ, rows, nocc, true, &occ_complex);
     if (rows != ngrid) {
       std::cerr << " * ERROR: aoR_half has " << rows << " grid points, aoR " << ngrid << std::endl;
       exit(1);
     }
+    if (complex_orbitals != occ_complex) {
+      // One of the two is real: widen it to (re, 0) pairs for the complex pass.
+      std::vector<double>& v = complex_orbitals ? phi_occ : phi;
+      std::vector<double> pairs(2 * v.size(), 0.0);
+      for (size_t i = 0; i < v.size(); i++) pairs[2 * i] = v[i];
+      v.swap(pairs);
+      complex_orbitals = true;
+    }
+    if (complex_orbitals)
+      std::cout << " * aoR / aoR_half are complex: Z = P_occ o conj(P) from complex "
+                   "pseudo-densities." << std::endl;
   }
   fft_grid = f.read_i32("fft_grid");
   interp = interp_indxs;
@@ -106,8 +118,8 @@ IVecs::IVecs(nlohmann::json& input, ContextHandler::BlacsHandler& BH, std::vecto
     w.write_i32("/Hamiltonian/THC/" + prfx + "InterpIndx", {(uint64_t)nmu}, interp.data());
   };
   if (rotate) {
-    write_mu(phi, nbasis, prefix + "Full", false);
-    write_mu(phi_occ, nocc, prefix + "Occ", false);
+    write_mu(phi, nbasis, prefix + "Full", complex_orbitals);
+    write_mu(phi_occ, nocc, prefix + "Occ", complex_orbitals);
   } else {
     write_mu(phi, nbasis, prefix, complex_orbitals);
   }
@@ -129,7 +141,11 @@ void IVecs::kernel(ContextHandler::BlacsHandler& BH)
   std::vector<double> L((size_t)nmu * nmu * 2);
   thc_isdf_stats st;
   int status;
-  if (half_rotate)
+  if (half_rotate && complex_orbitals)
+    status = thc_isdf_half_complex(thc_host::context(), phi.data(), ngrid, nbasis,
+                                   phi_occ.data(), nocc, interp.data(), nmu, fft_grid.data(),
+                                   coul.data(), nullptr, nullptr, L.data(), &st);
+  else if (half_rotate)
     status = thc_isdf_half(thc_host::context(), phi.data(), ngrid, nbasis, phi_occ.data(), nocc,
                            interp.data(), nmu, fft_grid.data(), coul.data(), -1.0, nullptr,
                            nullptr, L.data(), &st);
