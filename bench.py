@@ -212,6 +212,7 @@ def run_c4(args):
     t_seq = timed(run_seq)
     seq_launches = (ctx.kernel_launches - launches0) // (args.steps + args.warmup)
     t_bat = timed(run_bat)
+    tune = ctx.autotune_log()
     same_idx = all(torch.equal(a["out_idx"], b["out_idx"]) for a, b in zip(seq_arr, bat_arr))
     dm = max(float(torch.linalg.norm(a["out_M"] - b["out_M"]) / torch.linalg.norm(a["out_M"]))
              for a, b in zip(seq_arr, bat_arr))
@@ -233,6 +234,7 @@ def run_c4(args):
         "sequential_kmeans_ms_total": sum(t[0] for t in batch.run_sequential.times),
         "sequential_isdf_ms_total": sum(t[1] for t in batch.run_sequential.times),
         "sequential_largest_ms": max(t[0] + t[1] for t in batch.run_sequential.times),
+        "autotune": tune,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -531,6 +533,8 @@ def main():
                          "shift_used": isdf_st.shift_used, "refine_steps": refine,
                          "rank_deficient": int(isdf_st.rank_deficient)}
         line["device_memory_gb"] = round(mem_gb, 2)
+        # The sliced-GEMM autotuner's decisions (shape class -> k-step, tile order, split).
+        line["autotune"] = ctx.autotune_log()
         if qrcp:
             line["qrcp"] = qrcp
         if leg_errors:

@@ -103,7 +103,9 @@ int thc_ctx_set_stream(thc_ctx* ctx, void* cuda_stream);
  * default; 0 = warp-level mma.sync kernel); "km_prune" (1 = spatially pruned k-means
  * assignment, the default; 0 = exhaustive scan -- both exact); "graphs" (1 = replay the
  * k-means iteration block as a CUDA graph, the default); "tc_bk" (k-step per
- * pipeline stage of the tensor-core kernel: 32, the default, or 16); "fft64" (mixed path: 1 = zeta
+ * pipeline stage of the tensor-core kernel: 32, the default, or 16; setting it turns the
+ * autotuner off); "autotune" (1 = choose k-step, tile order and split of K per product shape
+ * by timing the candidates once per process, the default); "fft64" (mixed path: 1 = zeta
  * in FP64 through a D2Z FFT, 0 = FP32 and R2C, the default);
  * "profile" (1 = record a CUDA event pair around every launch of the named kernels,
  * 0 = stop and clear). */
@@ -112,6 +114,10 @@ int thc_ctx_set_option(thc_ctx* ctx, const char* key, double value);
  * named `kernel` since profiling was enabled; synchronises the context's stream. */
 int thc_ctx_kernel_time(thc_ctx* ctx, const char* kernel, double* ms, long long* launches);
 const char* thc_ctx_last_error(const thc_ctx* ctx);
+/* The decisions of the tensor-core GEMM's autotuner on the context's device, one line per
+ * shape class: k-step, tile order, split of K and the timed duration (context option
+ * "autotune", default 1; the text stays valid until the next call on the context). */
+const char* thc_ctx_autotune_log(thc_ctx* ctx);
 const char* thc_status_string(int status);
 /* Number of kernels this context has launched so far (its own kernels only). */
 long long thc_ctx_kernel_launches(const thc_ctx* ctx);

@@ -36,6 +36,7 @@ EXPORTS = [
     "thc_kmeans_history", "thc_factorize_batched", "thc_kmeans_noalloc",
     "thc_synth_gaussian_basis", "thc_isdf_half", "thc_qrcp", "thc_isdf_complex",
     "thc_qrcp_complex", "thc_isdf_interpolating_vectors", "thc_isdf_half_complex",
+    "thc_ctx_autotune_log",
 ]
 
 
@@ -103,6 +104,8 @@ def load(build_if_missing: bool = False):
     lib.thc_ctx_set_option.argtypes = [vp, ctypes.c_char_p, cd]
     lib.thc_ctx_last_error.argtypes = [vp]
     lib.thc_ctx_last_error.restype = ctypes.c_char_p
+    lib.thc_ctx_autotune_log.argtypes = [vp]
+    lib.thc_ctx_autotune_log.restype = ctypes.c_char_p
     lib.thc_status_string.argtypes = [ci]
     lib.thc_status_string.restype = ctypes.c_char_p
     lib.thc_ctx_kernel_launches.argtypes = [vp]
@@ -245,6 +248,11 @@ class Context:
         self._check(self.lib.thc_ctx_kernel_time(self.h, name.encode(), ctypes.byref(ms),
                                                  ctypes.byref(n)), "kernel_time")
         return ms.value, n.value
+
+    def autotune_log(self):
+        """The autotuner's decisions on this device, one string per shape class."""
+        txt = self.lib.thc_ctx_autotune_log(self.h).decode()
+        return [ln for ln in txt.splitlines() if ln]
 
     @property
     def kernel_launches(self) -> int:

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "ozgemm.cuh"
 #include "isdf.cuh"
 
 namespace thc {
@@ -285,6 +286,11 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
   if (!strcmp(key, "tc_bk")) {
     if (value != 16.0 && value != 32.0) return THC_ERR_ARG;
     h->c.tc_bk = (int)value;
+    h->c.autotune = 0;
+    return THC_OK;
+  }
+  if (!strcmp(key, "autotune")) {
+    h->c.autotune = value != 0.0;
     return THC_OK;
   }
   if (!strcmp(key, "qrcp_all_pairs")) {
@@ -315,6 +321,13 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
     return THC_OK;
   }
   return THC_ERR_ARG;
+}
+
+const char* thc_ctx_autotune_log(thc_ctx* h)
+{
+  if (!h) return "";
+  h->c.tune_log = thc::ozgemm_tune_log(h->c.device);
+  return h->c.tune_log.c_str();
 }
 
 const char* thc_ctx_last_error(const thc_ctx* h)

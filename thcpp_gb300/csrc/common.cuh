@@ -99,6 +99,11 @@ struct Ctx {
   // faster: 0.90 s against 1.00 s for the zeta product at N_g 1.26e6, N_mu 5184) or 16
   // (4 stages of half the size).
   int tc_bk = 32;
+  // Pick the tensor-core kernel's k-step, tile order and split of K per shape class by
+  // timing the candidates the first time a class is met (process-wide table; ozgemm_tc.cu).
+  // Setting "tc_bk" turns it off for the context.
+  int autotune = 1;
+  std::string tune_log;   // last thc_ctx_autotune_log text
   int tc_hi_stages = 8; // drain period of the level >= 3 accumulator, in 16-k MMA steps
   int fft64 = 0;        // mixed path: zeta in FP64 and a D2Z FFT (else FP32 and R2C)
   int qrcp_all_pairs = 0;  // half-rotated QRCP: every (occupied, orbital) pair as a row

@@ -99,5 +99,7 @@ int ozgemm(Ctx* c, const OzArgs& g);
 // tcgen05 / TMEM / TMA implementation; both operands K-contiguous.  err_flag (device int)
 // is set when a bounded wait inside the kernel gave up.
 int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag);
+// One line per shape class the tensor-core kernel's autotuner has decided on this device.
+std::string ozgemm_tune_log(int device);
 
 }  // namespace thc

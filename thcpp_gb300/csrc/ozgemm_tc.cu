@@ -25,6 +25,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
 
 #include "common.cuh"
 #include "ozgemm.cuh"
@@ -38,7 +42,6 @@ constexpr int kChunkK = 512;            // exact levels are drained every 512 k
 constexpr int kStageBudget = 200 * 1024;  // shared memory for the stage buffers
 constexpr int kSmemGuard = 16 * 1024;   // slack after the buffers (descriptor reads stay inside)
 constexpr int TEPI_WARPS = 8;
-constexpr int kGroupM = 8;    // m-tiles per group of the tile order
 constexpr int TTHREADS = 32 * (2 + TEPI_WARPS);
 constexpr long long kDrainLimit = 1LL << 22;   // teardown waits after an abort
 
@@ -229,6 +232,7 @@ struct TcArgs {
   int lower_only;
   int* error;                         // set to 1 when a bounded wait gave up
   long long spin_limit;               // polls before a wait gives up
+  int group_m;                        // m-tiles per group of the tile order
   int ksplit;
   double* part;
 };
@@ -259,15 +263,16 @@ __global__ void __launch_bounds__(TTHREADS, 1)
   using Cfg = TcCfg<LV, BK>;
   constexpr int A_BYTES = Cfg::A_BYTES, B_BYTES = Cfg::B_BYTES, STAGE_BYTES = Cfg::STAGE_BYTES;
   constexpr int NST = Cfg::STAGES;
-  // Grouped tile order: consecutive blocks sweep kGroupM m-tiles for each n-tile, so the
+  // Grouped tile order: consecutive blocks sweep g.group_m m-tiles for each n-tile, so the
   // CTAs resident at one time share a few A and B row blocks through L2.
   long long mt, nt;
   {
     const long long mtn = gridDim.x, ntn = gridDim.y;
     const long long b = (long long)blockIdx.y * mtn + blockIdx.x;
-    const long long per_group = (long long)kGroupM * ntn;
-    const long long grp = b / per_group, first_m = grp * kGroupM;
-    const long long gm = mtn - first_m < kGroupM ? mtn - first_m : kGroupM;
+    const long long grpm = g.group_m;
+    const long long per_group = grpm * ntn;
+    const long long grp = b / per_group, first_m = grp * grpm;
+    const long long gm = mtn - first_m < grpm ? mtn - first_m : grpm;
     const long long r = b - grp * per_group;
     mt = first_m + r % gm;
     nt = r / gm;
@@ -667,8 +672,16 @@ int make_map(Ctx* c, CUtensorMap* map, const void* base, long long width, long l
   return THC_OK;
 }
 
+// Launch choices of one product: k-step per stage, m-tiles per group of the tile order, and
+// the split of K (at most the caller's, whose partial buffer is sized for it).
+struct TcChoice {
+  int bk = 32;
+  int group_m = 8;
+  int ksplit = 1;
+};
+
 template <int LV, int BK>
-int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
+int launch_tc(Ctx* c, const OzArgs& g, int* err_flag, int group_m)
 {
   using Cfg = TcCfg<LV, BK>;
   CUtensorMap ta, tb;
@@ -694,6 +707,7 @@ int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
   t.ea = g.a.e; t.eb = g.b.e; t.C = g.C; t.ldc = g.ldc;
   t.epilogue = g.epilogue; t.lower_only = g.lower_only; t.error = err_flag;
   t.spin_limit = c->spin_limit;
+  t.group_m = group_m;
   t.ksplit = std::max(1, g.ksplit); t.part = g.part;
   const size_t smem = Cfg::SMEM;
   THC_CUDA(c, cudaFuncSetAttribute(ozgemm_tc_kernel<LV, BK>,
@@ -711,19 +725,67 @@ int launch_tc(Ctx* c, const OzArgs& g, int* err_flag)
 }
 
 template <int BK>
-int launch_bk(Ctx* c, const OzArgs& g, int* err_flag)
+int launch_bk(Ctx* c, const OzArgs& g, int* err_flag, int group_m)
 {
   switch (g.levels) {
-    case 2: return launch_tc<2, BK>(c, g, err_flag);
-    case 3: return launch_tc<3, BK>(c, g, err_flag);
-    case 4: return launch_tc<4, BK>(c, g, err_flag);
-    case 5: return launch_tc<5, BK>(c, g, err_flag);
-    case 6: return launch_tc<6, BK>(c, g, err_flag);
+    case 2: return launch_tc<2, BK>(c, g, err_flag, group_m);
+    case 3: return launch_tc<3, BK>(c, g, err_flag, group_m);
+    case 4: return launch_tc<4, BK>(c, g, err_flag, group_m);
+    case 5: return launch_tc<5, BK>(c, g, err_flag, group_m);
+    case 6: return launch_tc<6, BK>(c, g, err_flag, group_m);
     default: return set_error(c, THC_ERR_ARG, "ozgemm_tc: levels must be 2..6");
   }
 }
 
+int launch_choice(Ctx* c, const OzArgs& g_in, int* err_flag, const TcChoice& ch)
+{
+  OzArgs g = g_in;
+  g.ksplit = ch.ksplit;
+  if (g.ksplit <= 1) { g.ksplit = 1; g.part = nullptr; }
+  return ch.bk == 32 ? launch_bk<32>(c, g, err_flag, ch.group_m)
+                     : launch_bk<16>(c, g, err_flag, ch.group_m);
+}
+
+// The autotuner's decisions, one table per process and device, keyed by the shape class of a
+// product (log2 buckets of M, N and K, slice count, epilogue, lower-triangle flag, the
+// caller's split): every context uses the same decision for the same class, so two contexts
+// that factorise the same system produce the same bits.  A class is timed once, when first
+// met, on the stream of the context that meets it.
+struct TuneEntry {
+  TcChoice choice;
+  float us = 0.f;       // time of the chosen launch when it was tuned (0: model default)
+  int candidates = 0;
+};
+std::mutex g_tune_mu;
+std::map<std::vector<long long>, TuneEntry> g_tune;
+
+int ilog2c(long long x)
+{
+  int r = 0;
+  while ((1LL << r) < x) r++;
+  return r;
+}
+
 }  // namespace
+
+std::string ozgemm_tune_log(int device)
+{
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::string out;
+  char buf[256];
+  for (const auto& kv : g_tune) {
+    const auto& k = kv.first;
+    if (k[0] != device) continue;
+    const TuneEntry& e = kv.second;
+    snprintf(buf, sizeof(buf),
+             "M<=2^%lld N<=2^%lld K<=2^%lld slices=%lld epi=%lld lower=%lld split<=%lld: bk=%d "
+             "group_m=%d split=%d %.1fus (%d tried)\n",
+             k[1], k[2], k[3], k[4], k[5], k[6], k[7], e.choice.bk, e.choice.group_m,
+             e.choice.ksplit, e.us, e.candidates);
+    out += buf;
+  }
+  return out;
+}
 
 int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
 {
@@ -733,7 +795,62 @@ int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
   const long long br = g.b.kt_stride ? g.b.slice_stride / 32 : g.b.slice_stride / g.b.ld;
   if (g.a.ld % 32 || g.b.ld % 32 || ar % TBM || br % TBN)
     return set_error(c, THC_ERR_ARG, "ozgemm_tc: operand padding");
-  return c->tc_bk == 32 ? launch_bk<32>(c, g, err_flag) : launch_bk<16>(c, g, err_flag);
+  TcChoice dflt;
+  dflt.bk = c->tc_bk;
+  dflt.ksplit = g.ksplit;
+  if (!c->autotune) return launch_choice(c, g, err_flag, dflt);
+  const std::vector<long long> key = {c->device, ilog2c(g.M), ilog2c(g.N), ilog2c(g.K),
+                                      g.levels, g.epilogue, g.lower_only, g.ksplit};
+  std::lock_guard<std::mutex> lk(g_tune_mu);   // one tuning at a time; look-ups are brief
+  auto it = g_tune.find(key);
+  if (it != g_tune.end()) return launch_choice(c, g, err_flag, it->second.choice);
+  // Candidates: k-step 32 / 16, 8 / 16 m-tiles per group, the caller's split and half of
+  // it.  Products above ~10 ms of tensor work keep the default (their tiles fill the GPU
+  // many times over and a trial run would cost more than any choice gains).
+  const double work = (double)g.levels * (g.levels + 1) / 2 * 2.0 * g.M * g.N * g.K;
+  TuneEntry e;
+  e.choice = dflt;
+  if (work > 2e13) {
+    g_tune[key] = e;
+    return launch_choice(c, g, err_flag, dflt);
+  }
+  std::vector<TcChoice> cands;
+  for (int bk : {32, 16})
+    for (int gm : {8, 16})
+      for (int sp : {g.ksplit, std::max(1, g.ksplit / 2)}) {
+        TcChoice ch;
+        ch.bk = bk; ch.group_m = gm; ch.ksplit = sp;
+        bool dup = false;
+        for (const auto& x : cands) dup |= x.bk == bk && x.group_m == gm && x.ksplit == sp;
+        if (!dup) cands.push_back(ch);
+      }
+  cudaEvent_t ea = nullptr, eb = nullptr;
+  THC_CUDA(c, cudaEventCreate(&ea));
+  THC_CUDA(c, cudaEventCreate(&eb));
+  float best = 0.f;
+  int best_i = -1, last = -1;
+  int st = THC_OK;
+  for (size_t i = 0; i < cands.size() && st == THC_OK; i++) {
+    cudaEventRecord(ea, c->stream);
+    st = launch_choice(c, g, err_flag, cands[i]);
+    cudaEventRecord(eb, c->stream);
+    if (st) break;
+    if (cudaEventSynchronize(eb) != cudaSuccess) { st = THC_ERR_CUDA; break; }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ea, eb);
+    last = (int)i;
+    if (best_i < 0 || ms < best) { best = ms; best_i = (int)i; }
+  }
+  cudaEventDestroy(ea);
+  cudaEventDestroy(eb);
+  if (st) return st;
+  e.choice = cands[best_i];
+  e.us = 1e3f * best;
+  e.candidates = (int)cands.size();
+  g_tune[key] = e;
+  // The result in C must be the chosen launch's.
+  if (last != best_i) return launch_choice(c, g, err_flag, e.choice);
+  return THC_OK;
 }
 
 }  // namespace thc
