@@ -1,6 +1,6 @@
 """The sliced-GEMM autotuner: decisions are logged per shape class, shared by every context
 of the process (so two contexts produce the same bits), and any decision gives the same
-product to within the kernel's rounding."""
+result to within the mixed path's rounding."""
 import numpy as np
 import pytest
 
@@ -29,5 +29,8 @@ def test_autotune_shared_and_logged():
     with capi.Context(0, capi.THC_PREC_MIXED) as c:
         c.set_option("autotune", 0)
         rc = c.isdf(s.phi, idx, s.mesh, s.coulG)
+    # The choices change the summation order of the inexact level >= 3 accumulator and of the
+    # split-K partials, and zeta is rounded to FP32 after them: agreement at the path's own
+    # accuracy (~1e-7 against the FP64 oracle).
     Ma, Mc = _cplx(ra["M"]), _cplx(rc["M"])
-    assert np.linalg.norm(Ma - Mc) <= 1e-8 * np.linalg.norm(Mc)
+    assert np.linalg.norm(Ma - Mc) <= 1e-7 * np.linalg.norm(Mc)
