@@ -40,8 +40,10 @@ void* ws_get(Ctx* c, Slot s, size_t bytes)
       cudaGetLastError();
       // The pool keeps freed memory reserved (release threshold = max), possibly in pieces
       // too small for this request: return what no allocation uses and try once more.
+      // The whole device first: trimming may then release nothing that a kernel of another
+      // stream or context still uses.
       cudaMemPool_t pool;
-      if (cudaStreamSynchronize(c->stream) != cudaSuccess ||
+      if (cudaDeviceSynchronize() != cudaSuccess ||
           cudaDeviceGetDefaultMemPool(&pool, c->device) != cudaSuccess ||
           cudaMemPoolTrimTo(pool, 0) != cudaSuccess ||
           cudaMallocAsync(&p, bytes, c->stream) != cudaSuccess) {
@@ -512,6 +514,9 @@ int thc_factorize_batched(int device, int precision, thc_system* sys, int nsys, 
       thc_ctx* h = nullptr;
       int st = thc_ctx_create(device, precision, &h);
       if (st) return st;
+      // The systems already overlap across the workers' streams: each worker keeps its
+      // whole factorisation on its own stream.
+      h->c.overlap = 0;
       pool.push_back(h);
     }
     workers.assign(pool.begin(), pool.begin() + nstreams);

@@ -79,6 +79,7 @@ struct Ctx {
   // product), forked and joined with these events.
   cudaStream_t aux_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int overlap = 1;   // 0: keep that work on the main stream (the batch workers)
   void* ws[WS_NSLOTS] = {};
   size_t ws_bytes[WS_NSLOTS] = {};
   std::map<std::tuple<int, int, int, int, int>, cufftHandle> plans;  // (n0,n1,n2,batch,type)

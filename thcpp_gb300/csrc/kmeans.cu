@@ -1337,6 +1337,10 @@ __global__ void __launch_bounds__(kMapThreads) km_map_pruned(KmBufs b, const flo
           }
           if (d32 > thr32) continue;
           const int i = b.perm[q];
+          if ((unsigned)i >= (unsigned)b.ng) {   // a binning permutation entry out of range
+            atomicExch(&b.st->bad_label, 1);
+            continue;
+          }
           double d2 = d2_exact(b.gx[i], b.gy[i], b.gz[i], c3[0], c3[1], c3[2]);
           // Any order: a candidate can win on a smaller sqrt or on an equal sqrt and a
           // smaller index; equal sqrt values come from squared distances within a few ulps.

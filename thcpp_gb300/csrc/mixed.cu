@@ -347,17 +347,19 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   bool shifted = shift_rel > 0.0;
   bool cinv_tc = !shifted && nmu >= 512;
   CholStatus* hcs_p = (CholStatus*)c->pinned;      // pinned: the copy stays asynchronous
+  const cudaStream_t fs = c->overlap ? c->aux_stream : s;
   {
-    THC_CUDA(c, cudaEventRecord(c->ev_fork, s));
-    THC_CUDA(c, cudaStreamWaitEvent(c->aux_stream, c->ev_fork, 0));
-    StreamSwap on_aux(c, c->aux_stream);
+    if (fs != s) {
+      THC_CUDA(c, cudaEventRecord(c->ev_fork, s));
+      THC_CUDA(c, cudaStreamWaitEvent(fs, c->ev_fork, 0));
+    }
+    StreamSwap on_fs(c, fs);
     if ((st = factor(shifted ? shift_rel : 0.0))) return st;
     if ((st = chol_inverse(c, Lc, nmu, nmu, dinv, Xinv, Tinv, (shifted || cinv_tc) ? nullptr : Cinv,
                            cs)))
       return st;
-    THC_CUDA(c, cudaMemcpyAsync(hcs_p, cs, sizeof(CholStatus), cudaMemcpyDeviceToHost,
-                                c->aux_stream));
-    THC_CUDA(c, cudaEventRecord(c->ev_join, c->aux_stream));
+    THC_CUDA(c, cudaMemcpyAsync(hcs_p, cs, sizeof(CholStatus), cudaMemcpyDeviceToHost, fs));
+    if (fs != s) THC_CUDA(c, cudaEventRecord(c->ev_join, fs));
   }
   // Z = (Phi Phi_mu^T)^2 (N_g x N_mu) via the sliced GEMM: A = Phi sliced by grid point,
   // B = Phi_mu sliced by interpolating point; Z's rows are then K-contiguous for the solve.
@@ -380,8 +382,8 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   const SliceBuf zs = slices(sb, eb, ng_pad, mu_kpad, sz);
   if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs, keq))) return st;
   // Join C's factorisation.
-  THC_CUDA(c, cudaStreamSynchronize(c->aux_stream));
-  THC_CUDA(c, cudaStreamWaitEvent(s, c->ev_join, 0));
+  THC_CUDA(c, cudaStreamSynchronize(fs));
+  if (fs != s) THC_CUDA(c, cudaStreamWaitEvent(s, c->ev_join, 0));
   CholStatus hcs = *hcs_p;
   int chol_c_info = 0;
   if (hcs.flag) {
