@@ -299,6 +299,10 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
     h->c.qrcp_all_pairs = value != 0.0;
     return THC_OK;
   }
+  if (!strcmp(key, "overlap")) {
+    h->c.overlap = value != 0.0;
+    return THC_OK;
+  }
   if (!strcmp(key, "spin_limit")) {
     if (value < 0 || value > 1e12) return THC_ERR_ARG;
     h->c.spin_limit = (long long)value;
@@ -515,7 +519,7 @@ int thc_factorize_batched(int device, int precision, thc_system* sys, int nsys, 
       int st = thc_ctx_create(device, precision, &h);
       if (st) return st;
       // The systems already overlap across the workers' streams: each worker keeps its
-      // whole factorisation on its own stream.
+      // whole factorisation on its own stream (whatever the default of "overlap").
       h->c.overlap = 0;
       pool.push_back(h);
     }

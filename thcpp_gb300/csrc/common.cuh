@@ -75,11 +75,12 @@ struct Ctx {
   int precision = THC_PREC_FP64;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
-  // Second stream for work that overlaps the main one (C's factorisation beside the P
-  // product), forked and joined with these events.
+  // Second stream for work that may overlap the main one (C's factorisation beside the P
+  // product), forked and joined with these events.  Off by default ("overlap" option): the
+  // P product's CTAs fill every SM, so the overlap measured no gain at N_g 1.1e5.
   cudaStream_t aux_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  int overlap = 1;   // 0: keep that work on the main stream (the batch workers)
+  int overlap = 0;
   void* ws[WS_NSLOTS] = {};
   size_t ws_bytes[WS_NSLOTS] = {};
   std::map<std::tuple<int, int, int, int, int>, cufftHandle> plans;  // (n0,n1,n2,batch,type)

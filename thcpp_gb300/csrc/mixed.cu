@@ -339,9 +339,10 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     THC_LAUNCHED(c, "init_cs");
     return potrf_inv(c, Lc, nmu, nmu, thr, cs, dinv);
   };
-  // C's factorisation and inverse depend on Phi_mu only: they run on the context's second
-  // stream while the P product and Z's slicing run on the main one (the Cholesky's diagonal
-  // blocks occupy one SM at a time).  The expected case is taken ahead: the shift as given,
+  // C's factorisation and inverse depend on Phi_mu only: with the context option "overlap"
+  // they run on the context's second stream while the P product and Z's slicing run on the
+  // main one (the Cholesky's diagonal blocks occupy one SM at a time; by default they run in
+  // order on the main stream).  The expected case is taken ahead: the shift as given,
   // X = L^{-1}, and C^{-1} = X^T X in FP64 when N_mu < 512 without a shift; a breakdown of
   // the unshifted factorisation is retried on the main stream after the join.
   bool shifted = shift_rel > 0.0;
