@@ -108,7 +108,11 @@ int thc_ctx_set_stream(thc_ctx* ctx, void* cuda_stream);
  * by timing the candidates once per process, the default); "fft64" (mixed path: 1 = zeta
  * in FP64 through a D2Z FFT, 0 = FP32 and R2C, the default);
  * "profile" (1 = record a CUDA event pair around every launch of the named kernels,
- * 0 = stop and clear). */
+ * 0 = stop and clear); "refine" (steps of iterative refinement of zeta after a shifted
+ * solve of C, 0..8, default 0); "equilibrate" (mixed path: solve on C scaled to a unit-range
+ * diagonal by powers of two, default 1); "overlap" (mixed path: factor C on a second stream
+ * beside the P product, default 0); "spin_limit" (polls before a bounded device wait gives
+ * up with THC_ERR_TIMEOUT, default 2^24). */
 int thc_ctx_set_option(thc_ctx* ctx, const char* key, double value);
 /* Accumulated device time (ms, from the profile events) and launch count of the kernels
  * named `kernel` since profiling was enabled; synchronises the context's stream. */
