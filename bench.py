@@ -525,10 +525,20 @@ def main():
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "stage_ms_per_system": stage_ms,
         }
-        # Conditioning of C at the k-means points (side computation, after the timing).
-        pm = d_phi[d_idx.long()]
-        ev = torch.linalg.eigvalsh((pm @ pm.T) ** 2)
-        line["solve"] = {"cond_C": float(ev[-1] / ev[0]) if float(ev[0]) > 0 else None,
+        # Conditioning of C at the k-means points (side computation, after the timing; a
+        # failure here leaves it null).
+        cond = None
+        try:
+            pm = d_phi[d_idx.long()]
+            cmat = (pm @ pm.T) ** 2
+            try:
+                ev = torch.linalg.eigvalsh(cmat).cpu().numpy()
+            except RuntimeError:           # no GPU linear-algebra library in this process
+                ev = np.linalg.eigvalsh(cmat.cpu().numpy())
+            cond = float(ev[-1] / ev[0]) if float(ev[0]) > 0 else None
+        except Exception as e:
+            leg_errors["cond_C"] = f"{type(e).__name__}: {e}"
+        line["solve"] = {"cond_C": cond,
                          "shift_rel": shift_rel if shift_rel > 0 else None,
                          "shift_used": isdf_st.shift_used, "refine_steps": refine,
                          "rank_deficient": int(isdf_st.rank_deficient)}
