@@ -255,6 +255,24 @@ struct TcCfg {
   static_assert(STAGES >= 2, "stage buffers");
 };
 
+// Epilogue results whose power-of-two scale leaves the FP32 range (rare): formed in FP64.
+// mode: OZ_SQUARE_DW / OZ_STORE_DW give a double-word pair's bits, others the FP64 value.
+__device__ __noinline__ double wide_result(float h, float l, int ex, int mode)
+{
+  double val = ((double)h + (double)l) * pow2d(ex);
+  if (mode == OZ_SQUARE_F64 || mode == OZ_SQUARE_DW) val = val * val;
+  if (mode == OZ_SQUARE_DW || mode == OZ_STORE_DW) {
+    const float hi = (float)val, lo = (float)(val - (double)hi);
+    return __hiloint2double(__float_as_int(lo), __float_as_int(hi));
+  }
+  return val;
+}
+
+__device__ __noinline__ float wide_f32(float h, float l, int ex)
+{
+  return (float)(((double)h + (double)l) * pow2d(ex));
+}
+
 template <int LV, int BK>
 __global__ void __launch_bounds__(TTHREADS, 1)
     ozgemm_tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
@@ -544,43 +562,62 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       unsigned char* stg = smem + (size_t)ew * (32 * 64 * 8);
       float* stg32 = (float*)stg;
       double* stg64 = (double*)stg;
+      // One unrolled loop per epilogue, so that the instructions a CTA executes are one
+      // contiguous stretch (instruction fetch was the first stall of the short-K products);
+      // results whose scale leaves the FP32 range take a call.
+      const int mode = split ? -1 : g.epilogue;
+      if (mode == OZ_STORE_F32) {
 #pragma unroll
-      for (int q = 0; q < 64; q++) {
-        const int ex = ea + seb[q];
-        if (f32) {
-          float v;
-          if (ex > -126 && ex < 127) v = __fadd_rn(ah[q], al[q]) * pow2f(ex);
-          else v = (float)(((double)ah[q] + (double)al[q]) * pow2d(ex));
+        for (int q = 0; q < 64; q++) {
+          const int ex = ea + seb[q];
+          const float v = (ex > -126 && ex < 127) ? __fadd_rn(ah[q], al[q]) * pow2f(ex)
+                                                  : wide_f32(ah[q], al[q], ex);
           stg32[lane * 64 + (q ^ lane)] = v;
-          continue;
         }
-        double w;   // the 8-byte result: FP64 value, or a double-word pair's bits
-        if (!split && g.epilogue == OZ_STORE_DW && ex > -100 && ex < 100) {
-          float sc = pow2f(ex);
-          float zh, zl;
-          fast_two_sum(ah[q] * sc, al[q] * sc, zh, zl);
-          w = __hiloint2double(__float_as_int(zl), __float_as_int(zh));
-        } else if (!split && g.epilogue == OZ_SQUARE_DW && ex > -60 && ex < 60) {
-          // (h + l)^2 in double-word FP32: p + e = h^2 exactly (FMA), plus 2 h l.
-          float sc = pow2f(ex);
-          float h = ah[q] * sc, l = al[q] * sc;
-          float pp = __fmul_rn(h, h);
-          float e = __fmaf_rn(h, h, -pp);
-          e = __fmaf_rn(2.f * h, l, e);
-          float zh, zl;
-          fast_two_sum(pp, e, zh, zl);
-          w = __hiloint2double(__float_as_int(zl), __float_as_int(zh));
-        } else {
-          double val = ((double)ah[q] + (double)al[q]) * pow2d(ex);
-          if (!split && (g.epilogue == OZ_SQUARE_F64 || g.epilogue == OZ_SQUARE_DW)) val = val * val;
-          if (!split && (g.epilogue == OZ_SQUARE_DW || g.epilogue == OZ_STORE_DW)) {
-            float hi = (float)val, lo = (float)(val - (double)hi);
-            w = __hiloint2double(__float_as_int(lo), __float_as_int(hi));
+      } else if (mode == OZ_SQUARE_DW) {
+#pragma unroll
+        for (int q = 0; q < 64; q++) {
+          const int ex = ea + seb[q];
+          double w;
+          if (ex > -60 && ex < 60) {
+            // (h + l)^2 in double-word FP32: p + e = h^2 exactly (FMA), plus 2 h l.
+            const float sc = pow2f(ex);
+            const float h = ah[q] * sc, l = al[q] * sc;
+            const float pp = __fmul_rn(h, h);
+            float e = __fmaf_rn(h, h, -pp);
+            e = __fmaf_rn(2.f * h, l, e);
+            float zh, zl;
+            fast_two_sum(pp, e, zh, zl);
+            w = __hiloint2double(__float_as_int(zl), __float_as_int(zh));
           } else {
-            w = val;
+            w = wide_result(ah[q], al[q], ex, mode);
           }
+          stg64[lane * 64 + (q ^ (lane & 15))] = w;
         }
-        stg64[lane * 64 + (q ^ (lane & 15))] = w;
+      } else if (mode == OZ_STORE_DW) {
+#pragma unroll
+        for (int q = 0; q < 64; q++) {
+          const int ex = ea + seb[q];
+          double w;
+          if (ex > -100 && ex < 100) {
+            const float sc = pow2f(ex);
+            float zh, zl;
+            fast_two_sum(ah[q] * sc, al[q] * sc, zh, zl);
+            w = __hiloint2double(__float_as_int(zl), __float_as_int(zh));
+          } else {
+            w = wide_result(ah[q], al[q], ex, mode);
+          }
+          stg64[lane * 64 + (q ^ (lane & 15))] = w;
+        }
+      } else {
+        // FP64 results (stored, squared, or split-K partials).
+        const bool sq = mode == OZ_SQUARE_F64;
+#pragma unroll
+        for (int q = 0; q < 64; q++) {
+          double val = ((double)ah[q] + (double)al[q]) * pow2d(ea + seb[q]);
+          if (sq) val = val * val;
+          stg64[lane * 64 + (q ^ (lane & 15))] = val;
+        }
       }
       __syncwarp();
       // Row r of the staging: lane l writes columns 2l and 2l + 1.
