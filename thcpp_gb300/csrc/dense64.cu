@@ -119,7 +119,11 @@ __global__ void dgemm_reduce(GemmArgs g)
 
 // ---- Cholesky (lower, in place, row-major) --------------------------------------
 
-constexpr int NB = 64;
+// Diagonal block edge of the blocked Cholesky: 32 up to n = 1024, else 64.  The serial
+// part (the diagonal blocks, one SM each) costs n NB^2 / 3 FMAs on a latency chain of NB
+// dependent steps per block; the trailing updates are rank-NB FP64 GEMMs that lose
+// efficiency at NB = 32, which only matters for the large n.
+inline int chol_nb(int n) { return n <= 1024 ? 32 : 64; }
 
 // 1/sqrt(d) for a positive normal d: an FP32 seed y0 (relative error e0 < 2^-22), then one
 // third-order step of the binomial series for (1 - e)^(-1/2), e = 1 - d y0^2:
@@ -146,6 +150,7 @@ __device__ __forceinline__ double rsqrt_fast(double d)
 // block's ~nb^3/3 FMAs, so phase (2) runs as one flat list of work items with every lane
 // busy (a triangle ordered by decreasing column makes the items of step j a prefix).  The
 // thread that updates the next pivot a_{j+1,j+1} forms its reciprocal root at once.
+template <int NB>
 __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, int n, int k0,
                                                       const double* thr_p, CholStatus* cs,
                                                       double* dinv)
@@ -385,12 +390,18 @@ int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholSta
 {
   ProfScope prof(c, "potrf_inv");
   cudaStream_t s = c->stream;
+  const int NB = chol_nb(n);
   for (int k0 = 0; k0 < n; k0 += NB) {
     int nb = std::min(NB, n - k0);
     double* di = dinv + (long long)(k0 / NB) * NB * NB;
     const int smem = 2 * NB * (NB + 1) * (int)sizeof(double);
-    THC_CUDA(c, cudaFuncSetAttribute(potrf_diag_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    potrf_diag_inv<<<1, 256, smem, s>>>(A, ld, n, k0, thr, cs, di);
+    if (NB == 32) {
+      THC_CUDA(c, cudaFuncSetAttribute(potrf_diag_inv<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      potrf_diag_inv<32><<<1, 256, smem, s>>>(A, ld, n, k0, thr, cs, di);
+    } else {
+      THC_CUDA(c, cudaFuncSetAttribute(potrf_diag_inv<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      potrf_diag_inv<64><<<1, 256, smem, s>>>(A, ld, n, k0, thr, cs, di);
+    }
     THC_LAUNCHED(c, "potrf_diag_inv");
     int rest = n - k0 - nb;
     if (rest <= 0) break;
@@ -420,14 +431,15 @@ int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholSta
 }
 
 // X = L^{-1} (lower, n x n, ld) from the factor L and its inverted diagonal blocks, block row
-// by block row: X_ii = dinv_i, X[i, 0:i] = -dinv_i (L[i, 0:i] X[0:i, 0:i]).  T is an
-// NB x n scratch.  Then Cinv = X^T X.
+// by block row: X_ii = dinv_i, X[i, 0:i] = -dinv_i (L[i, 0:i] X[0:i, 0:i]), with the block
+// edge NB = chol_nb(n) that potrf_inv used.  T is an NB x n scratch.  Then Cinv = X^T X.
 int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* dinv, double* X,
                  double* T, double* Cinv, const CholStatus* cs)
 {
   ProfScope prof(c, "chol_inverse");
   cudaStream_t s = c->stream;
   THC_CUDA(c, cudaMemsetAsync(X, 0, sizeof(double) * (size_t)n * ld, s));
+  const int NB = chol_nb(n);
   int nblk = (n + NB - 1) / NB;
   for (int bi = 0; bi < nblk; bi++) {
     int i0 = bi * NB, nb = std::min(NB, n - i0);
