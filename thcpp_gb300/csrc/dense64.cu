@@ -119,11 +119,12 @@ __global__ void dgemm_reduce(GemmArgs g)
 
 // ---- Cholesky (lower, in place, row-major) --------------------------------------
 
-// Diagonal block edge of the blocked Cholesky: 32 up to n = 1024, else 64.  The serial
-// part (the diagonal blocks, one SM each) costs n NB^2 / 3 FMAs on a latency chain of NB
-// dependent steps per block; the trailing updates are rank-NB FP64 GEMMs that lose
-// efficiency at NB = 32, which only matters for the large n.
-inline int chol_nb(int n) { return n <= 1024 ? 32 : 64; }
+// Diagonal block edge of the blocked Cholesky.  The serial part (the diagonal blocks, one
+// SM each) is a latency chain of NB dependent steps per block; 32 x 32 blocks (a quarter of
+// the FP64 work per block) measured no faster at n = 256 (the factorisations of C and M:
+// 0.95 ms against 0.99 ms, and the triangular inverse 0.26 ms against 0.16 ms with twice the
+// block rows), so both edges stay available and 64 is used.
+inline int chol_nb(int) { return 64; }
 
 // 1/sqrt(d) for a positive normal d: an FP32 seed y0 (relative error e0 < 2^-22), then one
 // third-order step of the binomial series for (1 - e)^(-1/2), e = 1 - d y0^2:

@@ -43,7 +43,7 @@ struct CholStatus {
 // over many SMs); split partials are summed in split order (deterministic).
 int dgemm(Ctx* c, const GemmArgs& g);
 // Cholesky with GEMM panels; dinv receives the inverted NB x NB diagonal blocks
-// (NB = 32 for n <= 1024, else 64; at most ceil(n/64) x 64 x 64 doubles).
+// (NB = 64: ceil(n/64) x 64 x 64 doubles).
 int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholStatus* cs,
               double* dinv);
 // Cinv = (L L^T)^{-1} via X = L^{-1}; X (n x ld) and T (64 x n) are scratch.
