@@ -217,47 +217,23 @@ __global__ void __launch_bounds__(256) potrf_diag_inv(double* A, long long ld, i
     const int pe = ntri - (nb - 1 - j);                  // item (j+1, j+1): the next pivot
     const int w = j + 1;                                 // rectangle row length
     const float rw = 1.0f / (float)w;
-    // Four items per thread at a time, all operands loaded before any result is stored:
-    // the items of one step are independent (they write a[i][c], c > j, or v[i][c], i > j,
-    // and read column j of a and row j of v, which this step does not write), so their
-    // shared-memory loads and FP64 FMAs overlap instead of forming one latency chain.
-    const int total = ntri + nrect;
-    for (int e0 = threadIdx.x; e0 < total; e0 += 4 * blockDim.x) {
-      double x[4], y[4], z[4];
-      double* dst[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int e = e0 + u * (int)blockDim.x;
-        dst[u] = nullptr;
-        if (e >= total) continue;
-        if (e < ntri) {
-          const unsigned code = tri[e];
-          const int i = code >> 8, c = code & 255;
-          x[u] = a[i][j];
-          y[u] = a[c][j];
-          z[u] = a[i][c];
-          dst[u] = &a[i][c];
-        } else {
-          // q = r w + c without an integer division: the FP32 quotient of q < 2^12 is off
-          // by at most one, which the two corrections fix.
-          const int q = e - ntri;
-          int r = (int)((float)q * rw);
-          int c = q - r * w;
-          if (c < 0) { r--; c += w; }
-          if (c >= w) { r++; c -= w; }
-          const int i = j + 1 + r;
-          x[u] = a[i][j];
-          y[u] = v[j][c];
-          z[u] = v[i][c];
-          dst[u] = &v[i][c];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        if (!dst[u]) continue;
-        const double nv = __fma_rn(-x[u], y[u], z[u]);
-        *dst[u] = nv;
-        if (e0 + u * (int)blockDim.x == pe) pivot(j + 1, nv);
+    for (int e = threadIdx.x; e < ntri + nrect; e += blockDim.x) {
+      if (e < ntri) {
+        const unsigned code = tri[e];
+        const int i = code >> 8, c = code & 255;
+        const double nv = __fma_rn(-a[i][j], a[c][j], a[i][c]);
+        a[i][c] = nv;
+        if (e == pe) pivot(j + 1, nv);
+      } else {
+        // q = r w + c without an integer division: the FP32 quotient of q < 2^12 is off by
+        // at most one, which the two corrections fix.
+        const int q = e - ntri;
+        int r = (int)((float)q * rw);
+        int c = q - r * w;
+        if (c < 0) { r--; c += w; }
+        if (c >= w) { r++; c -= w; }
+        const int i = j + 1 + r;
+        v[i][c] = __fma_rn(-a[i][j], v[j][c], v[i][c]);
       }
     }
     __syncthreads();
