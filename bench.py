@@ -485,10 +485,17 @@ def main():
         pairs = lambda L: L * (L + 1) // 2
         n0, n1, n2 = s.mesh
         nc2 = 2 * n0 * n1 * (n2 // 2 + 1)
-        # P, zeta and M, plus C^{-1} = X^T X from N_mu = 512 on (the library's threshold).
+        # P, zeta and M; without a shift also C^{-1} = X^T X from N_mu = 512 on (the
+        # library's threshold); with a shift the solve is two products (Y^T = Z (P X)^T, then
+        # zeta^T = X^T Y) and refinement adds G = X X^T and one N_mu^3 product per step.
+        shifted = bool(isdf_st.rank_deficient)
         flops = (pairs(sp) * 2 * nmu * ng * no + pairs(sz) * 2 * nmu * ng * nmu
-                 + pairs(sm) * 2 * nmu * nmu * nc2 / 2
-                 + (pairs(sz) * 2 * nmu ** 3 if nmu >= 512 else 0))
+                 + pairs(sm) * 2 * nmu * nmu * nc2 / 2)
+        if shifted:
+            flops += pairs(sz) * 2 * nmu * ng * nmu + (
+                pairs(sz) * 2 * nmu ** 3 * (1 + refine) if refine > 0 else 0)
+        elif nmu >= 512:
+            flops += pairs(sz) * 2 * nmu ** 3
         # Aggregate over the timed launches: all their flops over all their time.
         achieved = flops * args.steps / (oz_ms * 1e-3) / 1e12 if oz_n else None
         roof = {"kernel": "ozgemm (sliced-BF16 tensor GEMMs of a factorisation, aggregate)",
