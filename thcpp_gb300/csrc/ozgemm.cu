@@ -250,15 +250,93 @@ __global__ void oz_reduce_kernel(OzArgs g)
   store_epilogue(g, m, n, v);
 }
 
-// One warp per row: exponent from the row maximum, then the slices of an FP64 input in
-// integer arithmetic.  With e the row exponent (|x| < 2^e), X = round(x 2^{7 ns - e}) is an
-// integer below 2^{7 ns} built from the IEEE bits (round half to even at the cut), and the
-// slices are its signed base-128 digits S_i = round(R_i / 2^{7(ns-1-i)}), R_{i+1} = R_i -
-// S_i 2^{7(ns-1-i)}, so |S_0| <= 128 and |S_i| <= 64.  Rows scaled by `scale` (optional,
-// indexed c >> shift) are multiplied in FP64 first.
+// Slicing.  A row's entries are cut relative to the row exponent e (|x| < 2^e for every
+// entry, from the row maximum) into ns signed base-128 digits,
+//     x = 2^{e-7} sum_{i<ns} S_i 2^{-7i},
+// computed in 32-bit arithmetic: with nh = min(ns, 3) and nl = ns - nh, the scaled value
+// a = x 2^{7 nh - e} (|a| < 2^{7 nh}) gives A = rint(a) and, from the exact remainder
+// a - A (plus the low word of a double-word input), B = rint((a - A + a_lo) 2^{7 nl}); A
+// and B are integers below 2^21 held exactly in FP32 and are split into nh and nl
+// balanced digits by exact power-of-two divisions and rint.  |S_0| <= 128, |S_1|, |S_2| <=
+// 64, |S_3| <= 72, |S_4|, |S_5| <= 64, all exact in BF16, and the expansion is within
+// 0.57 units of the last digit of x.  Each lane cuts eight consecutive columns, so every
+// slice is written as one 16-byte store per lane (the eight columns lie in one 32-wide k
+// tile of the tiled layout).
+
+// Slices are stored pre-scaled: digit S_s as S_s 2^{-7s} (exact in BF16), so that a product
+// of slices i and j carries its level's weight 2^{-7(i+j)} and the GEMM kernels need no
+// per-level scaling.
+__device__ __forceinline__ float slice_scale(int s) { return __int_as_float((127 - 7 * s) << 23); }
+
+// 2^e as an FP32 value, for -126 <= e <= 127.
+__device__ __forceinline__ float pow2_f32(int e) { return __int_as_float((e + 127) << 23); }
+
+// x * 2^e, exact whenever the result is a normal number (one multiply in range, else ldexpf).
+__device__ __forceinline__ float scale2(float x, int e)
+{
+  return (e >= -126 && e <= 127) ? __fmul_rn(x, pow2_f32(e)) : ldexpf(x, e);
+}
+
+// N balanced base-128 digits of an integer |x| <= 2^{7N} + 2^{7N-4} held in FP32.
+template <int N>
+__device__ __forceinline__ void int_digits(float x, float* d)
+{
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    const int sh = 7 * (N - 1 - i);
+    if (sh) {
+      const float q = rintf(__fmul_rn(x, pow2_f32(-sh)));
+      x = __fmaf_rn(-q, pow2_f32(sh), x);   // exact: an integer below 2^24
+      d[i] = q;
+    } else {
+      d[i] = x;
+    }
+  }
+}
+
+// The NS digits of a (scaled by 2^{7 nh - e}) with low word al.
+template <int NS>
+__device__ __forceinline__ void value_digits(float a, float al, float* d)
+{
+  constexpr int NH = NS < 3 ? NS : 3, NL = NS - NH;
+  const float A = rintf(a);
+  int_digits<NH>(A, d);
+  if (NL) {
+    const float B = rintf(__fmul_rn(__fadd_rn(__fsub_rn(a, A), al), pow2_f32(7 * NL)));
+    int_digits<NL>(B, d + NH);
+  }
+}
+
+// Offset of element (slice s2, row r, column cc) in a plain (kts == 0) or tiled slice
+// buffer (OzOperand).
+__device__ __forceinline__ long long slice_at(int s2, long long r, long long cc, long long ldo,
+                                              long long sstride, long long kts)
+{
+  return kts ? (cc >> 5) * kts + s2 * sstride + r * 32 + (cc & 31)
+             : s2 * sstride + r * ldo + cc;
+}
+
+// Columns c..c+7 (c a multiple of 8) of row r, every slice: one 16-byte store per slice.
+template <int NS>
+__device__ __forceinline__ void store_digits8(__nv_bfloat16* out, long long r, long long c,
+                                              long long ldo, long long sstride, long long kts,
+                                              const float (&d)[8][NS])
+{
+#pragma unroll
+  for (int s2 = 0; s2 < NS; s2++) {
+    const float sc = slice_scale(s2);
+    __nv_bfloat162 p[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      p[q] = __floats2bfloat162_rn(__fmul_rn(d[2 * q][s2], sc), __fmul_rn(d[2 * q + 1][s2], sc));
+    *(uint4*)(out + slice_at(s2, r, c, ldo, sstride, kts)) = *(const uint4*)p;
+  }
+}
+
+// round(|x| * 2^shift_total) of an FP64 value with the sign of x, from the IEEE bits (round
+// half to even); |x| * 2^shift_total < 2^62 assumed.
 __device__ __forceinline__ long long fixed_point(double x, int shift_total)
 {
-  // round(|x| * 2^shift_total) with the sign of x; |x| * 2^shift_total < 2^62 assumed.
   unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   int E = (int)((bits >> 52) & 0x7ff);
   if (E == 0) return 0;                              // zero or subnormal: below every slice
@@ -280,28 +358,33 @@ __device__ __forceinline__ long long fixed_point(double x, int shift_total)
   return (bits >> 63) ? -(long long)X : (long long)X;
 }
 
-// Slices are stored pre-scaled: digit S_s as S_s 2^{-7s} (exact in BF16), so that a product
-// of slices i and j carries its level's weight 2^{-7(i+j)} and the GEMM kernels need no
-// per-level scaling.
-__device__ __forceinline__ float slice_scale(int s) { return __int_as_float((127 - 7 * s) << 23); }
-
-// Offset of element (slice s2, row r, column cc) in a plain (kts == 0) or tiled slice
-// buffer (OzOperand).
-__device__ __forceinline__ long long slice_at(int s2, long long r, long long cc, long long ldo,
-                                              long long sstride, long long kts)
+// Lanes per row of the row-per-warp slicers: a power of two with 8 columns per lane, so
+// that short rows (N_o = 32 orbitals: four lanes) share a warp with other rows.
+inline int slice_lanes_per_row(long long ldo)
 {
-  return kts ? (cc >> 5) * kts + s2 * sstride + r * 32 + (cc & 31)
-             : s2 * sstride + r * ldo + cc;
+  int l = 32;
+  while (l > 4 && 8LL * l > ldo) l >>= 1;
+  return l;
 }
 
-__global__ void slice_rows_kernel(const double* __restrict__ X, long long rows, long long cols,
-                                  long long ldx, long long sc, const double* __restrict__ scale,
-                                  int shift, int ns, __nv_bfloat16* out, long long ldo,
-                                  long long sstride, long long kts, int* exps, long long rows_pad)
+// FP64 input, LPR lanes per row (32 / LPR rows per warp).  The FP64 value is taken to the
+// fixed-point integer R = round(x 2^{7 ns - e}) (|R| <= 2^{7 ns}) in integer arithmetic on
+// its bits (no FP64 arithmetic on this part's slow FP64 pipe), then R = A 2^{7 nl} + B with
+// FP32-exact A, B and the same digit split as above.  Rows scaled by `scale` (optional,
+// indexed c >> shift) are multiplied in FP64 first.  Element (r, c) is X[r * ldx + c * sc].
+template <int NS>
+__global__ void __launch_bounds__(256) slice_rows_kernel(
+    const double* __restrict__ X, long long rows, long long cols, long long ldx, long long sc,
+    const double* __restrict__ scale, int shift, __nv_bfloat16* out, long long ldo,
+    long long sstride, long long kts, int* exps, long long rows_pad, int lpr)
 {
-  long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (r >= rows_pad) return;
+  constexpr int NH = NS < 3 ? NS : 3, NL = NS - NH;
+  const int lane = threadIdx.x & 31, sub = lane & (lpr - 1);
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long r0 = warp * (32 / lpr);
+  if (r0 >= rows_pad) return;                        // whole warp
+  const long long r = r0 + lane / lpr;
+  const bool live_row = r < rows;
   auto val = [&](long long cidx) -> double {
     double v = X[r * ldx + cidx * sc];
     if (scale) v *= scale[cidx >> shift];
@@ -309,146 +392,184 @@ __global__ void slice_rows_kernel(const double* __restrict__ X, long long rows, 
   };
   // Row maximum of |x| through the bit patterns (monotone for non-negative doubles).
   unsigned long long mx = 0;
-  if (r < rows)
-    for (long long cc = lane; cc < cols; cc += 32) {
+  if (live_row)
+    for (long long cc = sub; cc < cols; cc += lpr) {
       unsigned long long a = (unsigned long long)__double_as_longlong(val(cc)) & 0x7fffffffffffffffULL;
       mx = a > mx ? a : mx;
     }
-  for (int off = 16; off; off >>= 1) {
+  for (int off = lpr >> 1; off; off >>= 1) {
     unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
     mx = o > mx ? o : mx;
   }
+  if (r >= rows_pad) return;                         // after the warp's shuffles
   // frexp exponent of the maximum: |x| < 2^e for every entry of the row.
   int e = 0;
-  int Em = (int)(mx >> 52);
+  const int Em = (int)(mx >> 52);
   if (Em > 0) e = Em - 1022;
-  if (lane == 0) exps[r] = e;
-  const int total = 7 * ns - e;
-  for (long long cc = lane; cc < ldo; cc += 32) {
-    long long R = (r < rows && cc < cols && Em > 0) ? fixed_point(val(cc), total) : 0;
-    for (int s2 = 0; s2 < ns; s2++) {
-      int sh = 7 * (ns - 1 - s2);
-      long long S = sh ? ((R + (1LL << (sh - 1))) >> sh) : R;
-      R -= S << sh;
-      // |S| <= 128: convert through int32 (a 64-bit integer conversion runs on the slow
-      // FP64-class path on this part).
-      out[slice_at(s2, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn((float)(int)S * slice_scale(s2));
+  if (sub == 0) exps[r] = e;
+  const int total = 7 * NS - e;
+  for (long long c0 = 8 * sub; c0 < ldo; c0 += 8 * lpr) {
+    float d[8][NS];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const long long cc = c0 + j;
+      const long long R = (live_row && cc < cols && Em > 0) ? fixed_point(val(cc), total) : 0;
+      // A = round(R / 2^{7 nl}), B = R - A 2^{7 nl}: |A| <= 2^{7 nh}, |B| <= 2^{7 nl - 1}.
+      const long long A = NL ? (R + (1LL << (7 * NL - 1))) >> (7 * NL) : R;
+      int_digits<NH>((float)(int)A, d[j]);
+      if (NL) int_digits<NL>((float)(int)(R - (A << (7 * NL))), d[j] + NH);
     }
+    store_digits8<NS>(out, r, c0, ldo, sstride, kts, d);
   }
 }
 
-// round(|x| 2^shift_total) of an FP32 value as a signed 64-bit integer (round half even).
-__device__ __forceinline__ long long fixed_point_f32(float x, int shift_total)
+// Eight consecutive double-word entries (columns c..c+7) of a row; entries at or past
+// `cols` read as zero.  vec: the row is 16-byte aligned and c + 8 <= cols.
+__device__ __forceinline__ void load_dw8(const float2* __restrict__ row, long long c,
+                                         long long cols, bool vec, float2 (&v)[8])
 {
-  unsigned bits = __float_as_uint(x);
-  int E = (int)((bits >> 23) & 0xff);
-  if (E == 0) return 0;
-  unsigned long long m = (bits & 0x7fffffu) | 0x800000u;
-  int s = E - 150 + shift_total;
-  unsigned long long X;
-  if (s >= 0) {
-    X = s < 40 ? m << s : 0;   // beyond 2^63: cannot occur for |x| < 2^e rows
-  } else if (s <= -32) {
-    X = 0;
+  if (vec && c + 8 <= cols) {
+    const float4* p = (const float4*)(row + c);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const float4 t = __ldg(p + q);
+      v[2 * q] = make_float2(t.x, t.y);
+      v[2 * q + 1] = make_float2(t.z, t.w);
+    }
   } else {
-    int r = -s;
-    unsigned long long q = m >> r;
-    unsigned long long rem = m & ((1ULL << r) - 1);
-    unsigned long long half = 1ULL << (r - 1);
-    if (rem > half || (rem == half && (q & 1))) q++;
-    X = q;
+#pragma unroll
+    for (int j = 0; j < 8; j++) v[j] = c + j < cols ? __ldg(row + c + j) : make_float2(0.f, 0.f);
   }
-  return (bits >> 31) ? -(long long)X : (long long)X;
 }
 
-// Slices of a double-word (hi, lo) matrix, one warp per row, as slice_rows_kernel: the row
-// exponent comes from max |hi| (|hi + lo| < 2^e whenever |hi| < 2^e), and the fixed-point
-// integer is the sum of the two parts' roundings (within one unit of the exact value).
-// With kexp, column k is scaled by 2^{-kexp[k]}: a shift of the fixed-point cut, exact.
-__global__ void slice_rows_dw_kernel(const float2* __restrict__ X, long long rows, long long cols,
-                                     long long ldx, int ns, __nv_bfloat16* out, long long ldo,
-                                     long long sstride, long long kts, int* exps,
-                                     long long rows_pad, const int* __restrict__ kexp)
+// Slices of a double-word (hi, lo) matrix, LPR lanes per row: the row exponent comes from
+// max |hi| (|hi + lo| < 2^e whenever |hi| < 2^e), and a = hi 2^{7 nh - e}, a_lo = lo
+// 2^{7 nh - e} feed the digit split above.  With kexp, column k is scaled by 2^{-kexp[k]}
+// (an exact shift of the cut).  Rows of at most 8 LPR entries are read once and kept in
+// registers between the two passes.
+template <int NS>
+__global__ void __launch_bounds__(256, 3) slice_rows_dw_kernel(
+    const float2* __restrict__ X, long long rows, long long cols, long long ldx,
+    __nv_bfloat16* out, long long ldo, long long sstride, long long kts, int* exps,
+    long long rows_pad, const int* __restrict__ kexp, bool vec, int lpr)
 {
-  long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (r >= rows_pad) return;
+  constexpr int NH = NS < 3 ? NS : 3;
+  const int lane = threadIdx.x & 31, sub = lane & (lpr - 1);
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long r0 = warp * (32 / lpr);
+  if (r0 >= rows_pad) return;                        // whole warp
+  const long long r = r0 + lane / lpr;
+  const float2* row = X + (r < rows ? r : 0) * ldx;
+  const long long ncols = r < rows ? cols : 0;
+  const bool one = ldo <= 8 * lpr;   // a single chunk of eight columns per lane
+  float2 keep[8];
   unsigned mx = 0;
-  if (r < rows)
-    for (long long cc = lane; cc < cols; cc += 32) {
-      float h = X[r * ldx + cc].x;
-      if (kexp) h = ldexpf(h, -kexp[cc]);
-      unsigned a = __float_as_uint(h) & 0x7fffffffu;
-      mx = a > mx ? a : mx;
+  for (long long c0 = 8 * sub; c0 < ncols; c0 += 8 * lpr) {
+    float2 v[8];
+    load_dw8(row, c0, ncols, vec, v);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      float h = v[j].x;
+      if (kexp && c0 + j < ncols) h = scale2(h, -__ldg(kexp + c0 + j));
+      mx = max(mx, __float_as_uint(h) & 0x7fffffffu);
+      if (one) keep[j] = v[j];
     }
-  for (int off = 16; off; off >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  }
+  for (int off = lpr >> 1; off; off >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if (r >= rows_pad) return;                         // after the warp's shuffles
   int e = 0;
-  int Em = (int)(mx >> 23);
+  const int Em = (int)(mx >> 23);
   if (Em > 0) e = Em - 126;
-  if (lane == 0) exps[r] = e;
-  const int total = 7 * ns - e;
-  for (long long cc = lane; cc < ldo; cc += 32) {
-    long long R = 0;
-    if (r < rows && cc < cols && Em > 0) {
-      float2 v = X[r * ldx + cc];
-      const int t = kexp ? total - kexp[cc] : total;
-      R = fixed_point_f32(v.x, t) + fixed_point_f32(v.y, t);
+  if (sub == 0) exps[r] = e;
+  const int sh0 = 7 * NH - e;
+  for (long long c0 = 8 * sub; c0 < ldo; c0 += 8 * lpr) {
+    float2 v[8];
+    if (one && c0 < ncols) {
+#pragma unroll
+      for (int j = 0; j < 8; j++) v[j] = keep[j];
+    } else {
+      load_dw8(row, c0, ncols, vec, v);
     }
-    for (int s2 = 0; s2 < ns; s2++) {
-      int sh = 7 * (ns - 1 - s2);
-      long long S = sh ? ((R + (1LL << (sh - 1))) >> sh) : R;
-      R -= S << sh;
-      out[slice_at(s2, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn((float)(int)S * slice_scale(s2));
+    float d[8][NS];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const bool live = Em > 0 && c0 + j < ncols;
+      const int sh = kexp && live ? sh0 - __ldg(kexp + c0 + j) : sh0;
+      const float a = live ? scale2(v[j].x, sh) : 0.f;
+      const float al = live ? scale2(v[j].y, sh) : 0.f;
+      value_digits<NS>(a, al, d[j]);
     }
+    store_digits8<NS>(out, r, c0, ldo, sstride, kts, d);
+  }
+}
+
+// Eight consecutive FP32 entries (columns c..c+7) of a row times their scales; entries at
+// or past `cols` read as zero.  vec: 16-byte aligned row and ldx a multiple of 4.
+__device__ __forceinline__ void load_f32x8(const float* __restrict__ row, long long c,
+                                           long long cols, bool vec,
+                                           const float* __restrict__ scale, int shift,
+                                           float (&v)[8])
+{
+  if (vec && c + 8 <= cols) {
+    const float4 t0 = __ldg((const float4*)(row + c)), t1 = __ldg((const float4*)(row + c) + 1);
+    v[0] = t0.x; v[1] = t0.y; v[2] = t0.z; v[3] = t0.w;
+    v[4] = t1.x; v[5] = t1.y; v[6] = t1.z; v[7] = t1.w;
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; j++) v[j] = c + j < cols ? __ldg(row + c + j) : 0.f;
+  }
+  if (scale) {
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (c + j < cols) v[j] = __fmul_rn(v[j], __ldg(scale + ((c + j) >> shift)));
   }
 }
 
 // FP32 input scaled by an FP32 copy of `scale` (rounded once to FP32, then sliced exactly
 // in FP32 arithmetic).  Two passes so that long rows use the whole GPU: per-row maxima by
-// column chunks (atomicMax on the bit pattern, valid for non-negative floats), then the
-// slices with one thread per element.
-__global__ void rowmax_f32_kernel(const float* __restrict__ X, long long rows, long long cols,
-                                  long long ldx, const float* __restrict__ scale, int shift,
-                                  unsigned* rowmax)
+// column chunks of 4096 (atomicMax on the bit pattern, valid for non-negative floats), then
+// the slices, eight columns per thread.
+__global__ void __launch_bounds__(256) rowmax_f32_kernel(
+    const float* __restrict__ X, long long rows, long long cols, long long ldx,
+    const float* __restrict__ scale, int shift, unsigned* rowmax, bool vec)
 {
-  long long r = blockIdx.y;
-  long long c0 = (long long)blockIdx.x * 4096;
+  const long long r = blockIdx.y;
+  if (r >= rows) return;
+  const float* row = X + r * ldx;
   float mx = 0.f;
-  if (r < rows)
-    for (long long cc = c0 + threadIdx.x; cc < cols && cc < c0 + 4096; cc += blockDim.x) {
-      float v = X[r * ldx + cc];
-      if (scale) v *= scale[cc >> shift];
-      mx = fmaxf(mx, fabsf(v));
-    }
+  const long long c1 = min(cols, (long long)(blockIdx.x + 1) * 4096);
+  for (long long c = (long long)blockIdx.x * 4096 + 8 * threadIdx.x; c < c1; c += 2048) {
+    float v[8];
+    load_f32x8(row, c, c1, vec, scale, shift, v);
+#pragma unroll
+    for (int j = 0; j < 8; j++) mx = fmaxf(mx, fabsf(v[j]));
+  }
   for (int off = 16; off; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
   if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(&rowmax[r], __float_as_uint(mx));
 }
 
-__global__ void slice_rows_f32_kernel(const float* __restrict__ X, long long rows,
-                                      long long cols, long long ldx,
-                                      const float* __restrict__ scale, int shift, int ns,
-                                      __nv_bfloat16* out, long long ldo, long long sstride,
-                                      long long kts, const unsigned* __restrict__ rowmax,
-                                      int* exps)
+template <int NS>
+__global__ void __launch_bounds__(256) slice_rows_f32_kernel(
+    const float* __restrict__ X, long long rows, long long cols, long long ldx,
+    const float* __restrict__ scale, int shift, __nv_bfloat16* out, long long ldo,
+    long long sstride, long long kts, const unsigned* __restrict__ rowmax, int* exps, bool vec)
 {
-  long long r = blockIdx.y;
-  long long cc = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  float mx = __uint_as_float(rowmax[r]);
+  constexpr int NH = NS < 3 ? NS : 3;
+  const long long r = blockIdx.y;
+  const long long c0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 8;
+  const float mx = __uint_as_float(rowmax[r]);
   int e = 0;
   if (mx > 0.f) frexpf(mx, &e);
-  if (cc == 0) exps[r] = e;
-  if (cc >= ldo) return;
-  float x = 0.f;
-  if (r < rows && cc < cols) {
-    float v = X[r * ldx + cc];
-    if (scale) v *= scale[cc >> shift];
-    x = ldexpf(v, 7 - e);
-  }
-  for (int s = 0; s < ns; s++) {
-    float q = rintf(x);
-    out[slice_at(s, r, cc, ldo, sstride, kts)] = __float2bfloat16_rn(q * slice_scale(s));
-    x = (x - q) * 128.f;
-  }
+  if (c0 == 0) exps[r] = e;
+  if (c0 >= ldo) return;
+  const long long ncols = r < rows ? cols : 0;
+  float v[8];
+  load_f32x8(X + (r < rows ? r : 0) * ldx, c0, ncols, vec, scale, shift, v);
+  const int sh = 7 * NH - e;
+  float d[8][NS];
+#pragma unroll
+  for (int j = 0; j < 8; j++) value_digits<NS>(mx > 0.f ? scale2(v[j], sh) : 0.f, 0.f, d[j]);
+  store_digits8<NS>(out, r, c0, ldo, sstride, kts, d);
 }
 
 }  // namespace
@@ -482,14 +603,28 @@ int oz_split_reduce(Ctx* c, const OzArgs& g)
   return THC_OK;
 }
 
+// Dispatch of a slicing kernel on the slice count (2..6); ARGS is the parenthesised
+// argument list.
+#define OZ_SLICE_DISPATCH(ns, KERNEL, GRID, ARGS)                                    \
+  switch (ns) {                                                                     \
+    case 2: KERNEL<2><<<GRID, 256, 0, c->stream>>> ARGS; break;                     \
+    case 3: KERNEL<3><<<GRID, 256, 0, c->stream>>> ARGS; break;                     \
+    case 4: KERNEL<4><<<GRID, 256, 0, c->stream>>> ARGS; break;                     \
+    case 5: KERNEL<5><<<GRID, 256, 0, c->stream>>> ARGS; break;                     \
+    case 6: KERNEL<6><<<GRID, 256, 0, c->stream>>> ARGS; break;                     \
+    default: return set_error(c, THC_ERR_ARG, "slicing: slice count must be 2..6");  \
+  }
+
 int oz_slice_rows_f64(Ctx* c, const double* X, long long rows, long long cols, long long ldx,
                       long long sc, const double* scale, int scale_shift, const SliceBuf& out)
 {
   ProfScope prof(c, "slice");
-  long long threads = out.rows_pad * 32;
-  slice_rows_kernel<<<(unsigned)cdiv(threads, 256), 256, 0, c->stream>>>(
-      X, rows, cols, ldx, sc, scale, scale_shift, out.ns, out.s, out.kpad, out.slice_stride(),
-      out.kt_stride(), out.e, out.rows_pad);
+  if (out.kpad % 32) return set_error(c, THC_ERR_ARG, "slicing: padded K must be a multiple of 32");
+  const int lpr = slice_lanes_per_row(out.kpad);
+  const unsigned blocks = (unsigned)cdiv(cdiv(out.rows_pad, 32 / lpr) * 32, 256);
+  OZ_SLICE_DISPATCH(out.ns, slice_rows_kernel, blocks,
+                    (X, rows, cols, ldx, sc, scale, scale_shift, out.s, out.kpad,
+                     out.slice_stride(), out.kt_stride(), out.e, out.rows_pad, lpr))
   THC_LAUNCHED(c, "slice_rows_f64");
   return THC_OK;
 }
@@ -498,10 +633,13 @@ int oz_slice_rows_dw(Ctx* c, const float2* X, long long rows, long long cols, lo
                      const SliceBuf& out, const int* kexp)
 {
   ProfScope prof(c, "slice");
-  long long threads = out.rows_pad * 32;
-  slice_rows_dw_kernel<<<(unsigned)cdiv(threads, 256), 256, 0, c->stream>>>(
-      X, rows, cols, ldx, out.ns, out.s, out.kpad, out.slice_stride(), out.kt_stride(), out.e,
-      out.rows_pad, kexp);
+  if (out.kpad % 32) return set_error(c, THC_ERR_ARG, "slicing: padded K must be a multiple of 32");
+  const int lpr = slice_lanes_per_row(out.kpad);
+  const unsigned blocks = (unsigned)cdiv(cdiv(out.rows_pad, 32 / lpr) * 32, 256);
+  const bool vec = (ldx % 2 == 0) && ((uintptr_t)X % 16 == 0);
+  OZ_SLICE_DISPATCH(out.ns, slice_rows_dw_kernel, blocks,
+                    (X, rows, cols, ldx, out.s, out.kpad, out.slice_stride(), out.kt_stride(),
+                     out.e, out.rows_pad, kexp, vec, lpr))
   THC_LAUNCHED(c, "slice_rows_dw");
   return THC_OK;
 }
@@ -510,18 +648,20 @@ int oz_slice_rows_f32(Ctx* c, const float* X, long long rows, long long cols, lo
                       const float* scale, int scale_shift, const SliceBuf& out)
 {
   ProfScope prof(c, "slice");
+  if (out.kpad % 32) return set_error(c, THC_ERR_ARG, "slicing: padded K must be a multiple of 32");
   const long long rows_pad = out.rows_pad;
   unsigned* rowmax = (unsigned*)ws_get(c, WS_ROWMAX, sizeof(unsigned) * rows_pad);
   if (!rowmax) return set_error(c, THC_ERR_NOMEM, "slice_rows_f32: row maxima");
   THC_CUDA(c, cudaMemsetAsync(rowmax, 0, sizeof(unsigned) * rows_pad, c->stream));
   if (rows_pad > 65535) return set_error(c, THC_ERR_SHAPE, "slice_rows_f32: too many rows");
+  const bool vec = (ldx % 4 == 0) && ((uintptr_t)X % 16 == 0);
   dim3 g1((unsigned)cdiv(cols, 4096), (unsigned)rows_pad);
-  rowmax_f32_kernel<<<g1, 256, 0, c->stream>>>(X, rows, cols, ldx, scale, scale_shift, rowmax);
+  rowmax_f32_kernel<<<g1, 256, 0, c->stream>>>(X, rows, cols, ldx, scale, scale_shift, rowmax, vec);
   THC_LAUNCHED(c, "rowmax_f32");
-  dim3 g2((unsigned)cdiv(out.kpad, 256), (unsigned)rows_pad);
-  slice_rows_f32_kernel<<<g2, 256, 0, c->stream>>>(X, rows, cols, ldx, scale, scale_shift,
-                                                   out.ns, out.s, out.kpad, out.slice_stride(),
-                                                   out.kt_stride(), rowmax, out.e);
+  dim3 g2((unsigned)cdiv(out.kpad, 8 * 256), (unsigned)rows_pad);
+  OZ_SLICE_DISPATCH(out.ns, slice_rows_f32_kernel, g2,
+                    (X, rows, cols, ldx, scale, scale_shift, out.s, out.kpad, out.slice_stride(),
+                     out.kt_stride(), rowmax, out.e, vec))
   THC_LAUNCHED(c, "slice_rows_f32");
   return THC_OK;
 }

@@ -4,18 +4,22 @@
 // of S_i T_j (slices stored pre-scaled by 2^{-7i}), with exact FP32 chunk sums folded into a
 // double-word FP32 total.
 //
-// CTA tile 128 x 128, k-step BK (16 or 32) per pipeline stage, all LV slices of A and B per
-// stage, as many stages as fit in ~200 KB of shared memory.
+// CTA tile 128 x BN (BN = 128, or 64 for two CTAs per SM), k-step BK (16 or 32) per
+// pipeline stage, all LV slices of A and B per stage, as many stages as fit in ~200 KB of
+// shared memory (BN = 128) or ~80 KB (BN = 64).
 // Warp roles (320 threads):
 //   warp 0      TMA producer: 2*LV tiled loads per stage (K-major, 32- or 64-byte swizzle)
 //   warp 1      TMEM allocator + single-thread MMA issuer
 //   warps 2-9   epilogue: two warps per TMEM lane quadrant, 64 columns each
-// TMEM (512 columns) holds four 128 x 128 FP32 accumulators: one each for the pair levels
+// TMEM (4 BN columns) holds four 128 x BN FP32 accumulators: one each for the pair levels
 // 0, 1 and 2, which carry the bulk of the value and are drained every 512 k while each of
 // their sums is still exact (an integer multiple of 2^{-7l} below 2^{24-7l}), and one for
 // all levels >= 3 together, which weigh <= 2^-21 of the total and are inexact FP32 sums
 // (drained every 128 k, so that no running sum grows over the whole K).  Around a drain the
 // MMA thread issues the pairs of the other accumulators first, which covers it.
+// BN = 64 halves the epilogue of a tile and its TMEM (256 columns) and shared memory, so two
+// CTAs share an SM and one's epilogue overlaps the other's loads and MMAs: the short-K
+// products (K = N_o) are epilogue-bound with one CTA per SM.
 // Every mbarrier wait is bounded; on timeout the kernel records an error, stops issuing,
 // and every role falls through to the teardown, which frees TMEM.
 #include <cuda.h>
@@ -37,9 +41,10 @@ namespace thc {
 
 namespace {
 
-constexpr int TBM = 128, TBN = 128;
+constexpr int TBM = 128;
 constexpr int kChunkK = 512;            // exact levels are drained every 512 k
-constexpr int kStageBudget = 200 * 1024;  // shared memory for the stage buffers
+constexpr int kStageBudget = 200 * 1024;  // shared memory for the stage buffers (BN = 128)
+constexpr int kStageBudget64 = 80 * 1024;  // the same for BN = 64 (two CTAs per SM)
 constexpr int kSmemGuard = 16 * 1024;   // slack after the buffers (descriptor reads stay inside)
 constexpr int TEPI_WARPS = 8;
 constexpr int TTHREADS = 32 * (2 + TEPI_WARPS);
@@ -123,16 +128,21 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
   return d;
 }
 
-// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TBN >> 3) << 17) |
-                            ((uint32_t)(TBM >> 4) << 24);
+// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = BN.
+template <int BN>
+__host__ __device__ constexpr uint32_t idesc()
+{
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+         ((uint32_t)(TBM >> 4) << 24);
+}
 
+template <int BN>
 __device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc)
 {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
+      "l"(a), "l"(b), "r"(idesc<BN>()), "r"(acc));
 }
 
 __device__ __forceinline__ void umma_commit(uint64_t* bar)
@@ -237,22 +247,27 @@ struct TcArgs {
   double* part;
 };
 
-// Stage geometry of one (LV, BK) instantiation.
-template <int LV, int BK>
+// Stage geometry of one (LV, BK, BN) instantiation.
+template <int LV, int BK, int BN>
 struct TcCfg {
   static constexpr int A_BYTES = TBM * BK * 2;            // one slice tile of A
-  static constexpr int B_BYTES = TBN * BK * 2;            // one slice tile of B
+  static constexpr int B_BYTES = BN * BK * 2;             // one slice tile of B
   static constexpr int STAGE_BYTES = LV * (A_BYTES + B_BYTES);
-  static constexpr int STAGES = kStageBudget / STAGE_BYTES < 4 ? kStageBudget / STAGE_BYTES : 4;
+  static constexpr int BUDGET = BN == 128 ? kStageBudget : kStageBudget64;
+  static constexpr int STAGES = BUDGET / STAGE_BYTES < 4 ? BUDGET / STAGE_BYTES : 4;
   static constexpr int CHUNK_STAGES = kChunkK / BK;
   static constexpr int NEXACT = LV < 3 ? LV : 3;          // exact level accumulators
-  // The stage buffers, reused after the main loop to stage the epilogue's 8 warps x 32 x 64
-  // 8-byte results; the barriers follow.
-  static constexpr int EPI_BYTES = TEPI_WARPS * 32 * 64 * 8;
+  static constexpr int ECOLS = BN / 2;                    // columns per epilogue warp
+  static constexpr int TMEM_COLS = 4 * BN;                // four accumulators
+  static constexpr int MIN_CTAS = BN == 128 ? 1 : 2;      // CTAs per SM
+  // The stage buffers, reused after the main loop to stage the epilogue's 8 warps x 32 x
+  // ECOLS 8-byte results; the barriers follow.
+  static constexpr int EPI_BYTES = TEPI_WARPS * 32 * ECOLS * 8;
   static constexpr int BUF_BYTES = STAGES * STAGE_BYTES > EPI_BYTES ? STAGES * STAGE_BYTES : EPI_BYTES;
   // + barriers (256 B) + the tile's 128 column exponents (512 B) + guard.
   static constexpr size_t SMEM = (size_t)BUF_BYTES + 1024 + 256 + 512 + kSmemGuard;
   static_assert(STAGES >= 2, "stage buffers");
+  static_assert(BN == 128 || BN == 64, "tile width");
 };
 
 // Epilogue results whose power-of-two scale leaves the FP32 range (rare): formed in FP64.
@@ -273,12 +288,13 @@ __device__ __noinline__ float wide_f32(float h, float l, int ex)
   return (float)(((double)h + (double)l) * pow2d(ex));
 }
 
-template <int LV, int BK>
-__global__ void __launch_bounds__(TTHREADS, 1)
+template <int LV, int BK, int BN>
+__global__ void __launch_bounds__(TTHREADS, (BN == 128 ? 1 : 2))
     ozgemm_tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
                      TcArgs g)
 {
-  using Cfg = TcCfg<LV, BK>;
+  using Cfg = TcCfg<LV, BK, BN>;
+  constexpr int EC = Cfg::ECOLS;
   constexpr int A_BYTES = Cfg::A_BYTES, B_BYTES = Cfg::B_BYTES, STAGE_BYTES = Cfg::STAGE_BYTES;
   constexpr int NST = Cfg::STAGES;
   // Grouped tile order: consecutive blocks sweep g.group_m m-tiles for each n-tile, so the
@@ -296,7 +312,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     nt = r / gm;
   }
   const long long m0 = mt * TBM;
-  const long long n0 = nt * TBN;
+  const long long n0 = nt * BN;
   if (g.lower_only && n0 > m0 + TBM - 1) return;
 
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -344,8 +360,8 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
-                     su32(tmem_slot)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     su32(tmem_slot)), "n"(Cfg::TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n");
@@ -411,7 +427,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
               for (int kk = 0; kk < BK / 16; kk++) {
                 uint64_t ad = sdesc<BK>(a0 + i * A_BYTES + kk * 32);
                 uint64_t bd = sdesc<BK>(b0 + j * B_BYTES + kk * 32);
-                umma(tmem + 3 * TBN, ad, bd, first ? 0u : 1u);
+                umma<BN>(tmem + 3 * BN, ad, bd, first ? 0u : 1u);
                 first = false;
               }
             }
@@ -429,7 +445,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
               for (int kk = 0; kk < BK / 16; kk++) {
                 uint64_t ad = sdesc<BK>(a0 + i * A_BYTES + kk * 32);
                 uint64_t bd = sdesc<BK>(b0 + j * B_BYTES + kk * 32);
-                umma(tmem + l * TBN, ad, bd, first ? 0u : 1u);
+                umma<BN>(tmem + l * BN, ad, bd, first ? 0u : 1u);
                 first = false;
               }
             }
@@ -468,24 +484,24 @@ __global__ void __launch_bounds__(TTHREADS, 1)
     // ------------------------------------------------------------------ epilogue
     const int ew = warp - 2;                 // 0..7
     const int quad = warp & 3;               // TMEM lane quadrant this warp may access
-    const int half = ew >> 2;                // which 64-column half of the tile
+    const int half = ew >> 2;                // which EC-column half of the tile
     const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
-    const int col0 = half * 64;
-    // Exponents of this row and of the half's 64 columns, loaded while the MMAs run (both
+    const int col0 = half * EC;
+    // Exponents of this row and of the half's EC columns, loaded while the MMAs run (both
     // warps of a half store the same values).
     int* seb = (int*)((unsigned char*)full + 256) + col0;
-    {
-      const long long na = n0 + col0 + lane, nb = na + 32;
-      seb[lane] = na < g.N ? g.eb[na] : 0;
-      seb[lane + 32] = nb < g.N ? g.eb[nb] : 0;
+#pragma unroll
+    for (int q = lane; q < EC; q += 32) {
+      const long long na = n0 + col0 + q;
+      seb[q] = na < g.N ? g.eb[na] : 0;
     }
     const long long m = m0 + quad * 32 + lane;
     const int ea = (m < g.M ? g.ea[m] : 0) - 14;
     __syncwarp();
-    // Double-word FP32 totals of this thread's row, 64 columns.
-    float ah[64], al[64];
+    // Double-word FP32 totals of this thread's row, EC columns.
+    float ah[EC], al[EC];
 #pragma unroll
-    for (int q = 0; q < 64; q++) { ah[q] = 0.f; al[q] = 0.f; }
+    for (int q = 0; q < EC; q++) { ah[q] = 0.f; al[q] = 0.f; }
     bool ok = true;
     const int nhp = nstages > 0 ? (nstages - 1 + HOFF) / HS + 1 : 0;
     int hpd = 0;                                     // level >= 3 periods drained
@@ -496,9 +512,9 @@ __global__ void __launch_bounds__(TTHREADS, 1)
         if (!mbar_wait(acc_full_hi, (uint32_t)(hpd & 1), abort, g.spin_limit)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
-        for (int b = 0; b < 8; b++) {
+        for (int b = 0; b < EC / 8; b++) {
           float v[8];
-          tmem_ld8(tmem + lane_base + 3 * TBN + (uint32_t)(col0 + 8 * b), v);
+          tmem_ld8(tmem + lane_base + 3 * BN + (uint32_t)(col0 + 8 * b), v);
           // |v| <= 2^-21 |ah|: the low word takes it with an FP32 rounding of ~2^-45 |ah|.
 #pragma unroll
           for (int q = 0; q < 8; q++) al[8 * b + q] = __fadd_rn(al[8 * b + q], v[q]);
@@ -511,12 +527,12 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       if (!mbar_wait(acc_full, (uint32_t)(ch & 1), abort, g.spin_limit)) { ok = false; break; }
       asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
-      for (int b = 0; b < 8; b++) {   // 8 columns at a time (register pressure)
+      for (int b = 0; b < EC / 8; b++) {   // 8 columns at a time (register pressure)
         float l0[8], l1[8], l2[8];
         const uint32_t cb = (uint32_t)(col0 + 8 * b);
-        tmem_ld8(tmem + lane_base + 0 * TBN + cb, l0);
-        if (LV > 1) tmem_ld8(tmem + lane_base + 1 * TBN + cb, l1);
-        if (LV > 2) tmem_ld8(tmem + lane_base + 2 * TBN + cb, l2);
+        tmem_ld8(tmem + lane_base + 0 * BN + cb, l0);
+        if (LV > 1) tmem_ld8(tmem + lane_base + 1 * BN + cb, l1);
+        if (LV > 2) tmem_ld8(tmem + lane_base + 2 * BN + cb, l2);
         // l0, l1, l2 are exact (multiples of 1, 2^-7, 2^-14 below 2^24, 2^17, 2^10); their
         // sum needs <= 38 bits and is carried exactly in (s, e).
 #pragma unroll
@@ -542,9 +558,9 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       if (!mbar_wait(acc_full_hi, (uint32_t)(hpd & 1), abort, g.spin_limit)) { ok = false; break; }
       asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
-      for (int b = 0; b < 8; b++) {
+      for (int b = 0; b < EC / 8; b++) {
         float v[8];
-        tmem_ld8(tmem + lane_base + 3 * TBN + (uint32_t)(col0 + 8 * b), v);
+        tmem_ld8(tmem + lane_base + 3 * BN + (uint32_t)(col0 + 8 * b), v);
 #pragma unroll
         for (int q = 0; q < 8; q++) al[8 * b + q] = __fadd_rn(al[8 * b + q], v[q]);
       }
@@ -559,7 +575,7 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       // instead of 32 rows kilobytes apart.
       const bool split = g.ksplit > 1;
       const bool f32 = !split && g.epilogue == OZ_STORE_F32;
-      unsigned char* stg = smem + (size_t)ew * (32 * 64 * 8);
+      unsigned char* stg = smem + (size_t)ew * (32 * EC * 8);
       float* stg32 = (float*)stg;
       double* stg64 = (double*)stg;
       // One unrolled loop per epilogue, so that the instructions a CTA executes are one
@@ -568,15 +584,15 @@ __global__ void __launch_bounds__(TTHREADS, 1)
       const int mode = split ? -1 : g.epilogue;
       if (mode == OZ_STORE_F32) {
 #pragma unroll
-        for (int q = 0; q < 64; q++) {
+        for (int q = 0; q < EC; q++) {
           const int ex = ea + seb[q];
           const float v = (ex > -126 && ex < 127) ? __fadd_rn(ah[q], al[q]) * pow2f(ex)
                                                   : wide_f32(ah[q], al[q], ex);
-          stg32[lane * 64 + (q ^ lane)] = v;
+          stg32[lane * EC + (q ^ lane)] = v;
         }
       } else if (mode == OZ_SQUARE_DW) {
 #pragma unroll
-        for (int q = 0; q < 64; q++) {
+        for (int q = 0; q < EC; q++) {
           const int ex = ea + seb[q];
           double w;
           if (ex > -60 && ex < 60) {
@@ -592,11 +608,11 @@ __global__ void __launch_bounds__(TTHREADS, 1)
           } else {
             w = wide_result(ah[q], al[q], ex, mode);
           }
-          stg64[lane * 64 + (q ^ (lane & 15))] = w;
+          stg64[lane * EC + (q ^ (lane & 15))] = w;
         }
       } else if (mode == OZ_STORE_DW) {
 #pragma unroll
-        for (int q = 0; q < 64; q++) {
+        for (int q = 0; q < EC; q++) {
           const int ex = ea + seb[q];
           double w;
           if (ex > -100 && ex < 100) {
@@ -607,31 +623,34 @@ __global__ void __launch_bounds__(TTHREADS, 1)
           } else {
             w = wide_result(ah[q], al[q], ex, mode);
           }
-          stg64[lane * 64 + (q ^ (lane & 15))] = w;
+          stg64[lane * EC + (q ^ (lane & 15))] = w;
         }
       } else {
         // FP64 results (stored, squared, or split-K partials).
         const bool sq = mode == OZ_SQUARE_F64;
 #pragma unroll
-        for (int q = 0; q < 64; q++) {
+        for (int q = 0; q < EC; q++) {
           double val = ((double)ah[q] + (double)al[q]) * pow2d(ea + seb[q]);
           if (sq) val = val * val;
-          stg64[lane * 64 + (q ^ (lane & 15))] = val;
+          stg64[lane * EC + (q ^ (lane & 15))] = val;
         }
       }
       __syncwarp();
-      // Row r of the staging: lane l writes columns 2l and 2l + 1.
+      // Row r of the staging: EC / 2 lanes per row, each writing two adjacent columns (one
+      // row per pass for EC = 64, two for EC = 32).
       const long long ld = split ? g.N : g.ldc;
-      const int c0 = 2 * lane;
+      constexpr int LPR = EC / 2, RPP = 32 / LPR;
+      const int c0 = 2 * (lane % LPR);
       const long long n = n0 + col0 + c0;
-      for (int r = 0; r < 32; r++) {
+      for (int r0 = 0; r0 < 32; r0 += RPP) {
+        const int r = r0 + lane / LPR;
         const long long mr = m0 + quad * 32 + r;
         if (mr >= g.M) break;
         const bool v0 = n < g.N && !(g.lower_only && n > mr);
         const bool v1 = n + 1 < g.N && !(g.lower_only && n + 1 > mr);
         const long long off = mr * ld + n;
         if (f32) {
-          const float a = stg32[r * 64 + (c0 ^ r)], bb = stg32[r * 64 + ((c0 + 1) ^ r)];
+          const float a = stg32[r * EC + (c0 ^ r)], bb = stg32[r * EC + ((c0 + 1) ^ r)];
           float* dst = (float*)g.C + off;
           if (v0 && v1 && !((uintptr_t)dst & 7)) *(float2*)dst = make_float2(a, bb);
           else {
@@ -639,8 +658,8 @@ __global__ void __launch_bounds__(TTHREADS, 1)
             if (v1) dst[1] = bb;
           }
         } else {
-          const double a = stg64[r * 64 + (c0 ^ (r & 15))];
-          const double bb = stg64[r * 64 + ((c0 + 1) ^ (r & 15))];
+          const double a = stg64[r * EC + (c0 ^ (r & 15))];
+          const double bb = stg64[r * EC + ((c0 + 1) ^ (r & 15))];
           double* dst = split ? g.part + (long long)blockIdx.z * g.M * g.N + off
                               : (double*)g.C + off;
           // Paired stores only at 16-byte aligned addresses (the partials of split z start at
@@ -671,7 +690,8 @@ __global__ void __launch_bounds__(TTHREADS, 1)
   __syncthreads();
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;\n");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                 "n"(Cfg::TMEM_COLS));
   }
 }
 
@@ -715,12 +735,13 @@ struct TcChoice {
   int bk = 32;
   int group_m = 8;
   int ksplit = 1;
+  int bn = 128;          // tile width: 128, or 64 (with bk = 16) for two CTAs per SM
 };
 
-template <int LV, int BK>
+template <int LV, int BK, int BN>
 int launch_tc(Ctx* c, const OzArgs& g, int* err_flag, int group_m)
 {
-  using Cfg = TcCfg<LV, BK>;
+  using Cfg = TcCfg<LV, BK, BN>;
   CUtensorMap ta, tb;
   const bool at = g.a.kt_stride > 0, bt = g.b.kt_stride > 0;
   long long a_rows = at ? g.a.slice_stride / 32 : g.a.slice_stride / g.a.ld;
@@ -732,8 +753,8 @@ int launch_tc(Ctx* c, const OzArgs& g, int* err_flag, int group_m)
   int st = at ? make_map(c, &ta, g.a.s, 32, (g.a.ld / 32) * (g.a.kt_stride / 32), TBM, BK)
               : make_map(c, &ta, g.a.s, g.a.ld, a_rows * LV, TBM, BK);
   if (st) return st;
-  st = bt ? make_map(c, &tb, g.b.s, 32, (g.b.ld / 32) * (g.b.kt_stride / 32), TBN, BK)
-          : make_map(c, &tb, g.b.s, g.b.ld, b_rows * LV, TBN, BK);
+  st = bt ? make_map(c, &tb, g.b.s, 32, (g.b.ld / 32) * (g.b.kt_stride / 32), BN, BK)
+          : make_map(c, &tb, g.b.s, g.b.ld, b_rows * LV, BN, BK);
   if (st) return st;
   TcArgs t;
   t.M = g.M; t.N = g.N; t.K = g.K;
@@ -747,29 +768,29 @@ int launch_tc(Ctx* c, const OzArgs& g, int* err_flag, int group_m)
   t.group_m = group_m;
   t.ksplit = std::max(1, g.ksplit); t.part = g.part;
   const size_t smem = Cfg::SMEM;
-  THC_CUDA(c, cudaFuncSetAttribute(ozgemm_tc_kernel<LV, BK>,
+  THC_CUDA(c, cudaFuncSetAttribute(ozgemm_tc_kernel<LV, BK, BN>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((unsigned)cdiv(g.M, TBM), (unsigned)cdiv(g.N, TBN), (unsigned)t.ksplit);
+  dim3 grid((unsigned)cdiv(g.M, TBM), (unsigned)cdiv(g.N, BN), (unsigned)t.ksplit);
   if (grid.y > 65535) return set_error(c, THC_ERR_SHAPE, "ozgemm_tc: N too large");
   {
     ProfScope prof(c, "ozgemm");
     ProfScope prof_tag(g.tag ? c : nullptr, g.tag ? g.tag : "");
-    ozgemm_tc_kernel<LV, BK><<<grid, TTHREADS, smem, c->stream>>>(ta, tb, t);
+    ozgemm_tc_kernel<LV, BK, BN><<<grid, TTHREADS, smem, c->stream>>>(ta, tb, t);
     THC_LAUNCHED(c, "ozgemm_tc");
   }
   if (t.ksplit > 1) return oz_split_reduce(c, g);
   return THC_OK;
 }
 
-template <int BK>
+template <int BK, int BN>
 int launch_bk(Ctx* c, const OzArgs& g, int* err_flag, int group_m)
 {
   switch (g.levels) {
-    case 2: return launch_tc<2, BK>(c, g, err_flag, group_m);
-    case 3: return launch_tc<3, BK>(c, g, err_flag, group_m);
-    case 4: return launch_tc<4, BK>(c, g, err_flag, group_m);
-    case 5: return launch_tc<5, BK>(c, g, err_flag, group_m);
-    case 6: return launch_tc<6, BK>(c, g, err_flag, group_m);
+    case 2: return launch_tc<2, BK, BN>(c, g, err_flag, group_m);
+    case 3: return launch_tc<3, BK, BN>(c, g, err_flag, group_m);
+    case 4: return launch_tc<4, BK, BN>(c, g, err_flag, group_m);
+    case 5: return launch_tc<5, BK, BN>(c, g, err_flag, group_m);
+    case 6: return launch_tc<6, BK, BN>(c, g, err_flag, group_m);
     default: return set_error(c, THC_ERR_ARG, "ozgemm_tc: levels must be 2..6");
   }
 }
@@ -779,8 +800,9 @@ int launch_choice(Ctx* c, const OzArgs& g_in, int* err_flag, const TcChoice& ch)
   OzArgs g = g_in;
   g.ksplit = ch.ksplit;
   if (g.ksplit <= 1) { g.ksplit = 1; g.part = nullptr; }
-  return ch.bk == 32 ? launch_bk<32>(c, g, err_flag, ch.group_m)
-                     : launch_bk<16>(c, g, err_flag, ch.group_m);
+  if (ch.bn == 64) return launch_bk<16, 64>(c, g, err_flag, ch.group_m);
+  return ch.bk == 32 ? launch_bk<32, 128>(c, g, err_flag, ch.group_m)
+                     : launch_bk<16, 128>(c, g, err_flag, ch.group_m);
 }
 
 // The autotuner's decisions, one table per process and device, keyed by the shape class of a
@@ -816,9 +838,9 @@ std::string ozgemm_tune_log(int device)
     const TuneEntry& e = kv.second;
     snprintf(buf, sizeof(buf),
              "M<=2^%lld N<=2^%lld K<=2^%lld slices=%lld epi=%lld lower=%lld split<=%lld: bk=%d "
-             "group_m=%d split=%d %.1fus (%d tried)\n",
-             k[1], k[2], k[3], k[4], k[5], k[6], k[7], e.choice.bk, e.choice.group_m,
-             e.choice.ksplit, e.us, e.candidates);
+             "bn=%d group_m=%d split=%d %.1fus (%d tried)\n",
+             k[1], k[2], k[3], k[4], k[5], k[6], k[7], e.choice.bk, e.choice.bn,
+             e.choice.group_m, e.choice.ksplit, e.us, e.candidates);
     out += buf;
   }
   return out;
@@ -830,7 +852,7 @@ int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
   if (!g.b.k_contig) return set_error(c, THC_ERR_ARG, "ozgemm_tc: B must be K-contiguous");
   const long long ar = g.a.kt_stride ? g.a.slice_stride / 32 : g.a.slice_stride / g.a.ld;
   const long long br = g.b.kt_stride ? g.b.slice_stride / 32 : g.b.slice_stride / g.b.ld;
-  if (g.a.ld % 32 || g.b.ld % 32 || ar % TBM || br % TBN)
+  if (g.a.ld % 32 || g.b.ld % 32 || ar % TBM || br % 128)
     return set_error(c, THC_ERR_ARG, "ozgemm_tc: operand padding");
   TcChoice dflt;
   dflt.bk = c->tc_bk;
@@ -841,9 +863,10 @@ int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
   std::lock_guard<std::mutex> lk(g_tune_mu);   // one tuning at a time; look-ups are brief
   auto it = g_tune.find(key);
   if (it != g_tune.end()) return launch_choice(c, g, err_flag, it->second.choice);
-  // Candidates: k-step 32 / 16, 8 / 16 m-tiles per group, the caller's split and half of
-  // it.  Products above ~10 ms of tensor work keep the default (their tiles fill the GPU
-  // many times over and a trial run would cost more than any choice gains).
+  // Candidates: 128-wide tiles with k-step 32 / 16, 64-wide tiles (k-step 16, two CTAs per
+  // SM), each with 8 / 16 m-tiles per group and the caller's split or half of it.  Products
+  // above ~10 ms of tensor work keep the default (their tiles fill the GPU many times over
+  // and a trial run would cost more than any choice gains).
   const double work = (double)g.levels * (g.levels + 1) / 2 * 2.0 * g.M * g.N * g.K;
   TuneEntry e;
   e.choice = dflt;
@@ -852,13 +875,14 @@ int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
     return launch_choice(c, g, err_flag, dflt);
   }
   std::vector<TcChoice> cands;
-  for (int bk : {32, 16})
+  for (int v : {0, 1, 2})              // (bk, bn) = (32, 128), (16, 128), (16, 64)
     for (int gm : {8, 16})
       for (int sp : {g.ksplit, std::max(1, g.ksplit / 2)}) {
         TcChoice ch;
-        ch.bk = bk; ch.group_m = gm; ch.ksplit = sp;
+        ch.bk = v == 0 ? 32 : 16; ch.bn = v == 2 ? 64 : 128; ch.group_m = gm; ch.ksplit = sp;
         bool dup = false;
-        for (const auto& x : cands) dup |= x.bk == bk && x.group_m == gm && x.ksplit == sp;
+        for (const auto& x : cands)
+          dup |= x.bk == ch.bk && x.bn == ch.bn && x.group_m == gm && x.ksplit == sp;
         if (!dup) cands.push_back(ch);
       }
   cudaEvent_t ea = nullptr, eb = nullptr;
