@@ -2,14 +2,14 @@
 //
 // Each row of A (each column of B) is scaled by a power of two 2^e so that its entries lie
 // in (-1, 1), then split into s integer slices of 7 bits:
-//     x = 2^e * sum_{i<s} S_i 2^{-7(i+1)},  |S_0| <= 128, |S_i| <= 64 (i >= 1),
+//     x = 2^e * sum_{i<s} S_i 2^{-7(i+1)},  |S_0| <= 128, |S_3| <= 72, |S_i| <= 64 otherwise,
 // every slice exactly representable in BF16 and stored pre-scaled as S_i 2^{-7i}.  The
 // product keeps the slice pairs with i + j <= L (L = s - 1):
 //     C[m,n] = 2^{eA[m] + eB[n] - 14} sum_{l<=L} sum_{i+j=l} sum_k (S_i 2^{-7i})[m,k] (T_j 2^{-7j})[k,n].
 // Every slice product of level l is an integer multiple of 2^{-7l} below 2^{14-7l} in
-// magnitude and every level sum over a chunk of 256 k (512 on the tensor-core kernel) such
-// a multiple below 2^{24-7l}, so the tensor cores' FP32 accumulation of a
-// chunk is exact; chunks are combined in FP64.  The only error is the truncation of the
+// magnitude (levels 0-2 use digits 0-2 only) and every level sum over a chunk of 256 k (512
+// on the tensor-core kernel, for levels 0-2) such a multiple below 2^{24-7l}, so the tensor
+// cores' FP32 accumulation of a chunk is exact; chunks are combined in FP64.  The only error is the truncation of the
 // slice expansion, about (L+2) 2^{-7(L+1)} relative to sum_k |A||B|.
 #pragma once
 
