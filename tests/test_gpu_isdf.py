@@ -162,6 +162,25 @@ def test_sliced_gemm_tc_matches_mma_sync(lib):
         assert d < 1e-7
 
 
+@pytest.mark.parametrize("name", ["tiny", "c2"])
+def test_sliced_gemm_tile_widths(lib, name):
+    """Every product of the mixed path through the 64-wide tiles (two CTAs per SM) and the
+    128-wide ones, the autotuner off: the same exact slice products in another tile order,
+    so M agrees to the path's rounding (zeta is FP32), and both match the oracle."""
+    s = system(name)
+    idx = kmeans_idx(name)
+    ref = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG)["M"]
+    out = {}
+    for bn in (128, 64):
+        with capi.Context(0, capi.THC_PREC_MIXED) as ctx:
+            ctx.set_option("tc_bn", bn)
+            out[bn] = _cplx(ctx.isdf(s.phi, idx, s.mesh, s.coulG)["M"])
+        e = _rel(out[bn], ref)
+        print(f"{name} tile width {bn}: ||dM||/||M|| vs oracle = {e:.3e}")
+        assert e < 1e-6
+    assert _rel(out[64], out[128]) < 1e-7
+
+
 def test_isdf_mesh_mismatch(gpu_ctx_fp64):
     s = system("tiny")
     r = gpu_ctx_fp64.isdf(s.phi, kmeans_idx("tiny"), (16, 16, 15), s.coulG, raise_on_error=False)

@@ -192,6 +192,8 @@ int thc_ctx_create(int device, int precision, thc_ctx** out)
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_check[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_check[1], cudaEventDisableTiming) != cudaSuccess ||
       cudaMallocHost(&c->pinned, 4096) != cudaSuccess) {
     cudaGetLastError();
     delete h;
@@ -228,6 +230,8 @@ int thc_ctx_destroy(thc_ctx* h)
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (cudaEvent_t e : c->ev_check)
+    if (e) cudaEventDestroy(e);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->aux_stream) {
@@ -288,6 +292,12 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
   if (!strcmp(key, "tc_bk")) {
     if (value != 16.0 && value != 32.0) return THC_ERR_ARG;
     h->c.tc_bk = (int)value;
+    h->c.autotune = 0;
+    return THC_OK;
+  }
+  if (!strcmp(key, "tc_bn")) {
+    if (value != 64.0 && value != 128.0) return THC_ERR_ARG;
+    h->c.tc_bn = (int)value;
     h->c.autotune = 0;
     return THC_OK;
   }

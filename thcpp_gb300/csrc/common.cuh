@@ -87,6 +87,7 @@ struct Ctx {
   std::map<std::tuple<int, int, int, int, int>, size_t> plan_work;   // their work-area bytes
   void* pinned = nullptr;          // 4 KB pinned host scratch
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_check[2] = {nullptr, nullptr};   // k-means convergence checks in flight
   long long launches = 0;
   int slices_p = 6;
   int slices_z = 6;
@@ -101,6 +102,9 @@ struct Ctx {
   // faster: 0.90 s against 1.00 s for the zeta product at N_g 1.26e6, N_mu 5184) or 16
   // (4 stages of half the size).
   int tc_bk = 32;
+  // Tile width of the tensor-core GEMM without the autotuner: 128, or 64 (k-step 16, two
+  // CTAs per SM).  Setting "tc_bn" turns the autotuner off for the context.
+  int tc_bn = 128;
   // Pick the tensor-core kernel's k-step, tile order and split of K per shape class by
   // timing the candidates the first time a class is met (process-wide table; ozgemm_tc.cu).
   // Setting "tc_bk" turns it off for the context.

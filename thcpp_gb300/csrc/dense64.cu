@@ -43,6 +43,9 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
     kbeg = blockIdx.z * kc;
     kend = min(g.K, kbeg + kc);
   }
+  // Tiles start at multiples of T >= BK, so the first nonzero k is a multiple of BK.
+  if (g.a_zero_below) kbeg = max(kbeg, (int)m0);
+  if (g.b_zero_below) kbeg = max(kbeg, (int)n0);
   for (int k0 = kbeg; k0 < kend; k0 += BK) {
 #pragma unroll
     for (int r = 0; r < LOADS; r++) {
@@ -453,6 +456,7 @@ int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* din
     g.M = nb; g.N = i0; g.K = i0;                       // T = L[i, 0:i] X[0:i, 0:i]
     g.A = L + (long long)i0 * ld; g.sam = ld; g.sak = 1;
     g.B = X; g.sbn = 1; g.sbk = ld;
+    g.b_zero_below = 1;                                 // X[0:i, 0:i] is lower triangular
     g.C = T; g.ldc = n;
     g.skip_flag = cs ? &cs->flag : nullptr;
     int st = dgemm(c, g);
@@ -472,6 +476,7 @@ int chol_inverse(Ctx* c, const double* L, long long ld, int n, const double* din
   g.M = n; g.N = n; g.K = n;                            // Cinv = X^T X
   g.A = X; g.sam = 1; g.sak = ld;
   g.B = X; g.sbn = 1; g.sbk = ld;
+  g.a_zero_below = g.b_zero_below = 1;                  // X lower triangular
   g.C = Cinv; g.ldc = n;
   g.skip_flag = cs ? &cs->flag : nullptr;
   return dgemm(c, g);

@@ -28,6 +28,11 @@ struct GemmArgs {
   int ksplit = 1;                    // > 1: K is split over blockIdx.z into FP64 partials
   double* part = nullptr;            // ksplit x M x N partial buffer (row-major, ld = N)
   int aliased = 0;                   // C overlaps A or B: products go through partials
+  // Known zeros: A(m, k) = 0 for k < m (a_zero_below) / B(k, n) = 0 for k < n
+  // (b_zero_below), as for a lower-triangular factor read transposed / as it is.  A tile
+  // then starts its k loop at its first row / column: the skipped terms are exact zeros,
+  // so the result is bit-identical.
+  int a_zero_below = 0, b_zero_below = 0;
   int tile = 64;                     // CTA tile edge (64, 32 or 16; chosen by dgemm)
 };
 

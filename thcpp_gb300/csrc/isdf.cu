@@ -480,6 +480,7 @@ int isdf_run(Ctx* c, const double* phi_in, long long ng, int no, const int* idx_
     GemmArgs g;                                   // C^{-1}_k = X^T (P X)
     g.M = nmu; g.N = nmu; g.K = nmu;
     g.A = Xinv; g.sam = 1; g.sak = nmu;
+    g.a_zero_below = 1;                           // X lower triangular, read transposed
     g.B = xt; g.sbn = 1; g.sbk = nmu;
     g.C = Cinv; g.ldc = nmu;
     if ((st = dgemm(c, g))) return st;

@@ -1578,7 +1578,7 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
   }
   THC_CUDA(c, cudaFuncSetAttribute(km_sums, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)sizeof(SumSmem)));
-  int* hflag = (int*)c->pinned;
+  int* hflag = (int*)c->pinned;   // [2]: the done flag after a block of iterations
   const int kCheckEvery = 8;
   // One k-means iteration; every kernel reads the iteration index from device state and
   // returns at once after convergence, so the same launch sequence serves any iteration.
@@ -1663,8 +1663,13 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
       c->km_graphs.emplace_back(key, gexec);
     }
   }
-  for (int it = 0; it < max_it;) {
-    int nblock = std::min(kCheckEvery, max_it - it);
+  // Blocks of kCheckEvery iterations, the host's convergence check one block behind the GPU:
+  // the done flag after block k is copied (with an event) while block k + 1 runs, so the GPU
+  // never waits for the host between blocks.  Iterations after convergence return at once,
+  // so at most one block of empty launches is spent after the last real iteration.
+  int launched = 0, blocks = 0, checked = 0;
+  auto launch_block = [&]() -> int {
+    const int nblock = std::min(kCheckEvery, max_it - launched);
     if (gexec && nblock == kCheckEvery) {
       THC_CUDA(c, cudaGraphLaunch(gexec, s));
       c->launches += (mixed ? 6LL : 5LL) * kCheckEvery;  // kernels per captured iteration
@@ -1674,11 +1679,24 @@ int kmeans_run(Ctx* c, const double* grid_in, const double* rho_in, long long ng
         if (rc) return rc;
       }
     }
-    it += nblock;
-    if (it < max_it) {
-      THC_CUDA(c, cudaMemcpyAsync(hflag, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
-      THC_CUDA(c, cudaStreamSynchronize(s));
-      if (*hflag) break;
+    launched += nblock;
+    const int slot = blocks++ & 1;
+    THC_CUDA(c, cudaMemcpyAsync(hflag + slot, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+    THC_CUDA(c, cudaEventRecord(c->ev_check[slot], s));
+    return THC_OK;
+  };
+  while (launched < max_it && blocks < 2) {
+    int rc = launch_block();
+    if (rc) return rc;
+  }
+  while (checked < blocks) {
+    const int slot = checked & 1;
+    THC_CUDA(c, cudaEventSynchronize(c->ev_check[slot]));
+    checked++;
+    if (hflag[slot]) break;                  // converged (or stopped): later blocks are no-ops
+    if (launched < max_it) {
+      int rc = launch_block();
+      if (rc) return rc;
     }
   }
   km_normdiff_exact<<<1, 1024, 0, s>>>(b);

@@ -855,7 +855,8 @@ int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
   if (g.a.ld % 32 || g.b.ld % 32 || ar % TBM || br % 128)
     return set_error(c, THC_ERR_ARG, "ozgemm_tc: operand padding");
   TcChoice dflt;
-  dflt.bk = c->tc_bk;
+  dflt.bk = c->tc_bn == 64 ? 16 : c->tc_bk;
+  dflt.bn = c->tc_bn;
   dflt.ksplit = g.ksplit;
   if (!c->autotune) return launch_choice(c, g, err_flag, dflt);
   const std::vector<long long> key = {c->device, ilog2c(g.M), ilog2c(g.N), ilog2c(g.K),
