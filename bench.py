@@ -45,7 +45,7 @@ WORKLOAD = "c2"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per sliced-GEMM launch, mean of
 # the three launches of one factorisation, from one ncu capture of the workload; None where
 # no capture was taken.
-OZ_TRAFFIC = {"c2": ((43.3 + 170.5) + (341.8 + 97.0) + (295.4 + 5.3)) * 1e6 / 3.0}
+OZ_TRAFFIC = {"c2": ((43.2 + 170.2) + (341.4 + 95.9) + (295.2 + 4.7)) * 1e6 / 3.0}
 CONFIG = dict(WORKLOADS[WORKLOAD], kmeans_max_it=100, kmeans_threshold=1e-6,
               l2="flushed (256 MB write) before every timed step", parallelism="replicas")
 METRIC = "ISDF s/system on 1 GB300 (mixed precision; FP64 path reported beside)"
