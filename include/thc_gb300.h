@@ -105,7 +105,10 @@ int thc_ctx_set_stream(thc_ctx* ctx, void* cuda_stream);
  * k-means iteration block as a CUDA graph, the default); "tc_bk" (k-step per
  * pipeline stage of the tensor-core kernel: 32, the default, or 16; setting it turns the
  * autotuner off); "tc_bn" (tile width of the tensor-core kernel: 128, the default, or 64
- * with k-step 16 and two CTAs per SM; setting it turns the autotuner off); "autotune" (1 = choose k-step, tile order and split of K per product shape
+ * with k-step 16 and two CTAs per SM; setting it turns the autotuner off); "tc_persistent"
+ * (1 = the persistent tensor-core kernel, one CTA per SM walking 128 x 64 tiles with two TMEM
+ * buffers, for every product with K <= 512 and no split of K; setting it turns the
+ * autotuner off); "autotune" (1 = choose k-step, tile order and split of K per product shape
  * by timing the candidates once per process, the default); "fft64" (mixed path: 1 = zeta
  * in FP64 through a D2Z FFT, 0 = FP32 and R2C, the default);
  * "profile" (1 = record a CUDA event pair around every launch of the named kernels,

@@ -164,21 +164,27 @@ def test_sliced_gemm_tc_matches_mma_sync(lib):
 
 @pytest.mark.parametrize("name", ["tiny", "c2"])
 def test_sliced_gemm_tile_widths(lib, name):
-    """Every product of the mixed path through the 64-wide tiles (two CTAs per SM) and the
-    128-wide ones, the autotuner off: the same exact slice products in another tile order,
-    so M agrees to the path's rounding (zeta is FP32), and both match the oracle."""
+    """Every product of the mixed path through the 64-wide tiles (two CTAs per SM), the
+    persistent kernel (for the products with K <= 512: P and, at these sizes, zeta) and the
+    128-wide tiles, the autotuner off: the same exact slice products in another tile order
+    (the persistent kernel drains its level >= 3 accumulator once per tile instead of every
+    128 k), so M agrees to the path's rounding (zeta is FP32), and all match the oracle."""
     s = system(name)
     idx = kmeans_idx(name)
     ref = oracle.isdf_real(s.phi, idx, s.mesh, s.coulG)["M"]
     out = {}
-    for bn in (128, 64):
+    for key, opt in (("128", ("tc_bn", 128)), ("64", ("tc_bn", 64)),
+                     ("persistent", ("tc_persistent", 1))):
         with capi.Context(0, capi.THC_PREC_MIXED) as ctx:
-            ctx.set_option("tc_bn", bn)
-            out[bn] = _cplx(ctx.isdf(s.phi, idx, s.mesh, s.coulG)["M"])
-        e = _rel(out[bn], ref)
-        print(f"{name} tile width {bn}: ||dM||/||M|| vs oracle = {e:.3e}")
+            ctx.set_option(*opt)
+            r = ctx.isdf(s.phi, idx, s.mesh, s.coulG)
+            assert r["status"] == 0
+            out[key] = _cplx(r["M"])
+        e = _rel(out[key], ref)
+        print(f"{name} tiles {key}: ||dM||/||M|| vs oracle = {e:.3e}")
         assert e < 1e-6
-    assert _rel(out[64], out[128]) < 1e-7
+    assert _rel(out["64"], out["128"]) < 1e-7
+    assert _rel(out["persistent"], out["128"]) < 1e-7
 
 
 def test_isdf_mesh_mismatch(gpu_ctx_fp64):

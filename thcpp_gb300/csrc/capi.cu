@@ -301,6 +301,11 @@ int thc_ctx_set_option(thc_ctx* h, const char* key, double value)
     h->c.autotune = 0;
     return THC_OK;
   }
+  if (!strcmp(key, "tc_persistent")) {
+    h->c.tc_persistent = value != 0.0;
+    h->c.autotune = 0;
+    return THC_OK;
+  }
   if (!strcmp(key, "autotune")) {
     h->c.autotune = value != 0.0;
     return THC_OK;

@@ -105,6 +105,9 @@ struct Ctx {
   // Tile width of the tensor-core GEMM without the autotuner: 128, or 64 (k-step 16, two
   // CTAs per SM).  Setting "tc_bn" turns the autotuner off for the context.
   int tc_bn = 128;
+  // Without the autotuner: the persistent short-K kernel (64-wide tiles, two TMEM buffers)
+  // for every product it takes (K <= 512, no split of K, no triangle).
+  int tc_persistent = 0;
   // Pick the tensor-core kernel's k-step, tile order and split of K per shape class by
   // timing the candidates the first time a class is met (process-wide table; ozgemm_tc.cu).
   // Setting "tc_bk" turns it off for the context.

@@ -695,6 +695,341 @@ __global__ void __launch_bounds__(TTHREADS, (BN == 128 ? 1 : 2))
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Persistent variant for short K (K <= 512, no split): one CTA per SM walks the tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ... in the grouped order, with 128 x 64 tiles and two
+// TMEM buffers of four 64-column accumulators, so the epilogue of one tile (TMEM drain,
+// double-word fold, staging and stores) runs while the MMAs of the next tile fill the other
+// buffer, and the TMA ring of stages runs on across tiles.  With K <= 512 every exact level
+// is exact over the whole K and the level >= 3 accumulator is drained once, at the end of
+// the tile.  The epilogue stages its results in a buffer of its own (the stage ring stays
+// in use).
+constexpr int kPersistBudget = 176 * 1024;   // stage ring + epilogue staging
+
+template <int LV, int BK>
+struct TpCfg {
+  static constexpr int BN = 64;
+  static constexpr int A_BYTES = TBM * BK * 2;
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = LV * (A_BYTES + B_BYTES);
+  static constexpr int EC = BN / 2;                          // columns per epilogue warp
+  static constexpr int STG_BYTES = TEPI_WARPS * 32 * EC * 8;  // epilogue staging
+  static constexpr int STAGES_FIT = (kPersistBudget - STG_BYTES) / STAGE_BYTES;
+  static constexpr int STAGES = STAGES_FIT < 4 ? STAGES_FIT : 4;
+  static constexpr int NEXACT = LV < 3 ? LV : 3;
+  static constexpr int BUF_COLS = 4 * BN;                    // one buffer of accumulators
+  // stage ring | staging | barriers (256 B) | exponents (8 warps x 32 ints) | guard
+  static constexpr size_t SMEM =
+      (size_t)STAGES * STAGE_BYTES + STG_BYTES + 1024 + 256 + 1024 + kSmemGuard;
+  static_assert(STAGES >= 2, "stage ring");
+};
+
+// Tile t of the grouped order (group_m m-tiles per n-tile, as ozgemm_tc_kernel's grid).
+__device__ __forceinline__ void tile_coords(long long t, long long mtn, long long ntn,
+                                            long long grpm, long long& mt, long long& nt)
+{
+  const long long per_group = grpm * ntn;
+  const long long grp = t / per_group, first_m = grp * grpm;
+  const long long gm = mtn - first_m < grpm ? mtn - first_m : grpm;
+  const long long r = t - grp * per_group;
+  mt = first_m + r % gm;
+  nt = r / gm;
+}
+
+template <int LV, int BK>
+__global__ void __launch_bounds__(TTHREADS, 1)
+    ozgemm_tc_persistent(const __grid_constant__ CUtensorMap ta,
+                         const __grid_constant__ CUtensorMap tb, TcArgs g)
+{
+  using Cfg = TpCfg<LV, BK>;
+  constexpr int BN = Cfg::BN, EC = Cfg::EC;
+  constexpr int A_BYTES = Cfg::A_BYTES, B_BYTES = Cfg::B_BYTES, STAGE_BYTES = Cfg::STAGE_BYTES;
+  constexpr int NST = Cfg::STAGES;
+  const long long mtn = (g.M + TBM - 1) / TBM, ntn = (g.N + BN - 1) / BN;
+  const long long ntiles = mtn * ntn;
+
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* stg_base = smem + (size_t)NST * STAGE_BYTES;
+  uint64_t* full = (uint64_t*)(stg_base + Cfg::STG_BYTES);
+  uint64_t* empty = full + NST;
+  uint64_t* acc_full = empty + NST;          // [2] a buffer's accumulators are final
+  uint64_t* acc_empty = acc_full + 2;        // [2] the epilogue has drained a buffer
+  uint64_t* mma_done = acc_empty + 2;
+  uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
+  volatile int* abort = (volatile int*)(tmem_slot + 1);
+  volatile int* issued = abort + 1;
+  volatile int* consumed = issued + 1;
+  int* sexp = (int*)((unsigned char*)full + 256);   // 8 warps x 32 column exponents
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nstages = (int)((g.K + BK - 1) / BK);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NST; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], TEPI_WARPS);
+    }
+    mbar_init(mma_done, 1);
+    *abort = 0;
+    *issued = 0;
+    *consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                     su32(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------------ TMA producer
+    if (lane == 0) {
+      int git = 0;
+      bool ok = true;
+      for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        long long mt, nt;
+        tile_coords(t, mtn, ntn, g.group_m, mt, nt);
+        const long long m0 = mt * TBM, n0 = nt * BN;
+        for (int it = 0; it < nstages; it++, git++) {
+          const int s = git % NST;
+          const uint32_t ph = (uint32_t)((git / NST) & 1);
+          if (!mbar_wait(&empty[s], ph ^ 1, abort, g.spin_limit)) { ok = false; break; }
+          unsigned char* st = smem + s * STAGE_BYTES;
+          *issued = git + 1;
+          mbar_expect_tx(&full[s], STAGE_BYTES);
+          const long long k = (long long)it * BK;
+          const int ax = g.a_tile_rows ? (int)(k & 31) : (int)k;
+          const int bx = g.b_tile_rows ? (int)(k & 31) : (int)k;
+          const long long ay0 = g.a_tile_rows ? (k >> 5) * g.a_tile_rows : 0;
+          const long long by0 = g.b_tile_rows ? (k >> 5) * g.b_tile_rows : 0;
+#pragma unroll
+          for (int sl = 0; sl < LV; sl++) {
+            tma_load_2d(st + sl * A_BYTES, &ta, ax, (int)(ay0 + sl * g.a_rows_pad + m0), &full[s]);
+            tma_load_2d(st + LV * A_BYTES + sl * B_BYTES, &tb, bx,
+                        (int)(by0 + sl * g.b_rows_pad + n0), &full[s]);
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      int git = 0, tc = 0;
+      bool ok = true;
+      for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x, tc++) {
+        const int b = tc & 1, use = tc >> 1;
+        const uint32_t acc0 = tmem + (uint32_t)(b * Cfg::BUF_COLS);
+        if (use > 0) {
+          if (!mbar_wait(&acc_empty[b], (uint32_t)((use - 1) & 1), abort, g.spin_limit)) break;
+          asm volatile("tcgen05.fence::after_thread_sync;\n");
+        }
+        for (int it = 0; it < nstages; it++, git++) {
+          const int s = git % NST;
+          const uint32_t ph = (uint32_t)((git / NST) & 1);
+          if (!mbar_wait(&full[s], ph, abort, g.spin_limit)) { ok = false; break; }
+          *consumed = git + 1;
+          asm volatile("tcgen05.fence::after_thread_sync;\n");
+          unsigned char* st = smem + s * STAGE_BYTES;
+          const uint32_t a0 = su32(st), b0 = su32(st + LV * A_BYTES);
+          bool first_hi = it == 0;
+#pragma unroll
+          for (int l = 0; l < LV; l++) {
+            bool first = it == 0;
+#pragma unroll
+            for (int i = 0; i <= l; i++) {
+              const int j = l - i;
+#pragma unroll
+              for (int kk = 0; kk < BK / 16; kk++) {
+                const uint64_t ad = sdesc<BK>(a0 + i * A_BYTES + kk * 32);
+                const uint64_t bd = sdesc<BK>(b0 + j * B_BYTES + kk * 32);
+                if (l < 3) {
+                  umma<BN>(acc0 + l * BN, ad, bd, first ? 0u : 1u);
+                  first = false;
+                } else {
+                  umma<BN>(acc0 + 3 * BN, ad, bd, first_hi ? 0u : 1u);
+                  first_hi = false;
+                }
+              }
+            }
+          }
+          umma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        umma_commit(&acc_full[b]);
+      }
+      umma_commit(mma_done);
+    }
+  } else {
+    // ------------------------------------------------------------------ epilogue
+    const int ew = warp - 2;
+    const int quad = warp & 3;
+    const int half = ew >> 2;
+    const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
+    const int col0 = half * EC;
+    int* seb = sexp + ew * 32;
+    unsigned char* stg = stg_base + (size_t)ew * (32 * EC * 8);
+    float* stg32 = (float*)stg;
+    double* stg64 = (double*)stg;
+    const int mode = g.epilogue;
+    int tc = 0;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, tc++) {
+      const int b = tc & 1, use = tc >> 1;
+      long long mt, nt;
+      tile_coords(t, mtn, ntn, g.group_m, mt, nt);
+      const long long m0 = mt * TBM, n0 = nt * BN;
+      {
+        const long long na = n0 + col0 + lane;
+        seb[lane] = na < g.N ? g.eb[na] : 0;
+      }
+      const long long m = m0 + quad * 32 + lane;
+      const int ea = (m < g.M ? g.ea[m] : 0) - 14;
+      __syncwarp();
+      if (!mbar_wait(&acc_full[b], (uint32_t)(use & 1), abort, g.spin_limit)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;\n");
+      const uint32_t acc0 = tmem + (uint32_t)(b * Cfg::BUF_COLS) + lane_base;
+      float ah[EC], al[EC];
+#pragma unroll
+      for (int bb = 0; bb < EC / 8; bb++) {
+        float l0[8], l1[8], l2[8], hi[8];
+        const uint32_t cb = (uint32_t)(col0 + 8 * bb);
+        tmem_ld8(acc0 + 0 * BN + cb, l0);
+        if (LV > 1) tmem_ld8(acc0 + 1 * BN + cb, l1);
+        if (LV > 2) tmem_ld8(acc0 + 2 * BN + cb, l2);
+        if (LV > 3) tmem_ld8(acc0 + 3 * BN + cb, hi);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          // The exact levels' sum needs <= 38 bits and is carried exactly in (s1, e1); the
+          // levels >= 3 (<= 2^-21 of the value) go to the low word.
+          float s1 = l0[q], e1 = 0.f;
+          if (LV > 1) two_sum(l0[q], l1[q], s1, e1);
+          if (LV > 2) {
+            float s2, e2;
+            two_sum(s1, l2[q], s2, e2);
+            s1 = s2;
+            e1 = __fadd_rn(e1, e2);
+          }
+          float h = 0.f, lo = LV > 3 ? hi[q] : 0.f;
+          dw_add(h, lo, s1);
+          dw_add(h, lo, e1);
+          ah[8 * bb + q] = h;
+          al[8 * bb + q] = lo;
+        }
+      }
+      // The buffer is free for the MMAs of the tile after next.
+      asm volatile("tcgen05.fence::before_thread_sync;\n");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[b]);
+      if (mode == OZ_STORE_F32) {
+#pragma unroll
+        for (int q = 0; q < EC; q++) {
+          const int ex = ea + seb[q];
+          const float v = (ex > -126 && ex < 127) ? __fadd_rn(ah[q], al[q]) * pow2f(ex)
+                                                  : wide_f32(ah[q], al[q], ex);
+          stg32[lane * EC + (q ^ lane)] = v;
+        }
+      } else if (mode == OZ_SQUARE_DW) {
+#pragma unroll
+        for (int q = 0; q < EC; q++) {
+          const int ex = ea + seb[q];
+          double w;
+          if (ex > -60 && ex < 60) {
+            const float sc = pow2f(ex);
+            const float h = ah[q] * sc, l = al[q] * sc;
+            const float pp = __fmul_rn(h, h);
+            float e = __fmaf_rn(h, h, -pp);
+            e = __fmaf_rn(2.f * h, l, e);
+            float zh, zl;
+            fast_two_sum(pp, e, zh, zl);
+            w = __hiloint2double(__float_as_int(zl), __float_as_int(zh));
+          } else {
+            w = wide_result(ah[q], al[q], ex, mode);
+          }
+          stg64[lane * EC + (q ^ (lane & 15))] = w;
+        }
+      } else if (mode == OZ_STORE_DW) {
+#pragma unroll
+        for (int q = 0; q < EC; q++) {
+          const int ex = ea + seb[q];
+          double w;
+          if (ex > -100 && ex < 100) {
+            const float sc = pow2f(ex);
+            float zh, zl;
+            fast_two_sum(ah[q] * sc, al[q] * sc, zh, zl);
+            w = __hiloint2double(__float_as_int(zl), __float_as_int(zh));
+          } else {
+            w = wide_result(ah[q], al[q], ex, mode);
+          }
+          stg64[lane * EC + (q ^ (lane & 15))] = w;
+        }
+      } else {
+        const bool sq = mode == OZ_SQUARE_F64;
+#pragma unroll
+        for (int q = 0; q < EC; q++) {
+          double val = ((double)ah[q] + (double)al[q]) * pow2d(ea + seb[q]);
+          if (sq) val = val * val;
+          stg64[lane * EC + (q ^ (lane & 15))] = val;
+        }
+      }
+      __syncwarp();
+      // Two rows per pass: 16 lanes per row, two adjacent columns per lane.
+      const bool f32 = mode == OZ_STORE_F32;
+      const int c0 = 2 * (lane & 15);
+      const long long n = n0 + col0 + c0;
+      for (int r0 = 0; r0 < 32; r0 += 2) {
+        const int r = r0 + (lane >> 4);
+        const long long mr = m0 + quad * 32 + r;
+        if (mr >= g.M) break;
+        const bool v0 = n < g.N, v1 = n + 1 < g.N;
+        const long long off = mr * g.ldc + n;
+        if (f32) {
+          const float a = stg32[r * EC + (c0 ^ r)], bv = stg32[r * EC + ((c0 + 1) ^ r)];
+          float* dst = (float*)g.C + off;
+          if (v0 && v1 && !((uintptr_t)dst & 7)) *(float2*)dst = make_float2(a, bv);
+          else {
+            if (v0) dst[0] = a;
+            if (v1) dst[1] = bv;
+          }
+        } else {
+          const double a = stg64[r * EC + (c0 ^ (r & 15))];
+          const double bv = stg64[r * EC + ((c0 + 1) ^ (r & 15))];
+          double* dst = (double*)g.C + off;
+          if (v0 && v1 && !((uintptr_t)dst & 15)) *(double2*)dst = make_double2(a, bv);
+          else {
+            if (v0) dst[0] = a;
+            if (v1) dst[1] = bv;
+          }
+        }
+      }
+      __syncwarp();   // the staging and the exponents are rewritten for the next tile
+    }
+  }
+  // ---------------------------------------------------------------------- teardown
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (*abort) {
+      atomicExch(g.error, 1);
+      for (int it = *consumed; it < *issued; it++)
+        mbar_drain(&full[it % NST], (uint32_t)((it / NST) & 1));
+    }
+    mbar_drain(mma_done, 0);
+  }
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 get_encoder()
 {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -736,7 +1071,15 @@ struct TcChoice {
   int group_m = 8;
   int ksplit = 1;
   int bn = 128;          // tile width: 128, or 64 (with bk = 16) for two CTAs per SM
+  int persistent = 0;    // ozgemm_tc_persistent (bn 64, bk 16; K <= 512, no split)
 };
+
+// Products the persistent kernel takes: the whole K in one exact chunk, no split of K, no
+// triangle.
+bool persistent_ok(const OzArgs& g)
+{
+  return g.K <= kChunkK && g.ksplit <= 1 && !g.lower_only;
+}
 
 template <int LV, int BK, int BN>
 int launch_tc(Ctx* c, const OzArgs& g, int* err_flag, int group_m)
@@ -795,11 +1138,68 @@ int launch_bk(Ctx* c, const OzArgs& g, int* err_flag, int group_m)
   }
 }
 
+template <int LV>
+int launch_persistent(Ctx* c, const OzArgs& g, int* err_flag, int group_m)
+{
+  using Cfg = TpCfg<LV, 16>;
+  if (!persistent_ok(g)) return set_error(c, THC_ERR_ARG, "ozgemm_tc: persistent kernel takes K <= 512");
+  CUtensorMap ta, tb;
+  const bool at = g.a.kt_stride > 0, bt = g.b.kt_stride > 0;
+  long long a_rows = at ? g.a.slice_stride / 32 : g.a.slice_stride / g.a.ld;
+  long long b_rows = bt ? g.b.slice_stride / 32 : g.b.slice_stride / g.b.ld;
+  if ((at && g.a.kt_stride != LV * g.a.slice_stride) ||
+      (bt && g.b.kt_stride != LV * g.b.slice_stride))
+    return set_error(c, THC_ERR_ARG, "ozgemm_tc: tiled operand with another slice count");
+  int st = at ? make_map(c, &ta, g.a.s, 32, (g.a.ld / 32) * (g.a.kt_stride / 32), TBM, 16)
+              : make_map(c, &ta, g.a.s, g.a.ld, a_rows * LV, TBM, 16);
+  if (st) return st;
+  st = bt ? make_map(c, &tb, g.b.s, 32, (g.b.ld / 32) * (g.b.kt_stride / 32), Cfg::BN, 16)
+          : make_map(c, &tb, g.b.s, g.b.ld, b_rows * LV, Cfg::BN, 16);
+  if (st) return st;
+  TcArgs t;
+  t.M = g.M; t.N = g.N; t.K = g.K;
+  t.a_rows_pad = a_rows; t.b_rows_pad = b_rows;
+  t.a_tile_rows = at ? g.a.kt_stride / 32 : 0;
+  t.b_tile_rows = bt ? g.b.kt_stride / 32 : 0;
+  t.hi_stages = 0;
+  t.ea = g.a.e; t.eb = g.b.e; t.C = g.C; t.ldc = g.ldc;
+  t.epilogue = g.epilogue; t.lower_only = 0; t.error = err_flag;
+  t.spin_limit = c->spin_limit;
+  t.group_m = group_m;
+  t.ksplit = 1; t.part = nullptr;
+  int sms = 0;
+  THC_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  const long long tiles = cdiv(g.M, TBM) * cdiv(g.N, Cfg::BN);
+  const unsigned grid = (unsigned)std::min<long long>(tiles, sms);
+  THC_CUDA(c, cudaFuncSetAttribute(ozgemm_tc_persistent<LV, 16>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
+  {
+    ProfScope prof(c, "ozgemm");
+    ProfScope prof_tag(g.tag ? c : nullptr, g.tag ? g.tag : "");
+    ozgemm_tc_persistent<LV, 16><<<grid, TTHREADS, Cfg::SMEM, c->stream>>>(ta, tb, t);
+    THC_LAUNCHED(c, "ozgemm_tc_persistent");
+  }
+  return THC_OK;
+}
+
+int launch_persistent_lv(Ctx* c, const OzArgs& g, int* err_flag, int group_m)
+{
+  switch (g.levels) {
+    case 2: return launch_persistent<2>(c, g, err_flag, group_m);
+    case 3: return launch_persistent<3>(c, g, err_flag, group_m);
+    case 4: return launch_persistent<4>(c, g, err_flag, group_m);
+    case 5: return launch_persistent<5>(c, g, err_flag, group_m);
+    case 6: return launch_persistent<6>(c, g, err_flag, group_m);
+    default: return set_error(c, THC_ERR_ARG, "ozgemm_tc: levels must be 2..6");
+  }
+}
+
 int launch_choice(Ctx* c, const OzArgs& g_in, int* err_flag, const TcChoice& ch)
 {
   OzArgs g = g_in;
   g.ksplit = ch.ksplit;
   if (g.ksplit <= 1) { g.ksplit = 1; g.part = nullptr; }
+  if (ch.persistent) return launch_persistent_lv(c, g, err_flag, ch.group_m);
   if (ch.bn == 64) return launch_bk<16, 64>(c, g, err_flag, ch.group_m);
   return ch.bk == 32 ? launch_bk<32, 128>(c, g, err_flag, ch.group_m)
                      : launch_bk<16, 128>(c, g, err_flag, ch.group_m);
@@ -838,9 +1238,10 @@ std::string ozgemm_tune_log(int device)
     const TuneEntry& e = kv.second;
     snprintf(buf, sizeof(buf),
              "M<=2^%lld N<=2^%lld K<=2^%lld slices=%lld epi=%lld lower=%lld split<=%lld: bk=%d "
-             "bn=%d group_m=%d split=%d %.1fus (%d tried)\n",
+             "bn=%d%s group_m=%d split=%d %.1fus (%d tried)\n",
              k[1], k[2], k[3], k[4], k[5], k[6], k[7], e.choice.bk, e.choice.bn,
-             e.choice.group_m, e.choice.ksplit, e.us, e.candidates);
+             e.choice.persistent ? " persistent" : "", e.choice.group_m, e.choice.ksplit, e.us,
+             e.candidates);
     out += buf;
   }
   return out;
@@ -857,6 +1258,11 @@ int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
   TcChoice dflt;
   dflt.bk = c->tc_bn == 64 ? 16 : c->tc_bk;
   dflt.bn = c->tc_bn;
+  if (c->tc_persistent && persistent_ok(g)) {
+    dflt.bk = 16;
+    dflt.bn = 64;
+    dflt.persistent = 1;
+  }
   dflt.ksplit = g.ksplit;
   if (!c->autotune) return launch_choice(c, g, err_flag, dflt);
   const std::vector<long long> key = {c->device, ilog2c(g.M), ilog2c(g.N), ilog2c(g.K),
@@ -865,7 +1271,8 @@ int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
   auto it = g_tune.find(key);
   if (it != g_tune.end()) return launch_choice(c, g, err_flag, it->second.choice);
   // Candidates: 128-wide tiles with k-step 32 / 16, 64-wide tiles (k-step 16, two CTAs per
-  // SM), each with 8 / 16 m-tiles per group and the caller's split or half of it.  Products
+  // SM), each with 8 / 16 m-tiles per group and the caller's split or half of it, and the
+  // persistent kernel (8 / 16 m-tiles per group) where K <= 512 without a split.  Products
   // above ~10 ms of tensor work keep the default (their tiles fill the GPU many times over
   // and a trial run would cost more than any choice gains).
   const double work = (double)g.levels * (g.levels + 1) / 2 * 2.0 * g.M * g.N * g.K;
@@ -876,16 +1283,21 @@ int ozgemm_tc(Ctx* c, const OzArgs& g, int* err_flag)
     return launch_choice(c, g, err_flag, dflt);
   }
   std::vector<TcChoice> cands;
-  for (int v : {0, 1, 2})              // (bk, bn) = (32, 128), (16, 128), (16, 64)
+  // (bk, bn) = (32, 128), (16, 128), (16, 64), and the persistent kernel where K fits.
+  for (int v : {0, 1, 2, 3}) {
+    if (v == 3 && !persistent_ok(g)) continue;
     for (int gm : {8, 16})
       for (int sp : {g.ksplit, std::max(1, g.ksplit / 2)}) {
         TcChoice ch;
-        ch.bk = v == 0 ? 32 : 16; ch.bn = v == 2 ? 64 : 128; ch.group_m = gm; ch.ksplit = sp;
+        ch.bk = v == 0 ? 32 : 16; ch.bn = v >= 2 ? 64 : 128; ch.persistent = v == 3;
+        ch.group_m = gm; ch.ksplit = v == 3 ? 1 : sp;
         bool dup = false;
         for (const auto& x : cands)
-          dup |= x.bk == ch.bk && x.bn == ch.bn && x.group_m == gm && x.ksplit == sp;
+          dup |= x.bk == ch.bk && x.bn == ch.bn && x.persistent == ch.persistent &&
+                 x.group_m == gm && x.ksplit == ch.ksplit;
         if (!dup) cands.push_back(ch);
       }
+  }
   cudaEvent_t ea = nullptr, eb = nullptr;
   THC_CUDA(c, cudaEventCreate(&ea));
   THC_CUDA(c, cudaEventCreate(&eb));
