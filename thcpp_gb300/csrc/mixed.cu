@@ -360,7 +360,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
                            cs)))
       return st;
     THC_CUDA(c, cudaMemcpyAsync(hcs_p, cs, sizeof(CholStatus), cudaMemcpyDeviceToHost, fs));
-    if (fs != s) THC_CUDA(c, cudaEventRecord(c->ev_join, fs));
+    THC_CUDA(c, cudaEventRecord(c->ev_join, fs));
   }
   // Z = (Phi Phi_mu^T)^2 (N_g x N_mu) via the sliced GEMM: A = Phi sliced by grid point,
   // B = Phi_mu sliced by interpolating point; Z's rows are then K-contiguous for the solve.
@@ -382,8 +382,9 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
   // the A operand of Y^T = Z X^T with a shift (the columns scaled by T, exactly).
   const SliceBuf zs = slices(sb, eb, ng_pad, mu_kpad, sz);
   if ((st = oz_slice_rows_dw(c, zg, ng, nmu, nmu, zs, keq))) return st;
-  // Join C's factorisation.
-  THC_CUDA(c, cudaStreamSynchronize(fs));
+  // Join C's factorisation: the host waits for its status only (the P product and Z's
+  // slicing, queued behind it, keep the GPU busy meanwhile).
+  THC_CUDA(c, cudaEventSynchronize(c->ev_join));
   if (fs != s) THC_CUDA(c, cudaStreamWaitEvent(s, c->ev_join, 0));
   CholStatus hcs = *hcs_p;
   int chol_c_info = 0;
@@ -521,9 +522,10 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
                                                        f64fft ? sqd : nullptr, n_anti, sqn,
                                                        f64fft ? sqdn : nullptr, n_neg);
   THC_LAUNCHED(c, "coulomb_weights");
-  int h_anti = 0, h_neg = 0;
-  THC_CUDA(c, cudaMemcpyAsync(&h_anti, n_anti, sizeof(int), cudaMemcpyDeviceToHost, s));
-  THC_CUDA(c, cudaMemcpyAsync(&h_neg, n_neg, sizeof(int), cudaMemcpyDeviceToHost, s));
+  int* h_flags = (int*)c->pinned + 16;             // pinned: [0] n_anti, [1] n_neg
+  THC_CUDA(c, cudaMemcpyAsync(h_flags, n_anti, sizeof(int), cudaMemcpyDeviceToHost, s));
+  THC_CUDA(c, cudaMemcpyAsync(h_flags + 1, n_neg, sizeof(int), cudaMemcpyDeviceToHost, s));
+  THC_CUDA(c, cudaEventRecord(c->ev_fork, s));
   double* mre = Mw;
   double* xim = Mw + nn;
   double* mcx = Mw + 2 * nn;
@@ -549,7 +551,9 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
     return gemm(g);
   };
   if ((st = coulomb_product(sq, sqd, mre))) return st;
-  THC_CUDA(c, cudaStreamSynchronize(s));
+  // The host waits for the two counts only; the Coulomb product runs meanwhile.
+  THC_CUDA(c, cudaEventSynchronize(c->ev_fork));
+  const int h_anti = h_flags[0], h_neg = h_flags[1];
   int nb2 = (int)cdiv(nn, 256);
   if (h_neg > 0) {
     double* mneg = Cinv;                          // free once zeta is formed
