@@ -1084,7 +1084,6 @@ __global__ void __launch_bounds__(kSumThreads) km_sums(KmBufs b)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tq = warp / kSumWins, tw = warp % kSumWins;   // this warp's window task
   const int k = blockIdx.x;
-  const int nmu = b.nmu;
   const int s = b.start[k], n = b.total[k];
   if (threadIdx.x < 4) sm.acc[threadIdx.x] = 0.0;
   for (int base = 0; base < n; base += kSumCap) {
@@ -1229,14 +1228,13 @@ __global__ void __launch_bounds__(1024) km_normdiff_exact(KmBufs b)
   }
 }
 
-// Bounding boxes of the 256-point tiles of the binned order (for the pruned map_to_grid).
-// Bounding box of each 256-point tile of the binned order, from the FP32 coordinates.
+// Bounding box of each 256-point tile of the binned order, from the FP32 coordinates (for
+// the pruned map_to_grid).
 __global__ void km_tile_boxes(KmBufs b, float* box)
 {
   __shared__ float red[6][8];
   long long t = blockIdx.x * 256LL + threadIdx.x;
   bool valid = t < b.ng;
-  long long i = valid ? b.perm[t] : 0;
   float g[3] = {valid ? b.pf[t] : 0.f, valid ? b.pf[b.ng + t] : 0.f,
                 valid ? b.pf[2 * b.ng + t] : 0.f};
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;

@@ -152,23 +152,6 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar)
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
-{
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-}
-
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v)
 {
   uint32_t r[8];
@@ -180,21 +163,6 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v)
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
-{
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-      "%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
 // Error-free transformations in FP32 (Knuth's TwoSum; Dekker's FastTwoSum for |a| >= |b|).
@@ -259,7 +227,6 @@ struct TcCfg {
   static constexpr int NEXACT = LV < 3 ? LV : 3;          // exact level accumulators
   static constexpr int ECOLS = BN / 2;                    // columns per epilogue warp
   static constexpr int TMEM_COLS = 4 * BN;                // four accumulators
-  static constexpr int MIN_CTAS = BN == 128 ? 1 : 2;      // CTAs per SM
   // The stage buffers, reused after the main loop to stage the epilogue's 8 warps x 32 x
   // ECOLS 8-byte results; the barriers follow.
   static constexpr int EPI_BYTES = TEPI_WARPS * 32 * ECOLS * 8;
@@ -289,7 +256,7 @@ __device__ __noinline__ float wide_f32(float h, float l, int ex)
 }
 
 template <int LV, int BK, int BN>
-__global__ void __launch_bounds__(TTHREADS, (BN == 128 ? 1 : 2))
+__global__ void __launch_bounds__(TTHREADS, (BN == 128 ? 1 : 2))   // CTAs per SM
     ozgemm_tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
                      TcArgs g)
 {
@@ -716,7 +683,6 @@ struct TpCfg {
   static constexpr int STG_BYTES = TEPI_WARPS * 32 * EC * 8;  // epilogue staging
   static constexpr int STAGES_FIT = (kPersistBudget - STG_BYTES) / STAGE_BYTES;
   static constexpr int STAGES = STAGES_FIT < 4 ? STAGES_FIT : 4;
-  static constexpr int NEXACT = LV < 3 ? LV : 3;
   static constexpr int BUF_COLS = 4 * BN;                    // one buffer of accumulators
   // stage ring | staging | barriers (256 B) | exponents (8 warps x 32 ints) | guard
   static constexpr size_t SMEM =
