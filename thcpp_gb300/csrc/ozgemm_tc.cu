@@ -1002,7 +1002,9 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encoder()
   if (!fn) {
     cudaDriverEntryPointQueryResult q;
     void* p = nullptr;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+    // The entry point with the ABI of CUDA 12.0, which the PFN type above describes.
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
       fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
   }
