@@ -1,14 +1,16 @@
 """Accuracy report of one config against the blocked FP64 GPU oracle (test infrastructure).
 
     python -m tests.accuracy_report c5 [--refine K] [--prec mixed|fp64] [--pairs 512]
+                                       [--slices P,Z,M]
 
 Runs the library's k-means and ISDF on the config exactly as bench.py does (the 216-atom
 cell generated on the GPU, its C solved with the shift 1e-10 tr(C)/N_mu and refinement),
 keeps the interpolating vectors, frees the library's workspace, then runs
 oracle/isdf_torch.py on the same points with the same shift and refinement steps and
 prints one JSON line: relative Frobenius errors of M and zeta, the ISDF reconstruction error
-of sampled orbital-pair densities for both, cond(C), and the device memory the library
-used.
+of sampled orbital-pair densities for both, cond(C), the device memory the library used and
+the device time of the ISDF call (the second of two, so that the autotuner's trials are not
+in it).  --slices sets the slice depths of the P, zeta and Coulomb products (mixed path).
 """
 import argparse
 import json
@@ -32,6 +34,7 @@ def main():
     ap.add_argument("--refine", type=int, default=None)
     ap.add_argument("--prec", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--pairs", type=int, default=512)
+    ap.add_argument("--slices", default=None, help="P,Z,M slice depths (2..6)")
     a = ap.parse_args()
     build.build()
     dev = torch.device("cuda", 0)
@@ -53,6 +56,12 @@ def main():
     with capi.Context(0, prec) as ctx:
         ctx.kmeans(grid, rho, s.nmu, init, s.max_it, s.threshold, out_idx=idx)
         ctx.set_option("refine", refine)
+        slices = None
+        if a.slices:
+            slices = [int(x) for x in a.slices.split(",")]
+            for key, v in zip(("slices_p", "slices_z", "slices_m"), slices):
+                ctx.set_option(key, v)
+        ctx.isdf(phi, idx, s.mesh, coul, shift_rel)
         r = ctx.isdf(phi, idx, s.mesh, coul, shift_rel)
         torch.cuda.synchronize()
         used_gb = (free0 - torch.cuda.mem_get_info()[0]) / 1e9
@@ -75,7 +84,8 @@ def main():
            else None, "shift_used": st.shift_used, "refine_steps": refine,
            "rel_err_M": em, "rel_err_zeta": ez, "pair_density_err": ep,
            "pair_density_err_oracle": ep_ref, "pairs_sampled": int(len(pairs)),
-           "library_device_memory_gb": round(used_gb, 2), "wall_s": round(time.time() - t0, 1)}
+           "library_device_memory_gb": round(used_gb, 2), "slices": slices,
+           "isdf_device_ms": round(float(st.device_ms), 3), "wall_s": round(time.time() - t0, 1)}
     print(json.dumps(out), flush=True)
 
 
