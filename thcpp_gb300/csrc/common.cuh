@@ -85,7 +85,12 @@ struct Ctx {
   size_t ws_bytes[WS_NSLOTS] = {};
   std::map<std::tuple<int, int, int, int, int>, cufftHandle> plans;  // (n0,n1,n2,batch,type)
   std::map<std::tuple<int, int, int, int, int>, size_t> plan_work;   // their work-area bytes
-  void* pinned = nullptr;          // 4 KB pinned host scratch
+  // 4 KB pinned host scratch for asynchronous device-to-host flags.  Users (never live at
+  // the same time within one call): bytes [0, 32) the k-means done flags of two blocks in
+  // flight (kmeans.cu) or the CholStatus of C (mixed.cu); bytes [kPinnedCounts, +8) the
+  // Coulomb kernel's two counts (mixed.cu).
+  void* pinned = nullptr;
+  static constexpr size_t kPinnedCounts = 64;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ev_check[2] = {nullptr, nullptr};   // k-means convergence checks in flight
   long long launches = 0;

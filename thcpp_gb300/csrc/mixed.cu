@@ -522,7 +522,7 @@ int isdf_run_mixed(Ctx* c, const double* phi_in, long long ng, int no, const int
                                                        f64fft ? sqd : nullptr, n_anti, sqn,
                                                        f64fft ? sqdn : nullptr, n_neg);
   THC_LAUNCHED(c, "coulomb_weights");
-  int* h_flags = (int*)c->pinned + 16;             // pinned: [0] n_anti, [1] n_neg
+  int* h_flags = (int*)((char*)c->pinned + Ctx::kPinnedCounts);   // [0] n_anti, [1] n_neg
   THC_CUDA(c, cudaMemcpyAsync(h_flags, n_anti, sizeof(int), cudaMemcpyDeviceToHost, s));
   THC_CUDA(c, cudaMemcpyAsync(h_flags + 1, n_neg, sizeof(int), cudaMemcpyDeviceToHost, s));
   THC_CUDA(c, cudaEventRecord(c->ev_fork, s));
