@@ -51,6 +51,27 @@ CONFIG = dict(WORKLOADS[WORKLOAD], kmeans_max_it=100, kmeans_threshold=1e-6,
 METRIC = "ISDF s/system on 1 GB300 (mixed precision; FP64 path reported beside)"
 
 
+def sliced_gemm_flops(ng, no, nmu, mesh, shifted, refine, slices=(6, 6, 5)):
+    """Algorithmic tensor-pipe work of one mixed factorisation: the sum over its sliced
+    GEMMs of (slice pairs) x 2 M N K.  P = Phi Phi_mu^T and the Coulomb product (its lower
+    half, K = 2 N_c over the half spectrum, Nyquist planes included) always; the solve is
+    zeta^T = C^{-1} Z^T with C^{-1} = X^T X formed by a sliced product from N_mu = 512 on
+    (the library's threshold), or, with a shift, two products (Y^T = Z (P X)^T, then
+    zeta^T = X^T Y) plus refinement's G = X X^T and one N_mu^3 product per step."""
+    sp, sz, sm = slices
+    pairs = lambda L: L * (L + 1) // 2
+    n0, n1, n2 = mesh
+    nc2 = 2 * n0 * n1 * (n2 // 2 + 1)
+    flops = (pairs(sp) * 2 * nmu * ng * no + pairs(sz) * 2 * nmu * ng * nmu
+             + pairs(sm) * 2 * nmu * nmu * nc2 / 2)
+    if shifted:
+        flops += pairs(sz) * 2 * nmu * ng * nmu + (
+            pairs(sz) * 2 * nmu ** 3 * (1 + refine) if refine > 0 else 0)
+    elif nmu >= 512:
+        flops += pairs(sz) * 2 * nmu ** 3
+    return flops
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -479,23 +500,8 @@ def main():
             peaks = _json.load(open(pk))
         bf16_peak = peaks.get("bf16_tflops", 1900.0)
         peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
-        # Dominant tensor kernel: the sliced GEMMs.  Algorithmic tensor-pipe work per
-        # factorisation = sum over the three GEMMs of (slice pairs) x 2 M N K.
-        sp, sz, sm = 6, 6, 5
-        pairs = lambda L: L * (L + 1) // 2
-        n0, n1, n2 = s.mesh
-        nc2 = 2 * n0 * n1 * (n2 // 2 + 1)
-        # P, zeta and M; without a shift also C^{-1} = X^T X from N_mu = 512 on (the
-        # library's threshold); with a shift the solve is two products (Y^T = Z (P X)^T, then
-        # zeta^T = X^T Y) and refinement adds G = X X^T and one N_mu^3 product per step.
-        shifted = bool(isdf_st.rank_deficient)
-        flops = (pairs(sp) * 2 * nmu * ng * no + pairs(sz) * 2 * nmu * ng * nmu
-                 + pairs(sm) * 2 * nmu * nmu * nc2 / 2)
-        if shifted:
-            flops += pairs(sz) * 2 * nmu * ng * nmu + (
-                pairs(sz) * 2 * nmu ** 3 * (1 + refine) if refine > 0 else 0)
-        elif nmu >= 512:
-            flops += pairs(sz) * 2 * nmu ** 3
+        # Dominant tensor kernel: the sliced GEMMs.
+        flops = sliced_gemm_flops(ng, no, nmu, s.mesh, bool(isdf_st.rank_deficient), refine)
         # Aggregate over the timed launches: all their flops over all their time.
         achieved = flops * args.steps / (oz_ms * 1e-3) / 1e12 if oz_n else None
         roof = {"kernel": "ozgemm (sliced-BF16 tensor GEMMs of a factorisation, aggregate)",
