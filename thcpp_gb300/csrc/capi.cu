@@ -191,6 +191,8 @@ int thc_ctx_create(int device, int precision, thc_ctx** out)
       cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_panel, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_trail, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_check[0], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_check[1], cudaEventDisableTiming) != cudaSuccess ||
@@ -234,6 +236,8 @@ int thc_ctx_destroy(thc_ctx* h)
     if (e) cudaEventDestroy(e);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->ev_panel) cudaEventDestroy(c->ev_panel);
+  if (c->ev_trail) cudaEventDestroy(c->ev_trail);
   if (c->aux_stream) {
     cudaStreamSynchronize(c->aux_stream);
     cudaStreamDestroy(c->aux_stream);

@@ -80,6 +80,7 @@ struct Ctx {
   // P product's CTAs fill every SM, so the overlap measured no gain at N_g 1.1e5.
   cudaStream_t aux_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_panel = nullptr, ev_trail = nullptr;   // Cholesky look-ahead (dense64.cu)
   int overlap = 0;
   void* ws[WS_NSLOTS] = {};
   size_t ws_bytes[WS_NSLOTS] = {};

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
   constexpr int LOADS = BK * T / 256;
   if (g.skip_flag && *g.skip_flag) return;
   long long m0 = (long long)blockIdx.y * T, n0 = (long long)blockIdx.x * T;
-  if (g.lower_only && n0 > m0 + T - 1) return;
+  if (g.lower_only && n0 > m0 + T - 1 + g.lower_offset) return;
   __shared__ double As[BK][T + 1];
   __shared__ double Bs[BK][T + 1];
   int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) dgemm_kernel(GemmArgs g)
     for (int j = 0; j < R; j++) {
       long long n = n0 + tx + 16 * j;
       if (n >= g.N) continue;
-      if (g.lower_only && n > m) continue;
+      if (g.lower_only && n > m + g.lower_offset) continue;
       double v = acc[i][j];
       if (g.ksplit > 1) {
         g.part[((long long)blockIdx.z * g.M + m) * g.N + n] = v;
@@ -110,7 +110,7 @@ __global__ void dgemm_reduce(GemmArgs g)
   long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e >= g.M * g.N) return;
   long long m = e / g.N, n = e % g.N;
-  if (g.lower_only && n > m) return;
+  if (g.lower_only && n > m + g.lower_offset) return;
   double v = 0.0;
   for (int z = 0; z < g.ksplit; z++) v += g.part[((long long)z * g.M + m) * g.N + n];
   double* cp = g.C + m * g.ldc + n;
@@ -367,6 +367,10 @@ int dgemm(Ctx* c, const GemmArgs& g_in)
     g.tile = tiles(64) >= want / 2 ? 64 : (tiles(32) >= want / 2 ? 32 : 16);
     long long split = std::min<long long>(cdiv(want, tiles(g.tile)), std::max(1, g.K / 32));
     if (g.aliased) split = std::max<long long>(split, 2);
+    if (g.no_split) {
+      if (g.aliased) return set_error(c, THC_ERR_ARG, "dgemm: aliased operands need a split");
+      split = 1;
+    }
     g.ksplit = (int)std::max<long long>(1, std::min<long long>(split, cdiv(g.K, BK)));
     if (g.ksplit > 1) {
       g.part = (double*)ws_get(c, WS_DPART, sizeof(double) * g.ksplit * g.M * g.N);
@@ -395,6 +399,14 @@ int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholSta
   ProfScope prof(c, "potrf_inv");
   cudaStream_t s = c->stream;
   const int NB = chol_nb(n);
+  // Look-ahead (n >= 512, with the context's second stream): after block k's panel, the
+  // next diagonal block is updated first, on the main stream, and factored there while the
+  // rest of block k's trailing update runs on the second stream; the next panel waits for
+  // that update.  The diagonal blocks' one-SM chain then runs beside the FP64 GEMMs on the
+  // other SMs instead of between them.
+  const bool la = n >= 512 && c->aux_stream && c->aux_stream != s;
+  cudaStream_t s2 = la ? c->aux_stream : s;
+  bool trail_pending = false;
   for (int k0 = 0; k0 < n; k0 += NB) {
     int nb = std::min(NB, n - k0);
     double* di = dinv + (long long)(k0 / NB) * NB * NB;
@@ -409,6 +421,10 @@ int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholSta
     THC_LAUNCHED(c, "potrf_diag_inv");
     int rest = n - k0 - nb;
     if (rest <= 0) break;
+    if (trail_pending) {     // the panel rows below were updated on the second stream
+      THC_CUDA(c, cudaStreamWaitEvent(s, c->ev_trail, 0));
+      trail_pending = false;
+    }
     {
       // L_panel = A_panel L_kk^{-T}, in place (each CTA owns its rows; N = nb <= 64).
       GemmArgs g{};
@@ -421,16 +437,56 @@ int potrf_inv(Ctx* c, double* A, long long ld, int n, const double* thr, CholSta
       int st = dgemm(c, g);
       if (st) return st;
     }
-    GemmArgs g{};
-    g.M = rest; g.N = rest; g.K = nb;
-    g.A = A + (long long)(k0 + nb) * ld + k0; g.sam = ld; g.sak = 1;
-    g.B = A + (long long)(k0 + nb) * ld + k0; g.sbn = ld; g.sbk = 1;
-    g.C = A + (long long)(k0 + nb) * ld + k0 + nb; g.ldc = ld;
-    g.alpha = -1.0; g.beta = 1.0; g.lower_only = 1; g.mode = GEMM_STORE;
-    g.skip_flag = &cs->flag;
-    int st = dgemm(c, g);
-    if (st) return st;
+    const double* l21 = A + (long long)(k0 + nb) * ld + k0;
+    if (!la) {
+      GemmArgs g{};
+      g.M = rest; g.N = rest; g.K = nb;
+      g.A = l21; g.sam = ld; g.sak = 1;
+      g.B = l21; g.sbn = ld; g.sbk = 1;
+      g.C = A + (long long)(k0 + nb) * ld + k0 + nb; g.ldc = ld;
+      g.alpha = -1.0; g.beta = 1.0; g.lower_only = 1; g.mode = GEMM_STORE;
+      g.skip_flag = &cs->flag;
+      int st = dgemm(c, g);
+      if (st) return st;
+      continue;
+    }
+    const int nb1 = std::min(NB, rest);
+    {
+      // The next diagonal block first (rows and columns k0 + nb .. k0 + nb + nb1).
+      GemmArgs g{};
+      g.M = nb1; g.N = nb1; g.K = nb;
+      g.A = l21; g.sam = ld; g.sak = 1;
+      g.B = l21; g.sbn = ld; g.sbk = 1;
+      g.C = A + (long long)(k0 + nb) * ld + k0 + nb; g.ldc = ld;
+      g.alpha = -1.0; g.beta = 1.0; g.lower_only = 1; g.mode = GEMM_STORE;
+      g.skip_flag = &cs->flag;
+      int st = dgemm(c, g);
+      if (st) return st;
+    }
+    if (rest > nb1) {
+      // The rest of the trailing triangle (rows below the next diagonal block, columns from
+      // it on) on the second stream, after the panel.
+      THC_CUDA(c, cudaEventRecord(c->ev_panel, s));
+      THC_CUDA(c, cudaStreamWaitEvent(s2, c->ev_panel, 0));
+      GemmArgs g{};
+      g.M = rest - nb1; g.N = rest; g.K = nb;
+      g.A = l21 + (long long)nb1 * ld; g.sam = ld; g.sak = 1;
+      g.B = l21; g.sbn = ld; g.sbk = 1;
+      g.C = A + (long long)(k0 + nb + nb1) * ld + k0 + nb; g.ldc = ld;
+      g.alpha = -1.0; g.beta = 1.0; g.lower_only = 1; g.lower_offset = nb1;
+      g.mode = GEMM_STORE; g.no_split = 1;
+      g.skip_flag = &cs->flag;
+      int st;
+      {
+        StreamSwap on_s2(c, s2);
+        st = dgemm(c, g);
+      }
+      if (st) return st;
+      THC_CUDA(c, cudaEventRecord(c->ev_trail, s2));
+      trail_pending = true;
+    }
   }
+  if (trail_pending) THC_CUDA(c, cudaStreamWaitEvent(s, c->ev_trail, 0));
   return THC_OK;
 }
 

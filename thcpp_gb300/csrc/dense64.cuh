@@ -33,6 +33,9 @@ struct GemmArgs {
   // then starts its k loop at its first row / column: the skipped terms are exact zeros,
   // so the result is bit-identical.
   int a_zero_below = 0, b_zero_below = 0;
+  int lower_offset = 0;              // lower_only keeps n <= m + lower_offset (C's own indices)
+  int no_split = 0;                  // no split of K (no shared partial buffer: a GEMM that
+                                     // runs beside others on a second stream)
   int tile = 64;                     // CTA tile edge (64, 32 or 16; chosen by dgemm)
 };
 
