@@ -116,7 +116,10 @@ int thc_ctx_set_stream(thc_ctx* ctx, void* cuda_stream);
  * solve of C, 0..8, default 0); "equilibrate" (mixed path: solve on C scaled to a unit-range
  * diagonal by powers of two, default 1); "overlap" (mixed path: factor C on a second stream
  * beside the P product, default 0); "spin_limit" (polls before a bounded device wait gives
- * up with THC_ERR_TIMEOUT, default 2^24). */
+ * up with THC_ERR_TIMEOUT, default 2^24); "tc_hi" (drain period of the tensor-core kernel's
+ * level >= 3 accumulator in 16-k steps, a power of two 1..32, default 8); "qrcp_all_pairs"
+ * (half-rotated QRCP: 1 = every (occupied, orbital) pair instead of the reference's
+ * overlapping row layout, default 0). */
 int thc_ctx_set_option(thc_ctx* ctx, const char* key, double value);
 /* Accumulated device time (ms, from the profile events) and launch count of the kernels
  * named `kernel` since profiling was enabled; synchronises the context's stream. */
