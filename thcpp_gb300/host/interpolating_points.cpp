@@ -17,18 +17,16 @@ IPoints::IPoints(nlohmann::json& input, ContextHandler::BlacsHandler& BH)
   std::cout << "##   Setting up interpolating point solver.    ##" << std::endl;
   std::cout << "#################################################" << std::endl;
   std::cout << std::endl;
-  nlohmann::json base = input.at("interpolating_points");
-  try {
-    nlohmann::json kmeans_dict = base.at("kmeans");
+  // The reference's key precedence: a "kmeans" block wins over a "qrcp" block, and with
+  // neither the k-means solver runs after a note.
+  const nlohmann::json& base = input.at("interpolating_points");
+  if (base.contains("kmeans")) {
     solver = "kmeans";
-  } catch (nlohmann::json::out_of_range& error) {
-    try {
-      nlohmann::json qrcp = base.at("qrcp");
-      solver = "qrcp";
-    } catch (nlohmann::json::out_of_range& error) {
-      std::cout << "No solver specified." << std::endl;
-      solver = "kmeans";
-    }
+  } else if (base.contains("qrcp")) {
+    solver = "qrcp";
+  } else {
+    std::cout << "No solver specified." << std::endl;
+    solver = "kmeans";
   }
 }
 
